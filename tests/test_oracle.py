@@ -1,0 +1,79 @@
+"""The oracle pinned by known answers: dense exp(-iHt) on full-rank trees, the
+uncoupled spin, conservation laws and the Householder conventions."""
+import numpy as np
+import pytest
+import scipy.linalg as sla
+
+from helpers import generic_state, random_sop, random_tree
+from oracle.oracle import Oracle, qr
+from ttns_lib_gb300 import spin_boson as sb
+from ttns_lib_gb300.model import full_state
+
+
+def test_full_rank_spin_boson_matches_dense_expm():
+    m = sb.build(N=4, alpha=0.5, wc=5.0, d=3, chi=9, eps=0.3, delta=1.0)
+    topo = m.topology
+    st = sb.initial_state_numpy(topo, seed=1, psi0=np.array([1, 0]))
+    psi = full_state(topo, st)
+    H = m.sop.dense()
+    orc = Oracle(topo, m.sop, krylov_dim=12, krylov_tol=1e-12)
+    orc.set_state(st)
+    dt = 0.05
+    for k in range(12):
+        orc.step(dt)
+        ex = sla.expm(-1j * H * (k + 1) * dt) @ psi
+        got = full_state(topo, orc.get_state())
+        assert np.linalg.norm(got - ex) < 1e-11
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_random_tree_random_sop_matches_dense_expm(seed):
+    rng = np.random.default_rng(100 + seed)
+    dims = [int(x) for x in rng.integers(2, 4, size=5)]
+    topo = random_tree(rng, dims)
+    H = random_sop(rng, dims, nterms=10)
+    st = generic_state(topo, rng)
+    psi = full_state(topo, st)
+    Hd = H.dense()
+    orc = Oracle(topo, H, krylov_dim=10, krylov_tol=1e-12)
+    orc.set_state(st)
+    for k in range(5):
+        orc.step(0.1)
+        ex = sla.expm(-1j * Hd * (k + 1) * 0.1) @ psi
+        got = full_state(topo, orc.get_state())
+        assert np.linalg.norm(got - ex) < 1e-10
+
+
+def test_uncoupled_spin_precesses():
+    m = sb.build(N=4, alpha=0.0, wc=5.0, d=4, chi=4, eps=0.0, delta=1.0)
+    orc = Oracle(m.topology, m.sop, krylov_dim=8)
+    orc.set_state(sb.initial_state_numpy(m.topology, seed=0, psi0=np.array([1, 0])))
+    for k in range(20):
+        orc.step(0.05)
+        t = (k + 1) * 0.05
+        assert abs(orc.expect(0, sb.SZ).real - np.cos(t)) < 1e-11
+
+
+def test_norm_and_energy_conserved_truncated():
+    m, cfg = sb.build_config("c1")
+    orc = Oracle(m.topology, m.sop, krylov_dim=cfg["krylov_dim"])
+    st = sb.initial_state_numpy(m.topology, seed=0, psi0=np.array([1, 0]))
+    orc.set_state(st)
+    for _ in range(5):
+        orc.step(cfg["dt"])
+        assert abs(orc.norm2() - 1.0) < 1e-11
+
+
+def test_householder_conventions():
+    rng = np.random.default_rng(0)
+    a = rng.normal(size=(9, 4)) + 1j * rng.normal(size=(9, 4))
+    q, r = qr(a)
+    assert np.allclose(q @ r, a, atol=1e-13)
+    assert np.allclose(q.conj().T @ q, np.eye(4), atol=1e-13)
+    assert np.allclose(np.tril(r, -1), 0)
+    # exact zeros give tau = 0: Q columns are unit vectors, R keeps alpha
+    z = np.zeros((6, 3), dtype=np.complex128)
+    z[0, 0] = 1.0
+    q, r = qr(z)
+    assert np.array_equal(q, np.eye(6, 3))
+    assert r[0, 0] == 1.0

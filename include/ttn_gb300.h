@@ -1,0 +1,142 @@
+/* ttn_gb300.h -- C-ABI of the GB300-native one-site projector-splitting TDVP sweep.
+ *
+ * The entry points replace the objects a caller of ttns_lib builds around the sweep
+ * (paths are relative to the ttns_lib project root):
+ *
+ *   ttn_tree_*        <- ntree<size_t> topology + httensor(topology, capacity)
+ *                        include/ttns_lib/httensor.hpp:51, :129-288
+ *   ttn_sop_*         <- sop_operator<T>(nterms, mode_dims), bind(op, r, mode), coeff(r)
+ *                        include/ttns_lib/operators/sop_operator.hpp:262, :323-392, :471-473
+ *   ttn_state_*       <- the httensor node matrices A[i]().as_matrix()
+ *                        include/ttns_lib/ttn_nodes/httensor_node.hpp:150-153
+ *   ttn_integrator_*  <- fixed_step_projector_splitting_integrator<T>
+ *                        include/ttns_lib/integrators/projector_splitting_integrator.hpp:76-218
+ *                        (initialise :115-129, operator() :136-169, dt() :187-188,
+ *                         nh_applications() :190)
+ *   ttn_expect_leaf / ttn_norm2
+ *                     <- matrix_element::operator()(op, mode, psi) and operator()(psi)
+ *                        include/ttns_lib/observables/matrix_element.hpp:153-187, :264-314
+ *
+ * Conventions
+ *   * complex numbers are interleaved double pairs (re, im);
+ *   * a node matrix is row-major (dimen x hrank) with the children's indices in child
+ *     order, the last child fastest, exactly the reference's as_matrix() layout;
+ *   * nodes are numbered in pre-order (parent[0] = -1, parent[i] < i) and the
+ *     children of a node are ordered by id;
+ *   * every call returns TTN_OK or an error code; ttn_last_error() gives the message
+ *     of the last failure on the calling thread.  No C++ exception crosses the ABI.
+ *   * objects are not thread-safe; use one integrator per host thread.  Each
+ *     integrator owns its CUDA stream and device workspaces.
+ */
+#ifndef TTN_GB300_H
+#define TTN_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  TTN_OK = 0,
+  TTN_EINVAL = 1,     /* bad argument or ill-formed tree / operator */
+  TTN_ECAPACITY = 2,  /* a size exceeds an allocated capacity */
+  TTN_ENUMERIC = 3,   /* non-finite values or a failed Krylov / eigen solve */
+  TTN_ECUDA = 4,      /* a CUDA runtime call failed */
+  TTN_ETIMEOUT = 5,   /* a bounded device-side wait gave up */
+  TTN_ENOTSUP = 6     /* valid request outside what this build implements */
+};
+
+/* precision of the contractions in the sweep */
+enum { TTN_PREC_FP64 = 0, TTN_PREC_MIXED = 1 };
+
+typedef struct ttn_tree ttn_tree;
+typedef struct ttn_sop ttn_sop;
+typedef struct ttn_state ttn_state;
+typedef struct ttn_integrator ttn_integrator;
+
+typedef struct ttn_integ_cfg {
+  int krylov_dim;          /* Lanczos dimension m (reference default 4; driver default 6) */
+  double krylov_tol;       /* local error tolerance of the exponential (reference 1e-12) */
+  int precision;           /* TTN_PREC_FP64 or TTN_PREC_MIXED */
+  int device;              /* CUDA device ordinal */
+} ttn_integ_cfg;
+
+const char* ttn_last_error(void);
+const char* ttn_version(void);
+
+/* ---- tree ---------------------------------------------------------------------- */
+/* parent[nnodes] (pre-order), hrank[nnodes]; leaf_mode[i] >= 0 and leaf_dim[i] > 0 on
+ * leaves, -1 / 0 on branch nodes.  hrank must not exceed the product of the node's
+ * child dimensions (ntree_builder::sanitise_tree, include/ttns_lib/tree/ntree_builder.hpp:215-233). */
+int ttn_tree_create(int nnodes, const int* parent, const int* hrank, const int* leaf_mode,
+                    const int* leaf_dim, ttn_tree** out);
+int ttn_tree_destroy(ttn_tree* t);
+int ttn_tree_num_nodes(const ttn_tree* t, int* out);
+int ttn_tree_node_shape(const ttn_tree* t, int node, long long* dimen, int* hrank);
+int ttn_tree_state_size(const ttn_tree* t, long long* n_complex);
+
+/* ---- sum-of-product operator --------------------------------------------------- */
+int ttn_sop_create(int nterms, int nmodes, const int* mode_dims, ttn_sop** out);
+int ttn_sop_destroy(ttn_sop* s);
+/* bind one operator on `mode` to the terms r[0..nr) (sop_operator::bind) */
+int ttn_sop_bind_dense(ttn_sop* s, int mode, const double* mat, const int* r, int nr);
+int ttn_sop_bind_diag(ttn_sop* s, int mode, const double* diag, const int* r, int nr);
+int ttn_sop_bind_csr(ttn_sop* s, int mode, const int* rowptr, const int* colind,
+                     const double* vals, const int* r, int nr);
+int ttn_sop_set_coeff(ttn_sop* s, int r, double re, double im);
+
+/* ---- state (device resident) ---------------------------------------------------- */
+int ttn_state_create(const ttn_tree* t, int device, ttn_state** out);
+int ttn_state_destroy(ttn_state* s);
+/* host <-> device copies of the node matrices; `data` holds all nodes concatenated
+ * in node order (ttn_tree_state_size complex numbers) */
+int ttn_state_upload(ttn_state* s, const double* data);
+int ttn_state_download(ttn_state* s, double* data);
+int ttn_state_upload_node(ttn_state* s, int node, const double* data);
+int ttn_state_download_node(ttn_state* s, int node, double* data);
+/* The spin-boson driver's start state (src/spin_boson.cpp:584-649): leaf SPF 0 is psi0
+ * on mode 0 and the vacuum elsewhere, the other leaf SPFs are random orthonormal
+ * vectors drawn with std::mt19937(seed), interior nodes are identities and the root
+ * is e_0.  Generated on the host, then uploaded.  psi0 may be NULL (vacuum). */
+int ttn_state_init_product(ttn_state* s, const double* psi0, unsigned int seed);
+
+/* ---- integrator ---------------------------------------------------------------- */
+int ttn_integrator_create(const ttn_tree* t, const ttn_sop* h, const ttn_integ_cfg* cfg,
+                          ttn_integrator** out);
+int ttn_integrator_destroy(ttn_integrator* it);
+int ttn_integrator_set_dt(ttn_integrator* it, double dt);
+int ttn_integrator_dt(const ttn_integrator* it, double* out);
+int ttn_integrator_t(const ttn_integrator* it, double* out);
+/* One call = one step of dt of exp(coeff * H t) (coeff = -i for Schroedinger
+ * dynamics); the first call prepares the environments and sub-steps dt as
+ * dt*1e-5, dt*1e-4, ... exactly as the reference integrator does. */
+int ttn_integrator_step(ttn_integrator* it, ttn_state* psi, double coeff_re, double coeff_im,
+                        double* dt_out);
+int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out);
+int ttn_integrator_reset(ttn_integrator* it);
+/* wait for all queued device work of this integrator */
+int ttn_integrator_synchronize(ttn_integrator* it);
+
+/* ---- observables ----------------------------------------------------------------- */
+/* <psi| O_mode |psi> with a dense d x d operator on one leaf mode */
+int ttn_expect_leaf(ttn_integrator* it, ttn_state* psi, int mode, const double* op, double* re,
+                    double* im);
+int ttn_norm2(ttn_integrator* it, ttn_state* psi, double* out);
+
+/* ---- kernel-level entry points (parity checks and benchmarks) -------------------- */
+/* recompute every environment for the current node tensors, without gauge moves */
+int ttn_debug_refresh_env(ttn_integrator* it, ttn_state* psi);
+/* out = H_eff(node) v with the current environments; v, out are host buffers */
+int ttn_debug_heff(ttn_integrator* it, int node, const double* v, double* out);
+/* v <- exp(coeff * tau * H_eff(node)) v; returns the number of H applications */
+int ttn_debug_expm_node(ttn_integrator* it, int node, double tau, double cre, double cim,
+                        double* v, long long* napps);
+/* environment matrix of one node group (which: 0 spf, 1 mean field) */
+int ttn_debug_num_groups(ttn_integrator* it, int node, int* out);
+int ttn_debug_get_env(ttn_integrator* it, int node, int group, int which, double* out);
+/* Householder QR of an m x n row-major matrix on the device: a <- Q, r <- R */
+int ttn_debug_qr(int m, int n, double* a, double* r, int device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

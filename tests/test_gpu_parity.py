@@ -1,0 +1,181 @@
+"""Device path vs the CPU oracle on the same inputs (GB300 only).
+
+Tolerances: the plain form is complex128 throughout, so kernel-level results agree to
+rounding (relative 1e-12) and sweeps from well-conditioned states agree to 1e-10.
+Runs that start from the rank-1 product state are compared against the oracle's own
+spread under rounding-level perturbations (see test_product_state_within_envelope)."""
+import copy
+
+import numpy as np
+import pytest
+import scipy.linalg as sla
+
+from helpers import generic_state, random_sop, random_tree
+from oracle.oracle import Oracle, qr as oracle_qr
+from ttns_lib_gb300 import api
+from ttns_lib_gb300 import spin_boson as sb
+from ttns_lib_gb300.model import full_state
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def make_pair(topo, sop, state, m=12, tol=1e-12):
+    orc = Oracle(topo, sop, krylov_dim=m, krylov_tol=tol)
+    orc.set_state(state)
+    A = api.httensor(topo)
+    A.set(state)
+    dev = api.fixed_step_projector_splitting_integrator(A, sop, krylov_dim=m, krylov_tolerance=tol)
+    return orc, A, dev
+
+
+@pytest.mark.parametrize("shape", [(9, 4), (64, 8), (256, 16), (4096, 64), (130, 33)])
+def test_device_qr_matches_oracle(shape):
+    rng = np.random.default_rng(shape[0])
+    a = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+    qd, rd = api.device_qr(a)
+    qo, ro = oracle_qr(a)
+    assert rel(qd, qo) < 1e-12 and rel(rd, ro) < 1e-12
+    assert np.allclose(qd @ rd, a, atol=1e-12 * np.abs(a).max() * shape[0])
+
+
+def test_device_qr_rank_deficient_exact_zeros():
+    z = np.zeros((40, 6), dtype=np.complex128)
+    z[7, 0] = 1.0
+    z[3, 2] = -2.0 + 1j
+    qd, rd = api.device_qr(z)
+    qo, ro = oracle_qr(z)
+    assert np.array_equal(qd, qo) and np.array_equal(rd, ro)
+
+
+def spin_boson_small():
+    m, cfg = sb.build_config("c1")
+    return m, cfg
+
+
+def test_environments_and_heff_match_oracle():
+    m, cfg = spin_boson_small()
+    topo = m.topology
+    st = generic_state(topo, np.random.default_rng(1))
+    orc, A, dev = make_pair(topo, m.sop, st, m=cfg["krylov_dim"])
+    orc.refresh_env()
+    dev.refresh_env(A)
+    rng = np.random.default_rng(2)
+    for node in range(topo.nnodes):
+        groups = orc.groups(node)
+        assert dev.num_groups(node) == len(groups)
+        for g, info in enumerate(groups):
+            if node != 0 and not info["id_spf"]:
+                assert rel(dev.env(node, g, "spf"), orc.env(node, g, "spf")) < 1e-12
+            if node != 0 and not info["id_mf"]:
+                assert rel(dev.env(node, g, "mf"), orc.env(node, g, "mf")) < 1e-12
+        v = rng.normal(size=topo.node_shape(node)) + 1j * rng.normal(size=topo.node_shape(node))
+        assert rel(dev.heff(node, v), orc.heff(node, v)) < 1e-12
+
+
+def test_expm_node_matches_oracle():
+    m, cfg = spin_boson_small()
+    topo = m.topology
+    st = generic_state(topo, np.random.default_rng(3))
+    orc, A, dev = make_pair(topo, m.sop, st, m=cfg["krylov_dim"])
+    orc.refresh_env()
+    dev.refresh_env(A)
+    for node in [0, 1, 2, 3, topo.nnodes - 1]:
+        v = st[node]
+        yo, no = orc.expm_node(node, v, 0.025)
+        yd, nd = dev.expm_node(node, v, 0.025)
+        assert rel(yd, yo) < 1e-11
+        assert nd == no
+
+
+def test_sweep_from_generic_state_matches_oracle():
+    m, cfg = spin_boson_small()
+    topo = m.topology
+    st = generic_state(topo, np.random.default_rng(4))
+    orc, A, dev = make_pair(topo, m.sop, st, m=cfg["krylov_dim"])
+    dev.dt = cfg["dt"]
+    for k in range(8):
+        orc.step(cfg["dt"])
+        dev(A, m.sop, -1j)
+        szo = orc.expect(0, sb.SZ).real
+        szd = dev.mel()(sb.SZ, 0, A).real
+        assert abs(szo - szd) < 1e-10, (k, szo, szd)
+    for a, b in zip(A.get(), orc.get_state()):
+        assert rel(a, b) < 1e-9
+    assert dev.nh_applications() == orc.nh_applications
+    assert abs(dev.mel()(A) - 1.0) < 1e-10
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_full_rank_random_tree_matches_dense_expm(seed):
+    rng = np.random.default_rng(200 + seed)
+    dims = [int(x) for x in rng.integers(2, 4, size=5)]
+    topo = random_tree(rng, dims)
+    H = random_sop(rng, dims, nterms=10)
+    st = generic_state(topo, rng)
+    psi = full_state(topo, st)
+    Hd = H.dense()
+    A = api.httensor(topo)
+    A.set(st)
+    dev = api.fixed_step_projector_splitting_integrator(A, H, krylov_dim=10)
+    dev.dt = 0.1
+    for k in range(5):
+        dev(A, H, -1j)
+        ex = sla.expm(-1j * Hd * (k + 1) * 0.1) @ psi
+        assert np.linalg.norm(full_state(topo, A.get()) - ex) < 1e-10
+
+
+def test_init_product_state_structure():
+    m, cfg = spin_boson_small()
+    topo = m.topology
+    A = api.httensor(topo)
+    A.init_product(np.array([1.0, 0.0]), seed=0)
+    st = A.get()
+    for i, a in enumerate(st):
+        if i == 0:
+            assert a[0, 0] == 1.0 and np.count_nonzero(a) == 1
+            continue
+        assert np.allclose(a.conj().T @ a, np.eye(a.shape[1]), atol=1e-12)
+        if topo.is_leaf(i):
+            assert a[0, 0] == 1.0 and np.all(a[1:, 0] == 0)
+
+
+def test_product_state_within_envelope():
+    """From spin-up x vacuum the truncated dynamics amplifies rounding; the device run
+    must stay inside the spread of the oracle under 1e-15 coefficient perturbations."""
+    m, cfg = spin_boson_small()
+    topo = m.topology
+    A = api.httensor(topo)
+    A.init_product(np.array([1.0, 0.0]), seed=0)
+    st = A.get()
+    nsteps = 20
+    dev = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=cfg["krylov_dim"])
+    dev.dt = cfg["dt"]
+    sd = []
+    for _ in range(nsteps):
+        dev(A, m.sop, -1j)
+        sd.append(dev.mel()(sb.SZ, 0, A).real)
+
+    def run(sop):
+        o = Oracle(topo, sop, krylov_dim=cfg["krylov_dim"])
+        o.set_state(st)
+        out = []
+        for _ in range(nsteps):
+            o.step(cfg["dt"])
+            out.append(o.expect(0, sb.SZ).real)
+        return np.array(out)
+
+    so = run(m.sop)
+    spreads = []
+    for seed in (1, 2, 3):
+        s2 = copy.deepcopy(m.sop)
+        s2.coeffs = s2.coeffs * (1 + 1e-15 * np.random.default_rng(seed).normal(size=s2.nterms))
+        spreads.append(np.abs(run(s2) - so))
+    env = np.max(spreads, axis=0)
+    diff = np.abs(np.array(sd) - so)
+    assert diff[0] < 1e-7
+    assert np.all(diff <= 20 * np.maximum(env, 1e-8)), (diff, env)

@@ -1,0 +1,306 @@
+"""Python mirror of the reference's integrator interface over the C-ABI of libttn_gb300.
+
+Names follow ttns_lib so that a caller's loop ports unchanged:
+
+    A = httensor(topology)                          # httensor(topology, capacity)
+    A.init_product(psi0, seed)                      # the driver's start state
+    tdvp = fixed_step_projector_splitting_integrator(A, H, krylov_dim, krylov_tol)
+    tdvp.dt = 0.05                                  # tdvp.dt() = dt
+    tdvp(A, H, -1j)                                 # one step, returns dt
+    tdvp.mel()(sz, 0, A)                            # <psi|O_0|psi>
+    tdvp.nh_applications()
+
+(include/ttns_lib/integrators/projector_splitting_integrator.hpp:76-218,
+ include/ttns_lib/observables/matrix_element.hpp:264-314, src/spin_boson.cpp:41-107.)
+
+Every call goes to the CUDA library; there is no host fallback.  A missing library or
+a missing GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from .model import SOPOperator, Topology
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libttn_gb300.so")
+
+TTN_OK, TTN_EINVAL, TTN_ECAPACITY, TTN_ENUMERIC, TTN_ECUDA, TTN_ETIMEOUT, TTN_ENOTSUP = range(7)
+PREC_FP64, PREC_MIXED = 0, 1
+
+_ERRNAMES = {1: "EINVAL", 2: "ECAPACITY", 3: "ENUMERIC", 4: "ECUDA", 5: "ETIMEOUT", 6: "ENOTSUP"}
+
+
+class TTNError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"TTN_{_ERRNAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class ttn_integ_cfg(C.Structure):
+    _fields_ = [("krylov_dim", C.c_int), ("krylov_tol", C.c_double), ("precision", C.c_int), ("device", C.c_int)]
+
+
+# every exported symbol and its argument types (pointers as void* / double* / int*)
+_P, _I, _D, _LL = C.c_void_p, C.c_int, C.c_double, C.c_longlong
+_IP, _DP, _LLP = C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_longlong)
+_PP = C.POINTER(C.c_void_p)
+SIGNATURES = {
+    "ttn_last_error": (C.c_char_p, []),
+    "ttn_version": (C.c_char_p, []),
+    "ttn_tree_create": (_I, [_I, _IP, _IP, _IP, _IP, _PP]),
+    "ttn_tree_destroy": (_I, [_P]),
+    "ttn_tree_num_nodes": (_I, [_P, _IP]),
+    "ttn_tree_node_shape": (_I, [_P, _I, _LLP, _IP]),
+    "ttn_tree_state_size": (_I, [_P, _LLP]),
+    "ttn_sop_create": (_I, [_I, _I, _IP, _PP]),
+    "ttn_sop_destroy": (_I, [_P]),
+    "ttn_sop_bind_dense": (_I, [_P, _I, _DP, _IP, _I]),
+    "ttn_sop_bind_diag": (_I, [_P, _I, _DP, _IP, _I]),
+    "ttn_sop_bind_csr": (_I, [_P, _I, _IP, _IP, _DP, _IP, _I]),
+    "ttn_sop_set_coeff": (_I, [_P, _I, _D, _D]),
+    "ttn_state_create": (_I, [_P, _I, _PP]),
+    "ttn_state_destroy": (_I, [_P]),
+    "ttn_state_upload": (_I, [_P, _DP]),
+    "ttn_state_download": (_I, [_P, _DP]),
+    "ttn_state_upload_node": (_I, [_P, _I, _DP]),
+    "ttn_state_download_node": (_I, [_P, _I, _DP]),
+    "ttn_state_init_product": (_I, [_P, _DP, C.c_uint]),
+    "ttn_integrator_create": (_I, [_P, _P, C.POINTER(ttn_integ_cfg), _PP]),
+    "ttn_integrator_destroy": (_I, [_P]),
+    "ttn_integrator_set_dt": (_I, [_P, _D]),
+    "ttn_integrator_dt": (_I, [_P, _DP]),
+    "ttn_integrator_t": (_I, [_P, _DP]),
+    "ttn_integrator_step": (_I, [_P, _P, _D, _D, _DP]),
+    "ttn_integrator_nh_applications": (_I, [_P, _LLP]),
+    "ttn_integrator_reset": (_I, [_P]),
+    "ttn_integrator_synchronize": (_I, [_P]),
+    "ttn_expect_leaf": (_I, [_P, _P, _I, _DP, _DP, _DP]),
+    "ttn_norm2": (_I, [_P, _P, _DP]),
+    "ttn_debug_refresh_env": (_I, [_P, _P]),
+    "ttn_debug_heff": (_I, [_P, _I, _DP, _DP]),
+    "ttn_debug_expm_node": (_I, [_P, _I, _D, _D, _D, _DP, _LLP]),
+    "ttn_debug_num_groups": (_I, [_P, _I, _IP]),
+    "ttn_debug_get_env": (_I, [_P, _I, _I, _I, _DP]),
+    "ttn_debug_qr": (_I, [_I, _I, _DP, _DP, _I]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m ttns_lib_gb300.build` (or __graft_entry__.build())")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != TTN_OK:
+        raise TTNError(rc, lib().ttn_last_error().decode())
+
+
+def _ip(a):
+    return a.ctypes.data_as(_IP)
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP)
+
+
+def _cplx(a):
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+class Tree:
+    def __init__(self, topo: Topology):
+        self.topo = topo
+        h = C.c_void_p()
+        _check(lib().ttn_tree_create(topo.nnodes, _ip(topo.parent), _ip(topo.hrank), _ip(topo.leaf_mode),
+                                     _ip(topo.leaf_dim), C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ttn_tree_destroy(self.h)
+            self.h = None
+
+
+class Operator:
+    """Device-side copy of a SOPOperator (sop_operator)."""
+
+    def __init__(self, sop: SOPOperator):
+        self.sop = sop
+        md = np.array(sop.mode_dims, dtype=np.int32)
+        h = C.c_void_p()
+        _check(lib().ttn_sop_create(sop.nterms, len(md), _ip(md), C.byref(h)))
+        self.h = h
+        for b in sop.ops:
+            m = _cplx(b.matrix)
+            r = np.array(b.terms, dtype=np.int32)
+            _check(lib().ttn_sop_bind_dense(h, b.mode, _dp(m.view(np.float64)), _ip(r), len(r)))
+        for r, c in enumerate(sop.coeffs):
+            _check(lib().ttn_sop_set_coeff(h, r, float(np.real(c)), float(np.imag(c))))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ttn_sop_destroy(self.h)
+            self.h = None
+
+
+class httensor:
+    """Device-resident tree tensor network state (one arena, one slab per node)."""
+
+    def __init__(self, topo: Topology, device: int = 0):
+        self.topo = topo
+        self.tree = Tree(topo)
+        self.device = device
+        h = C.c_void_p()
+        _check(lib().ttn_state_create(self.tree.h, device, C.byref(h)))
+        self.h = h
+        self.offsets = topo.offsets()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ttn_state_destroy(self.h)
+            self.h = None
+
+    def set(self, tensors: Sequence[np.ndarray]):
+        flat = np.concatenate([_cplx(t).ravel() for t in tensors])
+        if flat.size != self.offsets[-1]:
+            raise ValueError("tensor sizes do not match the topology")
+        _check(lib().ttn_state_upload(self.h, _dp(flat.view(np.float64))))
+
+    def get(self) -> List[np.ndarray]:
+        flat = np.zeros(int(self.offsets[-1]), dtype=np.complex128)
+        _check(lib().ttn_state_download(self.h, _dp(flat.view(np.float64))))
+        return [flat[self.offsets[i]:self.offsets[i + 1]].reshape(self.topo.node_shape(i)).copy()
+                for i in range(self.topo.nnodes)]
+
+    def init_product(self, psi0: Optional[np.ndarray] = None, seed: int = 0):
+        """Spin-boson start state with std::mt19937(seed) unoccupied SPFs (src/spin_boson.cpp:584-649)."""
+        if psi0 is None:
+            _check(lib().ttn_state_init_product(self.h, None, seed))
+        else:
+            p = _cplx(psi0)
+            _check(lib().ttn_state_init_product(self.h, _dp(p.view(np.float64)), seed))
+
+
+class matrix_element:
+    """<psi|O_mode|psi> and <psi|psi> (matrix_element::operator())."""
+
+    def __init__(self, integ: "fixed_step_projector_splitting_integrator"):
+        self.integ = integ
+
+    def __call__(self, *args):
+        if len(args) == 1:
+            out = C.c_double()
+            _check(lib().ttn_norm2(self.integ.h, args[0].h, C.byref(out)))
+            return out.value
+        op, mode, A = args
+        m = _cplx(op)
+        re, im = C.c_double(), C.c_double()
+        _check(lib().ttn_expect_leaf(self.integ.h, A.h, int(mode), _dp(m.view(np.float64)), C.byref(re), C.byref(im)))
+        return complex(re.value, im.value)
+
+
+class fixed_step_projector_splitting_integrator:
+    """One-site projector-splitting integrator with a fixed bond dimension."""
+
+    def __init__(self, A: httensor, H: SOPOperator, krylov_dim: int = 4, krylov_tolerance: float = 1e-12,
+                 precision: int = PREC_FP64, device: Optional[int] = None):
+        self.topo = A.topo
+        self.tree = Tree(A.topo)
+        self.op = Operator(H)
+        cfg = ttn_integ_cfg(int(krylov_dim), float(krylov_tolerance), int(precision),
+                            int(A.device if device is None else device))
+        h = C.c_void_p()
+        _check(lib().ttn_integrator_create(self.tree.h, self.op.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._mel = matrix_element(self)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ttn_integrator_destroy(self.h)
+            self.h = None
+
+    @property
+    def dt(self) -> float:
+        out = C.c_double()
+        _check(lib().ttn_integrator_dt(self.h, C.byref(out)))
+        return out.value
+
+    @dt.setter
+    def dt(self, value: float):
+        _check(lib().ttn_integrator_set_dt(self.h, float(value)))
+
+    def t(self) -> float:
+        out = C.c_double()
+        _check(lib().ttn_integrator_t(self.h, C.byref(out)))
+        return out.value
+
+    def __call__(self, A: httensor, H=None, coeff: complex = -1j) -> float:
+        out = C.c_double()
+        _check(lib().ttn_integrator_step(self.h, A.h, float(np.real(coeff)), float(np.imag(coeff)), C.byref(out)))
+        return out.value
+
+    step = __call__
+
+    def nh_applications(self) -> int:
+        out = C.c_longlong()
+        _check(lib().ttn_integrator_nh_applications(self.h, C.byref(out)))
+        return out.value
+
+    def mel(self) -> matrix_element:
+        return self._mel
+
+    def synchronize(self):
+        _check(lib().ttn_integrator_synchronize(self.h))
+
+    # ---- kernel-level entry points used by the parity tests
+    def refresh_env(self, A: httensor):
+        _check(lib().ttn_debug_refresh_env(self.h, A.h))
+
+    def heff(self, node: int, v: np.ndarray) -> np.ndarray:
+        x = _cplx(v).ravel()
+        y = np.zeros_like(x)
+        _check(lib().ttn_debug_heff(self.h, node, _dp(x.view(np.float64)), _dp(y.view(np.float64))))
+        return y.reshape(self.topo.node_shape(node))
+
+    def expm_node(self, node: int, v: np.ndarray, tau: float, coeff: complex = -1j):
+        x = _cplx(v).ravel().copy()
+        n = C.c_longlong()
+        _check(lib().ttn_debug_expm_node(self.h, node, tau, coeff.real, coeff.imag, _dp(x.view(np.float64)),
+                                         C.byref(n)))
+        return x.reshape(self.topo.node_shape(node)), n.value
+
+    def num_groups(self, node: int) -> int:
+        out = C.c_int()
+        _check(lib().ttn_debug_num_groups(self.h, node, C.byref(out)))
+        return out.value
+
+    def env(self, node: int, group: int, which: str) -> np.ndarray:
+        r = int(self.topo.hrank[node])
+        out = np.zeros((r, r), dtype=np.complex128)
+        _check(lib().ttn_debug_get_env(self.h, node, group, 0 if which == "spf" else 1, _dp(out.view(np.float64))))
+        return out
+
+
+def device_qr(a: np.ndarray, device: int = 0):
+    a = _cplx(a).copy()
+    m, n = a.shape
+    r = np.zeros((n, n), dtype=np.complex128)
+    _check(lib().ttn_debug_qr(m, n, _dp(a.view(np.float64)), _dp(r.view(np.float64)), device))
+    return a, r

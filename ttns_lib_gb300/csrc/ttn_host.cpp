@@ -1,0 +1,1417 @@
+// Host side of the GB300 sweep: tree, sum-of-product operator, the compiled term plan,
+// device arenas, the half-sweep schedule and the C-ABI of include/ttn_gb300.h.
+//
+// The schedule is that of ttns_lib's tdvp_algorithm_base (reference paths relative to
+// the ttns_lib root):
+//   forward half sweep ... include/ttns_lib/tdvp_core/tdvp_algorithm_engine.hpp:331-414
+//   backward half sweep .. include/ttns_lib/tdvp_core/tdvp_algorithm_engine.hpp:417-501
+//   prepare_evolution .... include/ttns_lib/tdvp_core/tdvp_algorithm_engine.hpp:257-321
+//   first-step schedule .. include/ttns_lib/integrators/projector_splitting_integrator.hpp:136-169
+// Every numerical operation is a device kernel (ttn_kernels.cu / ttn_tc.cu); the host only
+// walks the schedule and enqueues work on the integrator's stream.  The only
+// device-to-host traffic inside a step is one status word per Krylov sub-step.
+#include "../../include/ttn_gb300.h"
+#include "ttn_kernels.cuh"
+#include "ttn_tc.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <map>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace ttn {
+
+static thread_local std::string g_err;
+
+struct Err : std::runtime_error {
+  int code;
+  Err(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+#define TTN_REQUIRE(cond, code, msg) \
+  do { if (!(cond)) throw ::ttn::Err(code, msg); } while (0)
+#define CK(x)                                                                                       \
+  do {                                                                                              \
+    cudaError_t e_ = (x);                                                                           \
+    if (e_ != cudaSuccess) throw ::ttn::Err(TTN_ECUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+typedef std::complex<double> cd;
+
+// ------------------------------------------------------------------ tree
+struct Tree {
+  int n = 0;
+  std::vector<int> parent, slot, hrank, leaf_mode, leaf_dim, nmodes, sub_end, lo, hi, mode_node, mode_pos;
+  std::vector<std::vector<int>> children, dims;
+  std::vector<long long> dimen;
+  std::vector<int> euler;  // Euler tour, tdvp_tree_traversal.hpp:38-87
+  int nleaves = 0;
+
+  long long size(int i) const { return dimen[i] * hrank[i]; }
+  bool leaf(int i) const { return children[i].empty(); }
+
+  void build(int nn, const int* par, const int* hr, const int* lm, const int* ld) {
+    TTN_REQUIRE(nn >= 1 && par && hr && lm && ld, TTN_EINVAL, "tree arrays must be non-null");
+    n = nn;
+    parent.assign(par, par + n);
+    hrank.assign(hr, hr + n);
+    leaf_mode.assign(lm, lm + n);
+    leaf_dim.assign(ld, ld + n);
+    TTN_REQUIRE(parent[0] == -1, TTN_EINVAL, "node 0 must be the root (parent -1)");
+    children.assign(n, {});
+    slot.assign(n, -1);
+    for (int i = 1; i < n; ++i) {
+      TTN_REQUIRE(parent[i] >= 0 && parent[i] < i, TTN_EINVAL, "nodes must be numbered in pre-order");
+      slot[i] = (int)children[parent[i]].size();
+      children[parent[i]].push_back(i);
+    }
+    sub_end.assign(n, 0);
+    for (int i = n - 1; i >= 0; --i) {
+      sub_end[i] = i + 1;
+      for (int c : children[i]) sub_end[i] = std::max(sub_end[i], sub_end[c]);
+      for (int c : children[i]) TTN_REQUIRE(c < sub_end[i], TTN_EINVAL, "nodes must be numbered in pre-order");
+    }
+    dims.assign(n, {});
+    dimen.assign(n, 1);
+    nmodes.assign(n, 0);
+    nleaves = 0;
+    for (int i = 0; i < n; ++i) {
+      TTN_REQUIRE(hrank[i] >= 1, TTN_EINVAL, "hrank must be >= 1");
+      if (children[i].empty()) {
+        TTN_REQUIRE(leaf_mode[i] >= 0 && leaf_dim[i] >= 1, TTN_EINVAL, "leaves need leaf_mode >= 0 and leaf_dim >= 1");
+        dims[i] = {leaf_dim[i]};
+        nmodes[i] = 1;
+        ++nleaves;
+      } else {
+        TTN_REQUIRE(leaf_mode[i] < 0, TTN_EINVAL, "branch nodes must have leaf_mode -1");
+        for (int c : children[i]) dims[i].push_back(hrank[c]);
+        nmodes[i] = (int)children[i].size();
+      }
+      for (int d : dims[i]) dimen[i] *= d;
+      TTN_REQUIRE(hrank[i] <= dimen[i], TTN_EINVAL, "hrank exceeds the product of the child dimensions");
+    }
+    mode_node.assign(nleaves, -1);
+    mode_pos.assign(nleaves, -1);
+    int pos = 0;
+    for (int i = 0; i < n; ++i)
+      if (children[i].empty()) {
+        int m = leaf_mode[i];
+        TTN_REQUIRE(m < nleaves && mode_node[m] < 0, TTN_EINVAL, "leaf modes must be a permutation of 0..nleaves-1");
+        mode_node[m] = i;
+        mode_pos[m] = pos++;
+      }
+    lo.assign(n, 0);
+    hi.assign(n, 0);
+    for (int i = n - 1; i >= 0; --i) {
+      if (children[i].empty()) {
+        lo[i] = mode_pos[leaf_mode[i]];
+        hi[i] = lo[i] + 1;
+      } else {
+        lo[i] = lo[children[i].front()];
+        hi[i] = hi[children[i].back()];
+      }
+    }
+    for (int i = 0; i < n; ++i) {
+      TTN_REQUIRE(hrank[i] <= kQrMaxCols, TTN_ENOTSUP, "bond dimensions above 64 are not supported by this build");
+      if (!children[i].empty())
+        for (int m = 0; m < nmodes[i]; ++m) {
+          long long d2 = dims[i][m], d1 = dimen[i] * hrank[i] / d2;
+          TTN_REQUIRE(d1 >= d2, TTN_ENOTSUP, "root-to-leaf matricisation is wide; unsupported tree");
+        }
+    }
+    size_t nsites = 0;
+    for (int i = 0; i < n; ++i) nsites += children[i].empty() ? 2 : 1 + children[i].size();
+    euler.resize(nsites);
+    std::vector<int> tv(n, 0);
+    int cur = 0;
+    for (size_t k = 0; k < nsites; ++k) {
+      euler[k] = cur;
+      int t = tv[cur], nxt = cur;
+      if (t == 0 && children[cur].empty()) nxt = cur;
+      else if (t < (int)children[cur].size()) nxt = children[cur][t];
+      else if (cur != 0) nxt = parent[cur];
+      tv[cur]++;
+      cur = nxt;
+    }
+  }
+};
+
+// ------------------------------------------------------------------ operator
+struct Sop {
+  int nterms = 0, nmodes = 0;
+  std::vector<int> mode_dim;
+  std::vector<cd> coeff;
+  std::vector<std::vector<std::vector<cd>>> ops;  // [mode][k] dense d x d
+  std::vector<std::vector<int>> opidx;            // [mode][r]
+};
+
+// ------------------------------------------------------------------ compiled term plan
+// Per node the terms split into S (shared operator below the node, >= 2 terms; the
+// coefficients go into the mean field), M (remaining terms sharing the operator above
+// the node, >= 2; coefficients go into the single-particle operator) and singletons
+// (coefficient applied as a scalar) -- the common-spf / common-mf / standard split of
+// operator_container.hpp:426-444, 648-664.
+enum { G_S = 0, G_M = 1, G_1 = 2 };
+struct Item { int slot, grp; };
+struct SpfTuple { cd a; std::vector<Item> items; };
+struct MfKey { cd b; int pg; std::vector<Item> sib; };
+struct Group {
+  int type = G_1;
+  std::vector<int> members;
+  bool id_spf = false, id_mf = false;
+  cd s = 1.0;
+  std::vector<SpfTuple> spf;
+  std::vector<MfKey> mf;
+  double2* spf_dev = nullptr;
+  double2* mf_dev = nullptr;
+};
+
+struct SigHash {
+  size_t operator()(const std::vector<long long>& v) const {
+    size_t h = 1469598103934665603ull;
+    for (long long x : v) { h ^= (size_t)x + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2); }
+    return h;
+  }
+};
+
+static void compile_plan(const Tree& T, const Sop& H, std::vector<std::vector<Group>>& G,
+                         std::vector<std::vector<int>>& gof) {
+  const int n = T.n, R = H.nterms;
+  // supports sorted by leaf position
+  std::vector<std::vector<std::pair<int, long long>>> sup(R);
+  for (int m = 0; m < H.nmodes; ++m)
+    for (int r = 0; r < R; ++r)
+      if (H.opidx[m][r] >= 0) sup[r].push_back({T.mode_pos[m], ((long long)m << 32) | (unsigned)H.opidx[m][r]});
+  for (auto& s : sup) std::sort(s.begin(), s.end());
+  G.assign(n, {});
+  gof.assign(n, std::vector<int>(R, -1));
+  std::vector<std::vector<long long>> Ls(R), Rs(R);
+  for (int nd = 0; nd < n; ++nd) {
+    for (int r = 0; r < R; ++r) {
+      Ls[r].clear();
+      Rs[r].clear();
+      for (auto& e : sup[r]) {
+        if (e.first >= T.lo[nd] && e.first < T.hi[nd]) Ls[r].push_back(e.second);
+        else Rs[r].push_back(e.second);
+      }
+    }
+    std::unordered_map<std::vector<long long>, std::vector<int>, SigHash> lcls;
+    for (int r = 0; r < R; ++r) lcls[Ls[r]].push_back(r);
+    std::vector<char> isS(R, 0);
+    std::vector<std::vector<int>> sg, mg, sing;
+    for (auto& kv : lcls)
+      if (kv.second.size() >= 2) {
+        sg.push_back(kv.second);
+        for (int r : kv.second) isS[r] = 1;
+      }
+    std::unordered_map<std::vector<long long>, std::vector<int>, SigHash> rcls;
+    for (int r = 0; r < R; ++r)
+      if (!isS[r]) rcls[Rs[r]].push_back(r);
+    for (auto& kv : rcls) (kv.second.size() >= 2 ? mg : sing).push_back(kv.second);
+    auto first = [](const std::vector<int>& a, const std::vector<int>& b) { return a[0] < b[0]; };
+    std::sort(sg.begin(), sg.end(), first);
+    std::sort(mg.begin(), mg.end(), first);
+    std::sort(sing.begin(), sing.end(), first);
+    auto add = [&](std::vector<int>& mem, int type) {
+      std::sort(mem.begin(), mem.end());
+      Group g;
+      g.type = type;
+      g.members = mem;
+      g.id_spf = Ls[mem[0]].empty();
+      g.s = (type == G_1) ? H.coeff[mem[0]] : cd(1.0);
+      for (int r : mem) gof[nd][r] = (int)G[nd].size();
+      G[nd].push_back(std::move(g));
+    };
+    for (auto& v : sg) add(v, G_S);
+    for (auto& v : mg) add(v, G_M);
+    for (auto& v : sing) add(v, G_1);
+  }
+  // single-particle tuples
+  for (int nd = 0; nd < n; ++nd)
+    for (auto& g : G[nd]) {
+      if (g.id_spf) continue;
+      std::map<std::vector<int>, std::vector<int>> keys;
+      for (int r : g.members) {
+        std::vector<int> key;
+        if (T.leaf(nd)) key.push_back(H.opidx[T.leaf_mode[nd]][r]);
+        else
+          for (int s = 0; s < (int)T.children[nd].size(); ++s) {
+            int c = T.children[nd][s], cg = gof[c][r];
+            if (!G[c][cg].id_spf) { key.push_back(s); key.push_back(cg); }
+          }
+        keys[key].push_back(r);
+      }
+      std::vector<std::pair<int, std::vector<int>>> ord;
+      for (auto& kv : keys) ord.push_back({kv.second[0], kv.first});
+      std::sort(ord.begin(), ord.end());
+      for (auto& o : ord) {
+        const auto& key = o.second;
+        const auto& mem = keys[key];
+        SpfTuple t;
+        bool carrying = false;
+        if (T.leaf(nd)) t.items.push_back({-1, key[0]});
+        else
+          for (size_t q = 0; q < key.size(); q += 2) {
+            int c = T.children[nd][key[q]];
+            t.items.push_back({key[q], key[q + 1]});
+            if (G[c][key[q + 1]].type == G_M) {
+              carrying = true;
+              TTN_REQUIRE(G[c][key[q + 1]].members == mem, TTN_EINVAL, "term compression invariant violated");
+            }
+          }
+        if (g.type == G_M && !carrying) {
+          cd a = 0.0;
+          for (int r : mem) a += H.coeff[r];
+          t.a = a;
+        } else t.a = 1.0;
+        g.spf.push_back(t);
+      }
+      TTN_REQUIRE(g.type == G_M || g.spf.size() == 1, TTN_EINVAL, "term compression invariant violated");
+    }
+  // mean-field keys
+  for (int nd = 0; nd < n; ++nd) {
+    if (nd == 0) {
+      for (auto& g : G[nd]) g.id_mf = (g.type != G_S);
+      continue;
+    }
+    int p = T.parent[nd];
+    for (auto& g : G[nd]) {
+      std::map<std::vector<int>, std::vector<int>> keys;
+      for (int r : g.members) {
+        std::vector<int> key{gof[p][r]};
+        for (int s = 0; s < (int)T.children[p].size(); ++s) {
+          int c = T.children[p][s];
+          if (c == nd) continue;
+          int cg = gof[c][r];
+          if (!G[c][cg].id_spf) { key.push_back(s); key.push_back(cg); }
+        }
+        keys[key].push_back(r);
+      }
+      std::vector<std::pair<int, std::vector<int>>> ord;
+      for (auto& kv : keys) ord.push_back({kv.second[0], kv.first});
+      std::sort(ord.begin(), ord.end());
+      for (auto& o : ord) {
+        const auto& key = o.second;
+        const auto& mem = keys[key];
+        MfKey k;
+        k.pg = key[0];
+        const Group& pg = G[p][k.pg];
+        bool carrying = (pg.type == G_S);
+        const std::vector<int>* carrier = carrying ? &pg.members : nullptr;
+        for (size_t q = 1; q < key.size(); q += 2) {
+          int c = T.children[p][key[q]];
+          k.sib.push_back({key[q], key[q + 1]});
+          if (G[c][key[q + 1]].type == G_M) {
+            carrying = true;
+            carrier = &G[c][key[q + 1]].members;
+          }
+        }
+        TTN_REQUIRE(!(g.type != G_S && carrying), TTN_EINVAL, "term compression invariant violated");
+        TTN_REQUIRE(!carrying || *carrier == mem, TTN_EINVAL, "term compression invariant violated");
+        if (g.type == G_S && !carrying) {
+          cd b = 0.0;
+          for (int r : mem) b += H.coeff[r];
+          k.b = b;
+        } else k.b = 1.0;
+        g.mf.push_back(k);
+      }
+      g.id_mf = (g.mf.size() == 1 && g.mf[0].b == cd(1.0) && g.mf[0].sib.empty() && G[p][g.mf[0].pg].id_mf);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ device helpers
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int device = 0;
+  void alloc(size_t b) {
+    free();
+    if (b == 0) b = 16;
+    CK(cudaMalloc(&p, b));
+    bytes = b;
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  ~DevBuf() { free(); }
+  template <typename T> T* as() const { return (T*)p; }
+};
+
+static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+static inline double2 d2(cd z) { return make_double2(z.real(), z.imag()); }
+static const long long kBig = 1LL << 60;
+
+static ZOperand op_rowmajor(const double2* p, long long ld) {  // X(i,k) = p[i*ld + k]
+  ZOperand o{p, ld, 0, 1, kBig, 0, 1};
+  return o;
+}
+static ZOperand op_colk(const double2* p, long long sk, long long so) {  // X(o,k) = p[o*so + k*sk]
+  ZOperand o{p, so, 0, sk, kBig, 0, sk == 1};
+  return o;
+}
+
+}  // namespace ttn
+
+// ------------------------------------------------------------------ public objects
+struct ttn_tree {
+  ttn::Tree T;
+};
+struct ttn_sop {
+  ttn::Sop H;
+};
+struct ttn_state {
+  ttn::Tree T;
+  int device = 0;
+  ttn::DevBuf arena;
+  std::vector<size_t> off;  // element offsets (double2) of each node
+  double2* node(int i) const { return arena.as<double2>() + off[i]; }
+};
+
+namespace ttn {
+
+struct Integrator {
+  Tree T;
+  Sop H;
+  ttn_integ_cfg cfg{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<std::vector<Group>> G;
+  std::vector<std::vector<int>> gof;
+  // device arenas
+  DevBuf ops_buf, env_buf, r_buf, work_buf, ctl_buf, mel_buf;
+  std::vector<std::vector<double2*>> leaf_ops;  // [mode][k]
+  std::vector<double2*> rmat, mel;
+  double2 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w4 = nullptr, *V = nullptr, *p = nullptr, *part = nullptr,
+          *gws = nullptr, *qtau = nullptr, *scal = nullptr;
+  size_t gws_bytes = 0;
+  long long maxsize = 0, ldv = 0;
+  KrylovCtl* ctl = nullptr;
+  int* status = nullptr;
+  // host mirrors
+  struct HostCtl { int done, err; long long napps; };
+  HostCtl* hctl = nullptr;  // pinned
+  double dt = 0.0, t_engine = 0.0;
+  cd coeff = cd(0.0, -1.0);
+  long long nsteps = 0, nh = 0;
+  TcEngine* tc = nullptr;  // tensor-core contraction engine (mixed precision)
+
+  ~Integrator() {
+    if (tc) tc_destroy(tc);
+    if (hctl) cudaFreeHost(hctl);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  void setup() {
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    compile_plan(T, H, G, gof);
+    // leaf operators
+    size_t ob = 0;
+    for (int m = 0; m < H.nmodes; ++m)
+      for (auto& M : H.ops[m]) ob += align256(M.size() * sizeof(double2));
+    ops_buf.alloc(ob);
+    leaf_ops.assign(H.nmodes, {});
+    {
+      char* base = ops_buf.as<char>();
+      size_t o = 0;
+      for (int m = 0; m < H.nmodes; ++m)
+        for (auto& M : H.ops[m]) {
+          double2* dptr = (double2*)(base + o);
+          std::vector<double2> tmp(M.size());
+          for (size_t i = 0; i < M.size(); ++i) tmp[i] = d2(M[i]);
+          CK(cudaMemcpy(dptr, tmp.data(), tmp.size() * sizeof(double2), cudaMemcpyHostToDevice));
+          leaf_ops[m].push_back(dptr);
+          o += align256(M.size() * sizeof(double2));
+        }
+    }
+    // environments: one r x r matrix per non-identity spf / mf
+    size_t eb = 0;
+    for (int i = 0; i < T.n; ++i) {
+      size_t rr = (size_t)T.hrank[i] * T.hrank[i] * sizeof(double2);
+      for (auto& g : G[i]) eb += (g.id_spf ? 0 : align256(rr)) + (g.id_mf ? 0 : align256(rr));
+    }
+    env_buf.alloc(eb);
+    CK(cudaMemset(env_buf.p, 0, env_buf.bytes));
+    {
+      char* base = env_buf.as<char>();
+      size_t o = 0;
+      for (int i = 0; i < T.n; ++i) {
+        size_t rr = (size_t)T.hrank[i] * T.hrank[i] * sizeof(double2);
+        for (auto& g : G[i]) {
+          if (!g.id_spf) { g.spf_dev = (double2*)(base + o); o += align256(rr); }
+          if (!g.id_mf) {
+            g.mf_dev = (double2*)(base + o);
+            o += align256(rr);
+            if (i == 0) {  // root S group: (sum of coefficients) * I
+              cd sum = 0.0;
+              for (int r : g.members) sum += H.coeff[r];
+              zscale_identity(g.mf_dev, T.hrank[i], d2(sum), stream);
+            }
+          }
+        }
+      }
+    }
+    // R matrices and observable scratch
+    size_t rb = 0, mb = 0;
+    for (int i = 0; i < T.n; ++i) {
+      long long rmx = T.hrank[i];
+      for (int d : T.dims[i]) rmx = std::max<long long>(rmx, d);
+      rb += align256((size_t)rmx * rmx * sizeof(double2));
+      mb += align256((size_t)T.hrank[i] * T.hrank[i] * sizeof(double2));
+    }
+    r_buf.alloc(rb);
+    mel_buf.alloc(mb);
+    rmat.resize(T.n);
+    mel.resize(T.n);
+    {
+      size_t o = 0, o2 = 0;
+      for (int i = 0; i < T.n; ++i) {
+        long long rmx = T.hrank[i];
+        for (int d : T.dims[i]) rmx = std::max<long long>(rmx, d);
+        rmat[i] = (double2*)(r_buf.as<char>() + o);
+        o += align256((size_t)rmx * rmx * sizeof(double2));
+        mel[i] = (double2*)(mel_buf.as<char>() + o2);
+        o2 += align256((size_t)T.hrank[i] * T.hrank[i] * sizeof(double2));
+      }
+    }
+    // work space
+    maxsize = 0;
+    for (int i = 0; i < T.n; ++i) maxsize = std::max(maxsize, T.size(i));
+    ldv = (long long)(align256((size_t)maxsize * sizeof(double2)) / sizeof(double2));
+    size_t gmax = 0;
+    for (int i = 0; i < T.n; ++i) {
+      int r = T.hrank[i];
+      gmax = std::max(gmax, zgemm_split_workspace_bytes(r, r, (int)T.dimen[i]));
+      for (int m = 0; m < T.nmodes[i]; ++m) {
+        int d = T.dims[i][m];
+        gmax = std::max(gmax, zgemm_split_workspace_bytes(d, d, (int)(T.size(i) / d)));
+      }
+    }
+    gws_bytes = align256(gmax + 16);
+    const int m = cfg.krylov_dim;
+    size_t wb = 0;
+    wb += 4 * align256(ldv * sizeof(double2));                   // w1..w4
+    wb += (size_t)(m + 1) * ldv * sizeof(double2);               // V
+    wb += align256(ldv * sizeof(double2));                        // p
+    wb += align256(lanczos_partial_bytes());                      // partials
+    wb += gws_bytes;                                              // zgemm split-K
+    wb += align256(kQrMaxCols * sizeof(double2));                 // QR tau
+    wb += align256(64 * sizeof(double2));                         // scalars
+    work_buf.alloc(wb);
+    {
+      char* b = work_buf.as<char>();
+      size_t o = 0;
+      auto take = [&](size_t bytes) { char* q = b + o; o += align256(bytes); return (double2*)q; };
+      w1 = take(ldv * sizeof(double2));
+      w2 = take(ldv * sizeof(double2));
+      w3 = take(ldv * sizeof(double2));
+      w4 = take(ldv * sizeof(double2));
+      V = take((size_t)(m + 1) * ldv * sizeof(double2));
+      p = take(ldv * sizeof(double2));
+      part = take(lanczos_partial_bytes());
+      gws = take(gws_bytes);
+      qtau = take(kQrMaxCols * sizeof(double2));
+      scal = take(64 * sizeof(double2));
+    }
+    ctl_buf.alloc(align256(sizeof(KrylovCtl)) + 256);
+    ctl = ctl_buf.as<KrylovCtl>();
+    status = (int*)(ctl_buf.as<char>() + align256(sizeof(KrylovCtl)));
+    CK(cudaMemsetAsync(ctl_buf.p, 0, ctl_buf.bytes, stream));
+    CK(cudaMallocHost((void**)&hctl, sizeof(HostCtl)));
+    if (cfg.precision == TTN_PREC_MIXED) {
+      try {
+        tc = tc_create(device, maxsize, stream);
+      } catch (const Err&) {
+        throw;
+      } catch (const std::exception& e) {
+        throw Err(TTN_ENOTSUP, e.what());
+      }
+    }
+    CK(cudaStreamSynchronize(stream));
+  }
+
+  // ---------------------------------------------------------------- contractions
+  void r3(int nd, int mu, long long& na, int& d, long long& nb) const {
+    na = 1;
+    nb = T.hrank[nd];
+    for (int i = 0; i < mu; ++i) na *= T.dims[nd][i];
+    d = T.dims[nd][mu];
+    for (int i = mu + 1; i < T.nmodes[nd]; ++i) nb *= T.dims[nd][i];
+  }
+  // out(a,i,b) = alpha sum_j S(i,j) in(a,j,b) (+ out)
+  void mode_apply(const double2* S, int d, const double2* in, double2* out, long long na, long long nb, cd alpha,
+                  bool acc) {
+    if (tc && tc_mode_apply(tc, S, d, in, out, na, nb, d2(alpha), acc, stream)) return;
+    ZGemm g{};
+    g.M = d; g.N = (int)nb; g.K = d;
+    g.A = op_rowmajor(S, d);
+    g.B = op_colk(in, nb, 1);
+    g.C = out; g.ci = nb; g.cj = 1;
+    g.bsA = 0; g.bsB = (long long)d * nb; g.bsC = (long long)d * nb;
+    g.batch = (int)na;
+    g.alpha = d2(alpha);
+    g.beta = acc ? make_double2(1.0, 0.0) : make_double2(0.0, 0.0);
+    zgemm(g, gws, gws_bytes, stream);
+  }
+  // out(x,k) = alpha sum_l in(x,l) M(k,l) (+ out)
+  void mf_apply(const double2* in, const double2* M, int r, long long nx, double2* out, cd alpha, bool acc) {
+    if (tc && tc_mf_apply(tc, in, M, r, nx, out, d2(alpha), acc, stream)) return;
+    ZGemm g{};
+    g.M = (int)nx; g.N = r; g.K = r;
+    g.A = op_rowmajor(in, r);
+    g.B = op_rowmajor(M, r);  // B(l,k) = M[k*r + l]
+    g.C = out; g.ci = r; g.cj = 1;
+    g.batch = 1;
+    g.alpha = d2(alpha);
+    g.beta = acc ? make_double2(1.0, 0.0) : make_double2(0.0, 0.0);
+    zgemm(g, gws, gws_bytes, stream);
+  }
+  // out(i,j) = alpha sum_x conj(A(x,i)) X(x,j) (+ out)
+  void adj_mul(const double2* A, const double2* X, long long nx, int r, double2* out, cd alpha, bool acc) {
+    if (tc && tc_adj_mul(tc, A, X, nx, r, out, d2(alpha), acc, stream)) return;
+    ZGemm g{};
+    g.M = r; g.N = r; g.K = (int)nx;
+    g.A = op_colk(A, r, 1);
+    g.A.cj = 1;
+    g.B = op_colk(X, r, 1);
+    g.C = out; g.ci = r; g.cj = 1;
+    g.batch = 1;
+    g.alpha = d2(alpha);
+    g.beta = acc ? make_double2(1.0, 0.0) : make_double2(0.0, 0.0);
+    zgemm(g, gws, gws_bytes, stream);
+  }
+  // out(i,j) = alpha sum_{a,b} conj(A(a,i,b)) T(a,j,b) (+ out)
+  void mode_contract(const double2* A, const double2* Tt, long long na, int d, long long nb, double2* out, cd alpha,
+                     bool acc) {
+    if (tc && tc_mode_contract(tc, A, Tt, na, d, nb, out, d2(alpha), acc, stream)) return;
+    ZGemm g{};
+    g.M = d; g.N = d; g.K = (int)(na * nb);
+    ZOperand o{A, nb, (long long)d * nb, 1, nb, 1, 1};
+    g.A = o;
+    ZOperand o2{Tt, nb, (long long)d * nb, 1, nb, 0, 1};
+    g.B = o2;
+    g.C = out; g.ci = d; g.cj = 1;
+    g.batch = 1;
+    g.alpha = d2(alpha);
+    g.beta = acc ? make_double2(1.0, 0.0) : make_double2(0.0, 0.0);
+    zgemm(g, gws, gws_bytes, stream);
+  }
+  // C (m x r) = A (m x r) * R (r x r)
+  void right_mul(const double2* A, const double2* R, long long m, int r, double2* C) {
+    ZGemm g{};
+    g.M = (int)m; g.N = r; g.K = r;
+    g.A = op_rowmajor(A, r);
+    g.B = op_colk(R, r, 1);  // B(k,j) = R[k*r + j]
+    g.C = C; g.ci = r; g.cj = 1;
+    g.batch = 1;
+    g.alpha = make_double2(1.0, 0.0);
+    g.beta = make_double2(0.0, 0.0);
+    zgemm(g, gws, gws_bytes, stream);
+  }
+
+  const double2* apply_items(int nd, const std::vector<Item>& items, const double2* v, double2* b1, double2* b2,
+                             cd alpha_last = 1.0) {
+    const double2* cur = v;
+    double2* nxt = b1;
+    for (size_t q = 0; q < items.size(); ++q) {
+      const Item& it = items[q];
+      long long na, nb;
+      int d;
+      const double2* S;
+      if (it.slot < 0) {
+        S = leaf_ops[T.leaf_mode[nd]][it.grp];
+        na = 1; d = T.dims[nd][0]; nb = T.hrank[nd];
+      } else {
+        S = G[T.children[nd][it.slot]][it.grp].spf_dev;
+        r3(nd, it.slot, na, d, nb);
+      }
+      mode_apply(S, d, cur, nxt, na, nb, q + 1 == items.size() ? alpha_last : cd(1.0), false);
+      cur = nxt;
+      nxt = (nxt == b1) ? b2 : b1;
+    }
+    return cur;
+  }
+  const double2* apply_sibs(int p, const std::vector<Item>& items, const double2* v, double2* b1, double2* b2) {
+    const double2* cur = v;
+    double2* nxt = b1;
+    for (const Item& it : items) {
+      long long na, nb;
+      int d;
+      r3(p, it.slot, na, d, nb);
+      mode_apply(G[T.children[p][it.slot]][it.grp].spf_dev, d, cur, nxt, na, nb, 1.0, false);
+      cur = nxt;
+      nxt = (nxt == b1) ? b2 : b1;
+    }
+    return cur;
+  }
+
+  // bottom-up environment (single_particle_operator.hpp:26-103)
+  void update_spf(int nd, const double2* A) {
+    const long long sz = T.size(nd);
+    const int r = T.hrank[nd];
+    for (auto& g : G[nd]) {
+      if (g.id_spf) continue;
+      bool first = true;
+      for (const SpfTuple& t : g.spf) {
+        const double2* X = apply_items(nd, t.items, A, w1, w2);
+        adj_mul(A, X, sz / r, r, g.spf_dev, t.a, !first);
+        first = false;
+      }
+    }
+  }
+  // top-down environment of child nd (mean_field_operator.hpp:37-184)
+  void update_mf(int nd, const double2* Ap) {
+    if (nd == 0) return;
+    const int p = T.parent[nd], mu = T.slot[nd];
+    long long na, nb;
+    int d;
+    r3(p, mu, na, d, nb);
+    const int rp = T.hrank[p];
+    const long long szp = T.size(p);
+    for (auto& g : G[nd]) {
+      if (g.id_mf) continue;
+      bool first = true;
+      for (const MfKey& k : g.mf) {
+        const double2* X = apply_sibs(p, k.sib, Ap, w1, w2);
+        if (!G[p][k.pg].id_mf) {
+          double2* dst = (X == w1) ? w2 : w1;
+          mf_apply(X, G[p][k.pg].mf_dev, rp, szp / rp, dst, 1.0, false);
+          X = dst;
+        }
+        mode_contract(Ap, X, na, d, nb, g.mf_dev, k.b, !first);
+        first = false;
+      }
+    }
+  }
+  // out = H_eff(nd) v (coefficient_evolution_leaf / _branch)
+  void heff(int nd, const double2* v, double2* out) {
+    const long long sz = T.size(nd);
+    const int r = T.hrank[nd];
+    bool first = true;
+    for (auto& g : G[nd]) {
+      const bool direct = g.id_mf;  // accumulate straight into out
+      if (g.id_spf) {
+        if (direct) {
+          // out (+)= s v
+          mode_identity_axpy(v, out, sz, g.s, !first);
+        } else {
+          mf_apply(v, g.mf_dev, r, sz / r, out, g.s, !first);
+        }
+      } else if (g.spf.size() == 1) {
+        const auto& t = g.spf[0];
+        if (direct && t.items.size() == 1) {
+          // single contraction straight into out with the combined scalar
+          const Item& it = t.items[0];
+          long long na, nb;
+          int d;
+          const double2* S;
+          if (it.slot < 0) { S = leaf_ops[T.leaf_mode[nd]][it.grp]; na = 1; d = T.dims[nd][0]; nb = r; }
+          else { S = G[T.children[nd][it.slot]][it.grp].spf_dev; r3(nd, it.slot, na, d, nb); }
+          mode_apply(S, d, v, out, na, nb, g.s * t.a, !first);
+        } else {
+          const double2* X = apply_items(nd, t.items, v, w1, w2, t.a);
+          if (direct) mode_identity_axpy(X, out, sz, g.s, !first);
+          else mf_apply(X, g.mf_dev, r, sz / r, out, g.s, !first);
+        }
+      } else {
+        // several tuples: sum into w3 then one mean-field product
+        if (direct) {
+          bool f2 = first;
+          for (const SpfTuple& t : g.spf) {
+            if (t.items.size() == 1) {
+              const Item& it = t.items[0];
+              long long na, nb;
+              int d;
+              const double2* S;
+              if (it.slot < 0) { S = leaf_ops[T.leaf_mode[nd]][it.grp]; na = 1; d = T.dims[nd][0]; nb = r; }
+              else { S = G[T.children[nd][it.slot]][it.grp].spf_dev; r3(nd, it.slot, na, d, nb); }
+              mode_apply(S, d, v, out, na, nb, g.s * t.a, !f2);
+            } else {
+              const double2* X = apply_items(nd, t.items, v, w1, w2, t.a);
+              mode_identity_axpy(X, out, sz, g.s, !f2);
+            }
+            f2 = false;
+          }
+        } else {
+          bool f2 = true;
+          for (const SpfTuple& t : g.spf) {
+            if (t.items.size() == 1) {
+              const Item& it = t.items[0];
+              long long na, nb;
+              int d;
+              const double2* S;
+              if (it.slot < 0) { S = leaf_ops[T.leaf_mode[nd]][it.grp]; na = 1; d = T.dims[nd][0]; nb = r; }
+              else { S = G[T.children[nd][it.slot]][it.grp].spf_dev; r3(nd, it.slot, na, d, nb); }
+              mode_apply(S, d, v, w3, na, nb, t.a, !f2);
+            } else {
+              const double2* X = apply_items(nd, t.items, v, w1, w2, t.a);
+              mode_identity_axpy(X, w3, sz, 1.0, !f2);
+            }
+            f2 = false;
+          }
+          mf_apply(w3, g.mf_dev, r, sz / r, out, g.s, !first);
+        }
+      }
+      first = false;
+    }
+    if (first) zfill(out, make_double2(0.0, 0.0), sz, stream);
+  }
+  // out (+)= s * x
+  void mode_identity_axpy(const double2* x, double2* out, long long sz, cd s, bool acc) {
+    zaxpy(out, x, d2(s), sz, acc, stream);
+  }
+  // out = K_bond(nd) R (full_hamiltonian_action)
+  void kbond(int nd, const double2* R, double2* out) {
+    const int r = T.hrank[nd];
+    bool first = true;
+    for (auto& g : G[nd]) {
+      const double2* X = R;
+      if (!g.id_spf) {
+        ZGemm gg{};
+        gg.M = r; gg.N = r; gg.K = r;
+        gg.A = op_rowmajor(g.spf_dev, r);
+        gg.B = op_colk(R, r, 1);
+        gg.C = w1; gg.ci = r; gg.cj = 1;
+        gg.batch = 1;
+        gg.alpha = make_double2(1.0, 0.0);
+        gg.beta = make_double2(0.0, 0.0);
+        zgemm(gg, gws, gws_bytes, stream);
+        X = w1;
+      }
+      if (g.id_mf) mode_identity_axpy(X, out, (long long)r * r, g.s, !first);
+      else mf_apply(X, g.mf_dev, r, r, out, g.s, !first);
+      first = false;
+    }
+    if (first) zfill(out, make_double2(0.0, 0.0), (long long)r * r, stream);
+  }
+
+  // ---------------------------------------------------------------- Krylov exponential
+  template <typename Op>
+  void expm(Op&& hop, double2* y, long long n, double tau, cd cf, bool count) {
+    if (tau == 0.0) return;
+    const int m = cfg.krylov_dim;
+    krylov_init_ctl(ctl, m, tau, cf.real(), cf.imag(), cfg.krylov_tol, stream);
+    for (int sub = 0;; ++sub) {
+      TTN_REQUIRE(sub < 100000, TTN_ENUMERIC, "Krylov exponential did not finish");
+      krylov_begin(ctl, y, V, n, part, stream);
+      for (int j = 0; j < m; ++j) {
+        hop(V + (long long)j * ldv, p);
+        lanczos_orth(ctl, j, V, ldv, p, n, part, stream);
+      }
+      hop(V + (long long)m * ldv, p);
+      lanczos_avnorm(ctl, p, n, part, stream);
+      krylov_control(ctl, stream);
+      krylov_combine(ctl, V, ldv, y, n, m + 1, stream);
+      CK(cudaMemcpyAsync(&hctl->done, &ctl->done, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemcpyAsync(&hctl->napps, &ctl->napps, sizeof(long long), cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
+      TTN_REQUIRE(hctl->err == 0, TTN_ENUMERIC, "Krylov exponential failed (tolerance unreachable or non-finite values)");
+      if (hctl->done) break;
+    }
+    if (count) nh += hctl->napps;
+  }
+
+  // ---------------------------------------------------------------- gauge moves
+  void l2r(int nd, double2* A) {
+    const long long m = T.dimen[nd];
+    const int r = T.hrank[nd];
+    householder_qr(A, m, r, rmat[nd], 0, qtau, stream);
+  }
+  void apply_to_parent(int nd, double2* Ap, int p) {
+    long long na, nb;
+    int d;
+    r3(p, T.slot[nd], na, d, nb);
+    mode_apply(rmat[nd], d, Ap, w4, na, nb, 1.0, false);
+    zcopy(Ap, w4, T.size(p), stream);
+  }
+  void r2l(int nd, int mu, double2* A) {
+    long long pre = 1, post = T.hrank[nd];
+    for (int i = 0; i < mu; ++i) pre *= T.dims[nd][i];
+    const int dm = T.dims[nd][mu];
+    for (int i = mu + 1; i < T.nmodes[nd]; ++i) post *= T.dims[nd][i];
+    permute_mode_last(A, w4, pre, dm, post, stream);
+    householder_qr(w4, pre * post, dm, rmat[nd], 1, qtau, stream);
+    unpermute_mode_last(w4, A, pre, dm, post, stream);
+  }
+  void apply_from_parent(int nd, double2* A) {
+    const int p = T.parent[nd], r = T.hrank[nd];
+    right_mul(A, rmat[p], T.dimen[nd], r, w4);
+    zcopy(A, w4, T.size(nd), stream);
+  }
+
+  // ---------------------------------------------------------------- sweep
+  void evolve_node(ttn_state* S, int nd) {
+    double2* A = S->node(nd);
+    expm([&](const double2* v, double2* o) { heff(nd, v, o); }, A, T.size(nd), dt / 2.0, coeff, true);
+  }
+  void evolve_bond(int nd, double2* R) {
+    const long long rr = (long long)T.hrank[nd] * T.hrank[nd];
+    expm([&](const double2* v, double2* o) { kbond(nd, v, o); }, R, rr, -dt / 2.0, coeff, false);
+  }
+  void forward(ttn_state* S, bool evolve) {
+    std::vector<int> tv(T.n, 0);
+    for (int id : T.euler) {
+      int t = tv[id]++;
+      double2* A = S->node(id);
+      if (t != T.nmodes[id]) {
+        if (t == 0 && id != 0) apply_from_parent(id, A);
+        if (!T.leaf(id)) {
+          r2l(id, t, A);
+          update_mf(T.children[id][t], A);
+        }
+      } else {
+        if (evolve) evolve_node(S, id);
+        if (id != 0) {
+          l2r(id, A);
+          update_spf(id, A);
+          if (evolve) evolve_bond(id, rmat[id]);
+          apply_to_parent(id, S->node(T.parent[id]), T.parent[id]);
+        }
+      }
+    }
+  }
+  void backward(ttn_state* S, bool evolve) {
+    std::vector<int> tv(T.n, 0);
+    for (auto it = T.euler.rbegin(); it != T.euler.rend(); ++it) {
+      int id = *it;
+      int t = tv[id]++;
+      double2* A = S->node(id);
+      if (t != T.nmodes[id]) {
+        int mode = T.nmodes[id] - (t + 1);
+        if (t == 0) {
+          if (id != 0) {
+            if (evolve) evolve_bond(id, rmat[T.parent[id]]);
+            apply_from_parent(id, A);
+          }
+          if (evolve) evolve_node(S, id);
+        }
+        if (!T.leaf(id)) {
+          r2l(id, mode, A);
+          update_mf(T.children[id][mode], A);
+        }
+      } else if (id != 0) {
+        l2r(id, A);
+        apply_to_parent(id, S->node(T.parent[id]), T.parent[id]);
+        update_spf(id, A);
+      }
+    }
+  }
+  void sweep(ttn_state* S) {
+    forward(S, true);
+    t_engine += dt / 2.0;
+    backward(S, true);
+    t_engine += dt / 2.0;
+  }
+  void prepare(ttn_state* S) {
+    for (int id = T.n - 1; id >= 1; --id) update_spf(id, S->node(id));
+    forward(S, false);
+    backward(S, false);
+  }
+  void step(ttn_state* S, double step_dt, cd cf) {
+    coeff = cf;
+    if (nsteps == 0) {
+      double tevolve = 0.0, sdt = step_dt / 1e5;
+      dt = (sdt + tevolve <= step_dt) ? sdt : step_dt - tevolve;
+      prepare(S);
+      while (tevolve < step_dt) {
+        dt = (sdt + tevolve <= step_dt) ? sdt : step_dt - tevolve;
+        t_engine = tevolve;
+        sweep(S);
+        tevolve += sdt;
+        sdt *= 10.0;
+      }
+    } else {
+      dt = step_dt;
+      t_engine = nsteps * step_dt;
+      sweep(S);
+    }
+    ++nsteps;
+    dt = step_dt;
+    finish_check(S);
+  }
+  void finish_check(ttn_state* S) {
+    CK(cudaMemsetAsync(status, 0, sizeof(int), stream));
+    check_finite(S->arena.as<double2>(), (long long)(S->arena.bytes / sizeof(double2)), status, 1, stream);
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaGetLastError());
+    TTN_REQUIRE(h == 0, TTN_ENUMERIC, "the state holds non-finite values after the step");
+  }
+
+  // ---------------------------------------------------------------- observables
+  cd expect(ttn_state* S, int mode, const double2* op_dev) {
+    for (int id = T.n - 1; id >= 0; --id) {
+      const int r = T.hrank[id];
+      const long long sz = T.size(id);
+      const double2* A = S->node(id);
+      const double2* X = A;
+      if (T.leaf(id)) {
+        if (op_dev && T.leaf_mode[id] == mode) {
+          mode_apply(op_dev, T.dims[id][0], A, w1, 1, r, 1.0, false);
+          X = w1;
+        }
+      } else {
+        const double2* cur = A;
+        double2* nxt = w1;
+        for (int s = 0; s < T.nmodes[id]; ++s) {
+          long long na, nb;
+          int d;
+          r3(id, s, na, d, nb);
+          mode_apply(mel[T.children[id][s]], d, cur, nxt, na, nb, 1.0, false);
+          cur = nxt;
+          nxt = (nxt == w1) ? w2 : w1;
+        }
+        X = cur;
+      }
+      adj_mul(A, X, sz / r, r, mel[id], 1.0, false);
+    }
+    ztrace(mel[0], T.hrank[0], scal + 1, stream);
+    double2 h;
+    CK(cudaMemcpyAsync(&h, scal + 1, sizeof(double2), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    return cd(h.x, h.y);
+  }
+};
+
+static void check_same_tree(const Tree& a, const Tree& b) {
+  TTN_REQUIRE(a.parent == b.parent && a.hrank == b.hrank && a.leaf_dim == b.leaf_dim && a.leaf_mode == b.leaf_mode,
+              TTN_EINVAL, "state and integrator were built for different trees");
+}
+
+}  // namespace ttn
+
+struct ttn_integrator {
+  ttn::Integrator I;
+};
+
+// ====================================================================== C-ABI
+#define TTN_API_BEGIN try {
+#define TTN_API_END                                   \
+  return TTN_OK;                                      \
+  }                                                   \
+  catch (const ttn::Err& e) {                         \
+    ttn::g_err = e.what();                            \
+    return e.code;                                    \
+  }                                                   \
+  catch (const std::bad_alloc&) {                     \
+    ttn::g_err = "host allocation failed";            \
+    return TTN_ECAPACITY;                             \
+  }                                                   \
+  catch (const std::exception& e) {                   \
+    ttn::g_err = e.what();                            \
+    return TTN_EINVAL;                                \
+  }
+
+extern "C" {
+
+const char* ttn_last_error(void) { return ttn::g_err.c_str(); }
+const char* ttn_version(void) { return "ttn_gb300 1.0 (sm_103a)"; }
+
+int ttn_tree_create(int nnodes, const int* parent, const int* hrank, const int* leaf_mode, const int* leaf_dim,
+                    ttn_tree** out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(out, TTN_EINVAL, "out is null");
+  auto* t = new ttn_tree();
+  try { t->T.build(nnodes, parent, hrank, leaf_mode, leaf_dim); } catch (...) { delete t; throw; }
+  *out = t;
+  TTN_API_END
+}
+int ttn_tree_destroy(ttn_tree* t) { delete t; return TTN_OK; }
+int ttn_tree_num_nodes(const ttn_tree* t, int* out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(t && out, TTN_EINVAL, "null argument");
+  *out = t->T.n;
+  TTN_API_END
+}
+int ttn_tree_node_shape(const ttn_tree* t, int node, long long* dimen, int* hrank) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(t && node >= 0 && node < t->T.n, TTN_EINVAL, "node out of range");
+  if (dimen) *dimen = t->T.dimen[node];
+  if (hrank) *hrank = t->T.hrank[node];
+  TTN_API_END
+}
+int ttn_tree_state_size(const ttn_tree* t, long long* n) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(t && n, TTN_EINVAL, "null argument");
+  long long s = 0;
+  for (int i = 0; i < t->T.n; ++i) s += t->T.size(i);
+  *n = s;
+  TTN_API_END
+}
+
+int ttn_sop_create(int nterms, int nmodes, const int* mode_dims, ttn_sop** out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(out && nterms >= 1 && nmodes >= 1 && mode_dims, TTN_EINVAL, "bad operator shape");
+  auto* s = new ttn_sop();
+  s->H.nterms = nterms;
+  s->H.nmodes = nmodes;
+  s->H.mode_dim.assign(mode_dims, mode_dims + nmodes);
+  for (int d : s->H.mode_dim)
+    if (d < 1) { delete s; throw ttn::Err(TTN_EINVAL, "mode dimensions must be >= 1"); }
+  s->H.coeff.assign(nterms, 1.0);
+  s->H.ops.assign(nmodes, {});
+  s->H.opidx.assign(nmodes, std::vector<int>(nterms, -1));
+  *out = s;
+  TTN_API_END
+}
+int ttn_sop_destroy(ttn_sop* s) { delete s; return TTN_OK; }
+
+static void sop_bind(ttn_sop* s, int mode, std::vector<ttn::cd>&& M, const int* r, int nr) {
+  TTN_REQUIRE(s && mode >= 0 && mode < s->H.nmodes, TTN_EINVAL, "mode out of range");
+  TTN_REQUIRE(r && nr >= 1, TTN_EINVAL, "an operator must be bound to at least one term");
+  for (int q = 0; q < nr; ++q) {
+    TTN_REQUIRE(r[q] >= 0 && r[q] < s->H.nterms, TTN_EINVAL, "term index out of range");
+    TTN_REQUIRE(s->H.opidx[mode][r[q]] < 0, TTN_EINVAL, "term already has an operator on this mode");
+  }
+  for (auto& z : M) TTN_REQUIRE(std::isfinite(z.real()) && std::isfinite(z.imag()), TTN_EINVAL, "non-finite operator entry");
+  int k = (int)s->H.ops[mode].size();
+  s->H.ops[mode].push_back(std::move(M));
+  for (int q = 0; q < nr; ++q) s->H.opidx[mode][r[q]] = k;
+}
+int ttn_sop_bind_dense(ttn_sop* s, int mode, const double* mat, const int* r, int nr) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(s && mat && mode >= 0 && mode < s->H.nmodes, TTN_EINVAL, "bad argument");
+  int d = s->H.mode_dim[mode];
+  std::vector<ttn::cd> M((size_t)d * d);
+  for (size_t i = 0; i < M.size(); ++i) M[i] = ttn::cd(mat[2 * i], mat[2 * i + 1]);
+  sop_bind(s, mode, std::move(M), r, nr);
+  TTN_API_END
+}
+int ttn_sop_bind_diag(ttn_sop* s, int mode, const double* diag, const int* r, int nr) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(s && diag && mode >= 0 && mode < s->H.nmodes, TTN_EINVAL, "bad argument");
+  int d = s->H.mode_dim[mode];
+  std::vector<ttn::cd> M((size_t)d * d, 0.0);
+  for (int i = 0; i < d; ++i) M[(size_t)i * d + i] = ttn::cd(diag[2 * i], diag[2 * i + 1]);
+  sop_bind(s, mode, std::move(M), r, nr);
+  TTN_API_END
+}
+int ttn_sop_bind_csr(ttn_sop* s, int mode, const int* rowptr, const int* colind, const double* vals, const int* r,
+                     int nr) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(s && rowptr && mode >= 0 && mode < s->H.nmodes, TTN_EINVAL, "bad argument");
+  int d = s->H.mode_dim[mode];
+  std::vector<ttn::cd> M((size_t)d * d, 0.0);
+  for (int i = 0; i < d; ++i)
+    for (int q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+      TTN_REQUIRE(colind && vals && colind[q] >= 0 && colind[q] < d, TTN_EINVAL, "CSR column out of range");
+      M[(size_t)i * d + colind[q]] += ttn::cd(vals[2 * q], vals[2 * q + 1]);
+    }
+  sop_bind(s, mode, std::move(M), r, nr);
+  TTN_API_END
+}
+int ttn_sop_set_coeff(ttn_sop* s, int r, double re, double im) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(s && r >= 0 && r < s->H.nterms, TTN_EINVAL, "term index out of range");
+  TTN_REQUIRE(std::isfinite(re) && std::isfinite(im), TTN_EINVAL, "non-finite coefficient");
+  s->H.coeff[r] = ttn::cd(re, im);
+  TTN_API_END
+}
+
+int ttn_state_create(const ttn_tree* t, int device, ttn_state** out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(t && out, TTN_EINVAL, "null argument");
+  CK(cudaSetDevice(device));
+  auto* s = new ttn_state();
+  try {
+    s->T = t->T;
+    s->device = device;
+    s->off.resize(t->T.n + 1);
+    size_t o = 0;
+    for (int i = 0; i < t->T.n; ++i) {
+      s->off[i] = o;
+      o += ttn::align256((size_t)t->T.size(i) * sizeof(double2)) / sizeof(double2);
+    }
+    s->off[t->T.n] = o;
+    s->arena.alloc(o * sizeof(double2));
+    CK(cudaMemset(s->arena.p, 0, s->arena.bytes));
+  } catch (...) {
+    delete s;
+    throw;
+  }
+  *out = s;
+  TTN_API_END
+}
+int ttn_state_destroy(ttn_state* s) { delete s; return TTN_OK; }
+int ttn_state_upload_node(ttn_state* s, int node, const double* data) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(s && data && node >= 0 && node < s->T.n, TTN_EINVAL, "bad argument");
+  CK(cudaSetDevice(s->device));
+  CK(cudaMemcpy(s->node(node), data, s->T.size(node) * sizeof(double2), cudaMemcpyHostToDevice));
+  TTN_API_END
+}
+int ttn_state_download_node(ttn_state* s, int node, double* data) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(s && data && node >= 0 && node < s->T.n, TTN_EINVAL, "bad argument");
+  CK(cudaSetDevice(s->device));
+  CK(cudaMemcpy(data, s->node(node), s->T.size(node) * sizeof(double2), cudaMemcpyDeviceToHost));
+  TTN_API_END
+}
+int ttn_state_upload(ttn_state* s, const double* data) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(s && data, TTN_EINVAL, "bad argument");
+  CK(cudaSetDevice(s->device));
+  size_t o = 0;
+  for (int i = 0; i < s->T.n; ++i) {
+    CK(cudaMemcpy(s->node(i), data + 2 * o, s->T.size(i) * sizeof(double2), cudaMemcpyHostToDevice));
+    o += s->T.size(i);
+  }
+  TTN_API_END
+}
+int ttn_state_download(ttn_state* s, double* data) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(s && data, TTN_EINVAL, "bad argument");
+  CK(cudaSetDevice(s->device));
+  size_t o = 0;
+  for (int i = 0; i < s->T.n; ++i) {
+    CK(cudaMemcpy(data + 2 * o, s->node(i), s->T.size(i) * sizeof(double2), cudaMemcpyDeviceToHost));
+    o += s->T.size(i);
+  }
+  TTN_API_END
+}
+
+// The spin-boson driver's start state, src/spin_boson.cpp:584-649.
+int ttn_state_init_product(ttn_state* s, const double* psi0, unsigned int seed) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(s, TTN_EINVAL, "null state");
+  const ttn::Tree& T = s->T;
+  std::mt19937 rng(seed);
+  std::vector<double> host;
+  for (int i = 0; i < T.n; ++i) {
+    const long long d = T.dimen[i];
+    const int r = T.hrank[i];
+    std::vector<ttn::cd> A((size_t)d * r, 0.0);
+    if (T.leaf(i)) {
+      std::vector<std::vector<ttn::cd>> ct(r, std::vector<ttn::cd>(d, 0.0));
+      if (T.leaf_mode[i] == 0 && psi0) {
+        for (long long j = 0; j < d; ++j) ct[0][j] = ttn::cd(psi0[2 * j], psi0[2 * j + 1]);
+      } else {
+        ct[0][0] = 1.0;
+      }
+      std::uniform_real_distribution<double> dist(0, 2.0 * std::acos(-1.0));
+      std::normal_distribution<double> length_dist(0, 1);
+      for (int k = 1; k < r; ++k) {
+        bool done = false;
+        while (!done) {
+          for (long long j = 0; j < d; ++j) {
+            double theta = dist(rng);
+            ct[k][j] = length_dist(rng) * ttn::cd(std::cos(theta), std::sin(theta));
+          }
+          ttn::cd nn = 0.0;
+          for (auto& z : ct[k]) nn += std::conj(z) * z;
+          ttn::cd sn = std::sqrt(nn);
+          for (auto& z : ct[k]) z /= sn;
+          for (int q = 0; q < k; ++q) {
+            ttn::cd dp = 0.0;
+            for (long long j = 0; j < d; ++j) dp += std::conj(ct[q][j]) * ct[k][j];
+            for (long long j = 0; j < d; ++j) ct[k][j] -= dp * ct[q][j];
+          }
+          double norm = 0.0;
+          for (auto& z : ct[k]) norm += (std::conj(z) * z).real();
+          norm = std::sqrt(norm);
+          if (norm > 1e-12) {
+            for (auto& z : ct[k]) z /= norm;
+            done = true;
+          }
+        }
+      }
+      for (long long j = 0; j < d; ++j)
+        for (int k = 0; k < r; ++k) A[(size_t)j * r + k] = ct[k][j];
+    } else if (i != 0) {
+      for (long long j = 0; j < d; ++j)
+        for (int k = 0; k < r; ++k) A[(size_t)j * r + k] = (j == k) ? 1.0 : 0.0;
+    } else {
+      A[0] = 1.0;
+    }
+    for (auto& z : A) { host.push_back(z.real()); host.push_back(z.imag()); }
+  }
+  int rc = ttn_state_upload(s, host.data());
+  if (rc != TTN_OK) return rc;
+  TTN_API_END
+}
+
+int ttn_integrator_create(const ttn_tree* t, const ttn_sop* h, const ttn_integ_cfg* cfg, ttn_integrator** out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(t && h && cfg && out, TTN_EINVAL, "null argument");
+  TTN_REQUIRE(cfg->krylov_dim >= 2 && cfg->krylov_dim <= ttn::kKrylovMax, TTN_EINVAL, "krylov_dim must be in [2, 64]");
+  TTN_REQUIRE(cfg->krylov_tol > 0.0, TTN_EINVAL, "krylov_tol must be positive");
+  TTN_REQUIRE(cfg->precision == TTN_PREC_FP64 || cfg->precision == TTN_PREC_MIXED, TTN_EINVAL, "unknown precision");
+  TTN_REQUIRE(h->H.nmodes == t->T.nleaves, TTN_EINVAL, "operator and tree disagree on the number of modes");
+  for (int m = 0; m < h->H.nmodes; ++m)
+    TTN_REQUIRE(h->H.mode_dim[m] == t->T.leaf_dim[t->T.mode_node[m]], TTN_EINVAL, "operator and tree disagree on a mode dimension");
+  auto* it = new ttn_integrator();
+  try {
+    it->I.T = t->T;
+    it->I.H = h->H;
+    it->I.cfg = *cfg;
+    it->I.device = cfg->device;
+    it->I.setup();
+  } catch (...) {
+    delete it;
+    throw;
+  }
+  *out = it;
+  TTN_API_END
+}
+int ttn_integrator_destroy(ttn_integrator* it) { delete it; return TTN_OK; }
+int ttn_integrator_set_dt(ttn_integrator* it, double dt) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && std::isfinite(dt) && dt > 0.0, TTN_EINVAL, "dt must be positive");
+  it->I.dt = dt;
+  TTN_API_END
+}
+int ttn_integrator_dt(const ttn_integrator* it, double* out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && out, TTN_EINVAL, "null argument");
+  *out = it->I.dt;
+  TTN_API_END
+}
+int ttn_integrator_t(const ttn_integrator* it, double* out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && out, TTN_EINVAL, "null argument");
+  *out = it->I.dt * it->I.nsteps;
+  TTN_API_END
+}
+int ttn_integrator_step(ttn_integrator* it, ttn_state* psi, double cre, double cim, double* dt_out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi, TTN_EINVAL, "null argument");
+  TTN_REQUIRE(it->I.dt > 0.0, TTN_EINVAL, "set dt before stepping");
+  ttn::check_same_tree(it->I.T, psi->T);
+  CK(cudaSetDevice(it->I.device));
+  double dt = it->I.dt;
+  it->I.step(psi, dt, ttn::cd(cre, cim));
+  if (dt_out) *dt_out = dt;
+  TTN_API_END
+}
+int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && out, TTN_EINVAL, "null argument");
+  *out = it->I.nh;
+  TTN_API_END
+}
+int ttn_integrator_reset(ttn_integrator* it) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it, TTN_EINVAL, "null argument");
+  it->I.nsteps = 0;
+  it->I.nh = 0;
+  TTN_API_END
+}
+int ttn_integrator_synchronize(ttn_integrator* it) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it, TTN_EINVAL, "null argument");
+  CK(cudaStreamSynchronize(it->I.stream));
+  TTN_API_END
+}
+
+int ttn_expect_leaf(ttn_integrator* it, ttn_state* psi, int mode, const double* op, double* re, double* im) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi, TTN_EINVAL, "null argument");
+  ttn::check_same_tree(it->I.T, psi->T);
+  CK(cudaSetDevice(it->I.device));
+  const double2* dop = nullptr;
+  if (op) {
+    TTN_REQUIRE(mode >= 0 && mode < it->I.H.nmodes, TTN_EINVAL, "mode out of range");
+    int d = it->I.H.mode_dim[mode];
+    TTN_REQUIRE((long long)d * d <= it->I.ldv, TTN_ECAPACITY, "observable operator larger than the work buffer");
+    CK(cudaMemcpyAsync(it->I.w3, op, (size_t)d * d * sizeof(double2), cudaMemcpyHostToDevice, it->I.stream));
+    dop = it->I.w3;
+  }
+  ttn::cd v = it->I.expect(psi, mode, dop);
+  if (re) *re = v.real();
+  if (im) *im = v.imag();
+  TTN_API_END
+}
+int ttn_norm2(ttn_integrator* it, ttn_state* psi, double* out) {
+  double re = 0, im = 0;
+  int rc = ttn_expect_leaf(it, psi, 0, nullptr, &re, &im);
+  if (rc == TTN_OK && out) *out = re;
+  return rc;
+}
+
+int ttn_debug_refresh_env(ttn_integrator* it, ttn_state* psi) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi, TTN_EINVAL, "null argument");
+  ttn::check_same_tree(it->I.T, psi->T);
+  CK(cudaSetDevice(it->I.device));
+  auto& I = it->I;
+  for (int id = I.T.n - 1; id >= 1; --id) I.update_spf(id, psi->node(id));
+  for (int id = 1; id < I.T.n; ++id) I.update_mf(id, psi->node(I.T.parent[id]));
+  CK(cudaStreamSynchronize(I.stream));
+  CK(cudaGetLastError());
+  TTN_API_END
+}
+int ttn_debug_heff(ttn_integrator* it, int node, const double* v, double* out) {
+  TTN_API_BEGIN
+  auto& I = it->I;
+  TTN_REQUIRE(node >= 0 && node < I.T.n && v && out, TTN_EINVAL, "bad argument");
+  CK(cudaSetDevice(I.device));
+  const long long n = I.T.size(node);
+  CK(cudaMemcpyAsync(I.V, v, n * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  I.heff(node, I.V, I.p);
+  CK(cudaMemcpyAsync(out, I.p, n * sizeof(double2), cudaMemcpyDeviceToHost, I.stream));
+  CK(cudaStreamSynchronize(I.stream));
+  CK(cudaGetLastError());
+  TTN_API_END
+}
+int ttn_debug_expm_node(ttn_integrator* it, int node, double tau, double cre, double cim, double* v, long long* napps) {
+  TTN_API_BEGIN
+  auto& I = it->I;
+  TTN_REQUIRE(node >= 0 && node < I.T.n && v, TTN_EINVAL, "bad argument");
+  CK(cudaSetDevice(I.device));
+  const long long n = I.T.size(node);
+  CK(cudaMemcpyAsync(I.w4, v, n * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  // w4 is a gauge scratch; the exponential itself uses V, p, w1-w3
+  long long before = I.nh;
+  I.expm([&](const double2* a, double2* o) { I.heff(node, a, o); }, I.w4, n, tau, ttn::cd(cre, cim), true);
+  CK(cudaMemcpyAsync(v, I.w4, n * sizeof(double2), cudaMemcpyDeviceToHost, I.stream));
+  CK(cudaStreamSynchronize(I.stream));
+  if (napps) *napps = I.nh - before;
+  I.nh = before;
+  TTN_API_END
+}
+int ttn_debug_num_groups(ttn_integrator* it, int node, int* out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && out && node >= 0 && node < it->I.T.n, TTN_EINVAL, "bad argument");
+  *out = (int)it->I.G[node].size();
+  TTN_API_END
+}
+int ttn_debug_get_env(ttn_integrator* it, int node, int group, int which, double* out) {
+  TTN_API_BEGIN
+  auto& I = it->I;
+  TTN_REQUIRE(node >= 0 && node < I.T.n && group >= 0 && group < (int)I.G[node].size() && out, TTN_EINVAL, "bad argument");
+  const auto& g = I.G[node][group];
+  const double2* p = which == 0 ? g.spf_dev : g.mf_dev;
+  TTN_REQUIRE(p, TTN_EINVAL, "that environment matrix is the identity");
+  const int r = I.T.hrank[node];
+  CK(cudaMemcpyAsync(out, p, (size_t)r * r * sizeof(double2), cudaMemcpyDeviceToHost, I.stream));
+  CK(cudaStreamSynchronize(I.stream));
+  TTN_API_END
+}
+int ttn_debug_qr(int m, int n, double* a, double* r, int device) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(a && r && m >= n && n >= 1 && n <= ttn::kQrMaxCols, TTN_EINVAL, "bad QR shape");
+  CK(cudaSetDevice(device));
+  ttn::DevBuf buf;
+  buf.alloc(((size_t)m * n + (size_t)n * n + ttn::kQrMaxCols) * sizeof(double2));
+  double2* dA = buf.as<double2>();
+  double2* dR = dA + (size_t)m * n;
+  double2* dt = dR + (size_t)n * n;
+  CK(cudaMemcpy(dA, a, (size_t)m * n * sizeof(double2), cudaMemcpyHostToDevice));
+  ttn::householder_qr(dA, m, n, dR, 0, dt, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(a, dA, (size_t)m * n * sizeof(double2), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(r, dR, (size_t)n * n * sizeof(double2), cudaMemcpyDeviceToHost));
+  TTN_API_END
+}
+
+}  // extern "C"

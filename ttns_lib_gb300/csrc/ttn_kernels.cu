@@ -1,0 +1,845 @@
+// FP64 device kernels of the sweep (the plain complex128 form).
+//
+//   * k_zgemm: complex FP64 GEMM with per-operand index maps.  One kernel covers the
+//     mode contraction res(a,i,b) = sum_j S(i,j) A(a,j,b) of
+//     include/ttns_lib/tdvp_core/kronecker_product_operator_helper.hpp:212-315, the
+//     mean-field product A * mf^T of projector_splitting_evolution_functions.hpp:33-249,
+//     the spf reduction A^H X of single_particle_operator.hpp:49-86 and the mean-field
+//     reduction contract(conj(A),0,2,HA,0,2) of mean_field_operator.hpp:84-117 (the last
+//     two by split-K with a deterministic second pass).
+//   * Lanczos passes with every block re-reducing the previous pass's partials, so the
+//     scalar recurrences need no host round trip; an on-device step controller
+//     (Sidje's Expokit scheme) decides sub-steps and the combination coefficients.
+//   * Householder QR with LAPACK zlarfg conventions for the gauge moves of
+//     root_to_leaf_decomposition.hpp:113-183 and leaf_to_root_decomposition.hpp:57-101.
+#include "ttn_kernels.cuh"
+
+#include <cmath>
+#include <cstdio>
+
+namespace ttn {
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// conj(a) * b
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
+  return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {
+  c.x = fma(a.x, b.x, c.x);
+  c.x = fma(-a.y, b.y, c.x);
+  c.y = fma(a.x, b.y, c.y);
+  c.y = fma(a.y, b.x, c.y);
+  return c;
+}
+__device__ __forceinline__ double2 cscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double2 warp_sum2(double2 v) {
+  v.x = warp_sum(v.x);
+  v.y = warp_sum(v.y);
+  return v;
+}
+
+// =====================================================================================
+// complex FP64 GEMM
+// =====================================================================================
+namespace {
+constexpr int GT_M = 32, GT_N = 32, GT_K = 16, GT_THREADS = 256;
+
+__device__ __forceinline__ double2 ld_op(const ZOperand& o, long long outer, long long k) {
+  long long off = outer * o.s0 + (k / o.kdiv) * o.k1 + (k % o.kdiv) * o.k2;
+  double2 v = o.p[off];
+  if (o.cj) v.y = -v.y;
+  return v;
+}
+
+__global__ void __launch_bounds__(GT_THREADS) k_zgemm(ZGemm g, double2* part, int ksplit) {
+  __shared__ double2 As[GT_K][GT_M + 1];
+  __shared__ double2 Bs[GT_K][GT_N + 1];
+  const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+  const long long i0 = (long long)blockIdx.y * GT_M, j0 = (long long)blockIdx.x * GT_N;
+  const int z = blockIdx.z;
+  ZOperand A = g.A, B = g.B;
+  double2* C = g.C;
+  long long kb = 0, ke = g.K;
+  if (ksplit > 1) {
+    long long chunk = (g.K + ksplit - 1) / ksplit;
+    kb = (long long)z * chunk;
+    ke = min((long long)g.K, kb + chunk);
+  } else {
+    A.p += (long long)z * g.bsA;
+    B.p += (long long)z * g.bsB;
+    C += (long long)z * g.bsC;
+  }
+  double2 acc[2][2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) acc[u][v] = make_double2(0.0, 0.0);
+
+  for (long long k0 = kb; k0 < ke; k0 += GT_K) {
+    for (int e = tid; e < GT_M * GT_K; e += GT_THREADS) {
+      int ii, kk;
+      if (A.kfast) { kk = e % GT_K; ii = e / GT_K; } else { ii = e % GT_M; kk = e / GT_M; }
+      long long i = i0 + ii, k = k0 + kk;
+      As[kk][ii] = (i < g.M && k < ke) ? ld_op(A, i, k) : make_double2(0.0, 0.0);
+    }
+    for (int e = tid; e < GT_N * GT_K; e += GT_THREADS) {
+      int jj, kk;
+      if (B.kfast) { kk = e % GT_K; jj = e / GT_K; } else { jj = e % GT_N; kk = e / GT_N; }
+      long long j = j0 + jj, k = k0 + kk;
+      Bs[kk][jj] = (j < g.N && k < ke) ? ld_op(B, j, k) : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GT_K; ++kk) {
+      double2 a0 = As[kk][ty], a1 = As[kk][ty + 16];
+      double2 b0 = Bs[kk][tx], b1 = Bs[kk][tx + 16];
+      acc[0][0] = cfma(a0, b0, acc[0][0]);
+      acc[0][1] = cfma(a0, b1, acc[0][1]);
+      acc[1][0] = cfma(a1, b0, acc[1][0]);
+      acc[1][1] = cfma(a1, b1, acc[1][1]);
+    }
+    __syncthreads();
+  }
+  const bool has_beta = (g.beta.x != 0.0 || g.beta.y != 0.0);
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      long long i = i0 + ty + 16 * u, j = j0 + tx + 16 * v;
+      if (i >= g.M || j >= g.N) continue;
+      if (ksplit > 1) {
+        part[((long long)z * g.M + i) * g.N + j] = acc[u][v];
+      } else {
+        double2* c = C + i * g.ci + j * g.cj;
+        double2 r = cmul(g.alpha, acc[u][v]);
+        if (has_beta) r = cfma(g.beta, *c, r);
+        *c = r;
+      }
+    }
+}
+
+__global__ void k_zgemm_reduce(ZGemm g, const double2* part, int ksplit) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long total = (long long)g.M * g.N;
+  if (idx >= total) return;
+  long long i = idx / g.N, j = idx % g.N;
+  double2 s = make_double2(0.0, 0.0);
+  for (int q = 0; q < ksplit; ++q) s = cadd(s, part[(long long)q * total + idx]);
+  double2* c = g.C + i * g.ci + j * g.cj;
+  double2 r = cmul(g.alpha, s);
+  if (g.beta.x != 0.0 || g.beta.y != 0.0) r = cfma(g.beta, *c, r);
+  *c = r;
+}
+
+int choose_split(int M, int N, int K, int batch) {
+  if (batch != 1) return 1;
+  long long tiles = (long long)((M + GT_M - 1) / GT_M) * ((N + GT_N - 1) / GT_N);
+  if (tiles >= 304 || K < 256) return 1;
+  long long want = (608 + tiles - 1) / tiles;
+  long long maxs = (K + 127) / 128;
+  long long s = want < maxs ? want : maxs;
+  if (s > 512) s = 512;
+  return s < 1 ? 1 : (int)s;
+}
+}  // namespace
+
+size_t zgemm_split_workspace_bytes(int M, int N, int K) {
+  int s = choose_split(M, N, K, 1);
+  return s > 1 ? (size_t)s * M * N * sizeof(double2) : 0;
+}
+
+void zgemm(const ZGemm& g, double2* ws, size_t ws_bytes, cudaStream_t s) {
+  if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return;
+  int ksplit = choose_split(g.M, g.N, g.K, g.batch);
+  while (ksplit > 1 && (size_t)ksplit * g.M * g.N * sizeof(double2) > ws_bytes) ksplit /= 2;
+  if (ksplit == 1 && g.batch > 65535) {
+    // grid.z is limited to 65535: issue the batch in chunks
+    for (int b0 = 0; b0 < g.batch; b0 += 65535) {
+      ZGemm c = g;
+      c.batch = (g.batch - b0 < 65535) ? g.batch - b0 : 65535;
+      c.A.p += (long long)b0 * g.bsA;
+      c.B.p += (long long)b0 * g.bsB;
+      c.C += (long long)b0 * g.bsC;
+      zgemm(c, ws, ws_bytes, s);
+    }
+    return;
+  }
+  dim3 grid((g.N + GT_N - 1) / GT_N, (g.M + GT_M - 1) / GT_M, ksplit > 1 ? ksplit : g.batch);
+  k_zgemm<<<grid, GT_THREADS, 0, s>>>(g, ws, ksplit);
+  if (ksplit > 1) {
+    long long total = (long long)g.M * g.N;
+    k_zgemm_reduce<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(g, ws, ksplit);
+  }
+}
+
+// =====================================================================================
+// Lanczos vector passes
+// =====================================================================================
+namespace {
+constexpr int VT = 256;       // threads per block
+constexpr int VQ = 72;        // max vectors reduced in one pass
+constexpr int VMAXB = 512;    // max blocks of a pass
+
+// Block-reduce nq complex partials held as (per-warp) shared sums; writes part[block*nq + q].
+struct RedSmem {
+  double2 w[VT / 32][VQ];
+};
+
+__device__ void block_store_partials(RedSmem& sm, int nq, double2* part) {
+  __syncthreads();
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int w = 0; w < VT / 32; ++w) s = cadd(s, sm.w[w][q]);
+    part[(long long)blockIdx.x * nq + q] = s;
+  }
+}
+
+// Every block sums the partials of the previous pass in the same order (deterministic).
+__device__ double2 sum_partials(const double2* part, int nblocks, int nq, int q) {
+  double2 s = make_double2(0.0, 0.0);
+  for (int b = 0; b < nblocks; ++b) s = cadd(s, part[(long long)b * nq + q]);
+  return s;
+}
+
+__global__ void k_norm_partial(const double2* __restrict__ x, long long n, double2* part) {
+  __shared__ RedSmem sm;
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    double2 v = x[i];
+    s += v.x * v.x + v.y * v.y;
+  }
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sm.w[threadIdx.x >> 5][0] = make_double2(s, 0.0);
+  block_store_partials(sm, 1, part);
+}
+
+// V0 = y / ||y||; block 0 records beta.
+__global__ void k_begin(KrylovCtl* ctl, const double2* __restrict__ y, double2* __restrict__ V0, long long n,
+                        const double2* part, int nparts) {
+  __shared__ double sbeta;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nparts; ++b) s += part[b].x;
+    sbeta = sqrt(s);
+  }
+  __syncthreads();
+  double beta = sbeta;
+  double inv = beta > 0.0 ? 1.0 / beta : 0.0;
+  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
+    V0[i] = cscale(inv, y[i]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->beta = beta;
+    ctl->mb = ctl->m;
+    ctl->k1 = 2;
+    ctl->bet[0] = 0.0;
+    if (!(beta > 0.0) || !isfinite(beta)) {
+      ctl->done = 1;
+      if (!isfinite(beta)) ctl->err |= 2;
+    }
+  }
+}
+
+// pass 1: partial <V_j, p>
+__global__ void k_orth1(const double2* __restrict__ Vj, const double2* __restrict__ p, long long n, double2* part) {
+  __shared__ RedSmem sm;
+  double2 s = make_double2(0.0, 0.0);
+  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
+    s = cadd(s, cmulc(Vj[i], p[i]));
+  s = warp_sum2(s);
+  if ((threadIdx.x & 31) == 0) sm.w[threadIdx.x >> 5][0] = s;
+  block_store_partials(sm, 1, part);
+}
+
+// pass 2: alpha = Re<V_j,p>; p -= alpha V_j + bet_j V_{j-1}; partial h_q = <V_q, p>, q <= j
+__global__ void k_orth2(KrylovCtl* ctl, int j, const double2* __restrict__ V, long long ldv, double2* __restrict__ p,
+                        long long n, const double2* part_in, int nparts, double2* part_out) {
+  __shared__ RedSmem sm;
+  __shared__ double salpha;
+  if (threadIdx.x == 0) salpha = sum_partials(part_in, nparts, 1, 0).x;
+  __syncthreads();
+  const double a = salpha;
+  const double bj = (j > 0) ? ctl->bet[j] : 0.0;
+  const double2* Vj = V + (long long)j * ldv;
+  const double2* Vm = V + (long long)(j > 0 ? j - 1 : 0) * ldv;
+  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    double2 x = p[i];
+    double2 vj = Vj[i];
+    x.x -= a * vj.x;
+    x.y -= a * vj.y;
+    if (j > 0) {
+      double2 vm = Vm[i];
+      x.x -= bj * vm.x;
+      x.y -= bj * vm.y;
+    }
+    p[i] = x;
+  }
+  // p was only touched element-wise by this thread; dots use the updated values
+  for (int q = 0; q <= j; ++q) {
+    const double2* Vq = V + (long long)q * ldv;
+    double2 s = make_double2(0.0, 0.0);
+    for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
+      s = cadd(s, cmulc(Vq[i], p[i]));
+    s = warp_sum2(s);
+    if ((threadIdx.x & 31) == 0) sm.w[threadIdx.x >> 5][q] = s;
+  }
+  block_store_partials(sm, j + 1, part_out);
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->alpha[j] = a;
+}
+
+// pass 3: p -= sum_q h_q V_q; partial ||p||^2
+__global__ void k_orth3(int j, const double2* __restrict__ V, long long ldv, double2* __restrict__ p, long long n,
+                        const double2* part_in, int nparts, double2* part_out) {
+  __shared__ RedSmem sm;
+  __shared__ double2 h[VQ];
+  for (int q = threadIdx.x; q <= j; q += blockDim.x) h[q] = sum_partials(part_in, nparts, j + 1, q);
+  __syncthreads();
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    double2 x = p[i];
+    for (int q = 0; q <= j; ++q) {
+      double2 v = V[(long long)q * ldv + i];
+      double2 hv = cmul(h[q], v);
+      x = csub(x, hv);
+    }
+    p[i] = x;
+    s += x.x * x.x + x.y * x.y;
+  }
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sm.w[threadIdx.x >> 5][0] = make_double2(s, 0.0);
+  block_store_partials(sm, 1, part_out);
+}
+
+// pass 4: beta_{j+1} = ||p||; breakdown test; V_{j+1} = p / beta (or 0)
+__global__ void k_orth4(KrylovCtl* ctl, int j, double2* __restrict__ V, long long ldv, const double2* __restrict__ p,
+                        long long n, const double2* part_in, int nparts) {
+  __shared__ double sb;
+  __shared__ int sbreak;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nparts; ++b) s += part_in[b].x;
+    double beta = sqrt(s);
+    double anorm = 0.0;
+    for (int q = 0; q <= j; ++q) {
+      double nb = (q < j) ? ctl->bet[q + 1] : beta;
+      double v = fabs(ctl->alpha[q]) + ctl->bet[q] + nb;
+      anorm = v > anorm ? v : anorm;
+    }
+    sb = beta;
+    sbreak = (beta <= 1e-14 * (1.0 + anorm)) ? 1 : 0;
+  }
+  __syncthreads();
+  const double beta = sb;
+  const int brk = sbreak;
+  const double inv = brk ? 0.0 : 1.0 / beta;
+  double2* Vn = V + (long long)(j + 1) * ldv;
+  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
+    Vn[i] = cscale(inv, p[i]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->bet[j + 1] = brk ? 0.0 : beta;
+    if (brk && ctl->mb == ctl->m) {
+      ctl->mb = j + 1;
+      ctl->k1 = 0;
+    }
+    if (!isfinite(beta)) ctl->err |= 2;
+  }
+}
+
+// ---- small dense math for the controller (single thread) ---------------------------
+// Implicit-QL eigen-decomposition of a symmetric tridiagonal matrix (EISPACK tql2
+// scheme).  z is n x n row-major, columns are eigenvectors.
+__device__ int dev_tql2(int n, double* d, double* e, double* z) {
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < n; ++k) z[i * n + k] = (i == k) ? 1.0 : 0.0;
+  for (int l = 0; l < n; ++l) {
+    int iter = 0, m;
+    for (;;) {
+      for (m = l; m < n - 1; ++m) {
+        double dd = fabs(d[m]) + fabs(d[m + 1]);
+        if (fabs(e[m]) <= 1e-300 + 2.220446049250313e-16 * dd) break;
+      }
+      if (m == l) break;
+      if (++iter > 60) return 1;
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = hypot(g, 1.0);
+      g = d[m] - d[l] + e[l] / (g + (g >= 0.0 ? fabs(r) : -fabs(r)));
+      double s = 1.0, c = 1.0, p = 0.0;
+      bool underflow = false;
+      for (int i = m - 1; i >= l; --i) {
+        double f = s * e[i], b = c * e[i];
+        r = hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {
+          d[i + 1] -= p;
+          e[m] = 0.0;
+          underflow = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - p;
+        r = (d[i] - g) * s + 2.0 * c * b;
+        p = s * r;
+        d[i + 1] = g + p;
+        g = c * r - b;
+        for (int k = 0; k < n; ++k) {
+          f = z[k * n + i + 1];
+          z[k * n + i + 1] = s * z[k * n + i] + c * f;
+          z[k * n + i] = c * z[k * n + i] - s * f;
+        }
+      }
+      if (underflow) continue;
+      d[l] -= p;
+      e[l] = g;
+      e[m] = 0.0;
+    }
+  }
+  return 0;
+}
+
+__device__ double2 cexp_d(double2 x) {
+  double ex = exp(x.x);
+  double sn, cs;
+  sincos(x.y, &sn, &cs);
+  return make_double2(ex * cs, ex * sn);
+}
+__device__ double cabs_d(double2 x) { return hypot(x.x, x.y); }
+__device__ double2 cdiv_d(double2 a, double2 b) {
+  double den = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+// phi_1(x) = (e^x - 1)/x, phi_2(x) = (e^x - 1 - x)/x^2
+__device__ double2 dphi1(double2 x) {
+  if (cabs_d(x) < 0.5) {
+    double2 s = make_double2(0.0, 0.0), t = make_double2(1.0, 0.0);
+    for (int k = 1; k <= 18; ++k) {
+      s = cadd(s, t);
+      t = cscale(1.0 / double(k + 1), cmul(t, x));
+    }
+    return s;
+  }
+  double2 ex = cexp_d(x);
+  return cdiv_d(make_double2(ex.x - 1.0, ex.y), x);
+}
+__device__ double2 dphi2(double2 x) {
+  if (cabs_d(x) < 0.5) {
+    double2 s = make_double2(0.0, 0.0), t = make_double2(0.5, 0.0);
+    for (int k = 2; k <= 20; ++k) {
+      s = cadd(s, t);
+      t = cscale(1.0 / double(k + 1), cmul(t, x));
+    }
+    return s;
+  }
+  double2 ex = cexp_d(x);
+  return cdiv_d(make_double2(ex.x - 1.0 - x.x, ex.y - x.y), cmul(x, x));
+}
+
+__global__ void k_avnorm(KrylovCtl* ctl, const double2* part, int nparts) {
+  if (threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int b = 0; b < nparts; ++b) s += part[b].x;
+  ctl->avnorm = sqrt(s);
+}
+
+// Expokit step control on the mb x mb tridiagonal (single thread; m <= 64).
+__global__ void k_control(KrylovCtl* ctl) {
+  __shared__ double z[64 * 64];
+  __shared__ double d[64], e[64];
+  __shared__ double2 F[66];
+  if (threadIdx.x != 0) return;
+  if (ctl->done) {
+    for (int q = 0; q < 2 * 72; ++q) ctl->coef[q] = 0.0;
+    return;
+  }
+  const int m = ctl->m, mb = ctl->mb, k1 = ctl->k1;
+  const double tol = ctl->tol, gamma = 0.9, delta = 1.2;
+  const double beta = ctl->beta, avnorm = ctl->avnorm;
+  double t_step = fmin(ctl->t_out - ctl->t_now, ctl->t_new);
+  if (k1 == 0) t_step = ctl->t_out - ctl->t_now;
+  for (int i = 0; i < mb; ++i) d[i] = ctl->alpha[i];
+  for (int i = 0; i + 1 < mb; ++i) e[i] = ctl->bet[i + 1];
+  e[mb - 1] = 0.0;
+  if (dev_tql2(mb, d, e, z)) {
+    ctl->err |= 4;
+    ctl->done = 1;
+    return;
+  }
+  const double2 cf = make_double2(ctl->cf_re, ctl->cf_im);
+  double err_loc = 0.0, xm = 1.0 / m;
+  int ireject = 0;
+  for (;;) {
+    double2 zc = cscale(ctl->sgn * t_step, cf);
+    for (int i = 0; i < mb; ++i) {
+      double2 s = make_double2(0.0, 0.0);
+      for (int q = 0; q < mb; ++q) {
+        double2 ex = cexp_d(cscale(d[q], zc));
+        s = cadd(s, cscale(z[i * mb + q] * z[q], ex));
+      }
+      F[i] = s;
+    }
+    if (k1 == 0) {
+      err_loc = 1e-14;
+      break;
+    }
+    double2 f1 = make_double2(0.0, 0.0), f2 = make_double2(0.0, 0.0);
+    for (int q = 0; q < mb; ++q) {
+      double2 x = cscale(d[q], zc);
+      double w = z[(mb - 1) * mb + q] * z[q];
+      f1 = cadd(f1, cscale(w, cmul(zc, dphi1(x))));
+      f2 = cadd(f2, cscale(w, cmul(cmul(zc, zc), dphi2(x))));
+    }
+    F[mb] = cscale(ctl->bet[mb], f1);
+    F[mb + 1] = cscale(ctl->bet[mb], f2);
+    double p1 = cabs_d(F[mb]) * beta, p2 = cabs_d(F[mb + 1]) * beta * avnorm;
+    if (p1 > 10.0 * p2) {
+      err_loc = p2;
+      xm = 1.0 / m;
+    } else if (p1 > p2) {
+      err_loc = p1 * p2 / (p1 - p2);
+      xm = 1.0 / m;
+    } else {
+      err_loc = p1;
+      xm = 1.0 / (m - 1);
+    }
+    if (err_loc <= delta * t_step * tol) break;
+    if (ireject == 10) {
+      ctl->err |= 1;
+      ctl->done = 1;
+      return;
+    }
+    t_step = gamma * t_step * pow(t_step * tol / err_loc, xm);
+    double sc = pow(10.0, floor(log10(t_step)) - 1.0);
+    t_step = ceil(t_step / sc) * sc;
+    ++ireject;
+  }
+  if (!isfinite(t_step) || !(t_step > 0.0) || !isfinite(err_loc)) {
+    ctl->err |= 8;
+    ctl->done = 1;
+    return;
+  }
+  const int mx = mb + (k1 > 1 ? k1 - 1 : 0);
+  for (int q = 0; q < 72; ++q) {
+    double2 c = (q < mx) ? cscale(beta, F[q]) : make_double2(0.0, 0.0);
+    ctl->coef[2 * q] = c.x;
+    ctl->coef[2 * q + 1] = c.y;
+  }
+  ctl->t_now += t_step;
+  if (k1 != 0) {
+    double tn = gamma * t_step * pow(t_step * tol / fmax(err_loc, 1e-300), xm);
+    double sc = pow(10.0, floor(log10(tn)) - 1.0);
+    ctl->t_new = ceil(tn / sc) * sc;
+    if (!isfinite(ctl->t_new) || !(ctl->t_new > 0.0)) ctl->t_new = t_step;
+  }
+  ctl->napps += mb + (k1 != 0 ? 1 : 0);
+  ctl->substeps += 1;
+  if (ctl->t_now >= ctl->t_out) ctl->done = 1;
+}
+
+// y = sum_q c_q V_q
+__global__ void k_combine(const KrylovCtl* ctl, const double2* __restrict__ V, long long ldv, double2* __restrict__ y,
+                          long long n, int nq) {
+  __shared__ double2 c[VQ];
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) c[q] = make_double2(ctl->coef[2 * q], ctl->coef[2 * q + 1]);
+  __syncthreads();
+  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int q = 0; q < nq; ++q) s = cfma(c[q], V[(long long)q * ldv + i], s);
+    y[i] = s;
+  }
+}
+
+__global__ void k_init_ctl(KrylovCtl* ctl, int m, double tau, double cre, double cim, double tol) {
+  if (threadIdx.x != 0) return;
+  ctl->m = m;
+  ctl->t_out = fabs(tau);
+  ctl->sgn = tau >= 0.0 ? 1.0 : -1.0;
+  ctl->t_now = 0.0;
+  ctl->t_new = fabs(tau);
+  ctl->cf_re = cre;
+  ctl->cf_im = cim;
+  ctl->tol = tol;
+  ctl->done = (tau == 0.0) ? 1 : 0;
+  ctl->err = 0;
+  ctl->substeps = 0;
+  ctl->napps = 0;
+  ctl->mb = m;
+  ctl->k1 = 2;
+  for (int q = 0; q < 73; ++q) ctl->bet[q] = 0.0;
+  for (int q = 0; q < 72; ++q) ctl->alpha[q] = 0.0;
+}
+}  // namespace
+
+size_t lanczos_partial_bytes() { return (size_t)2 * VMAXB * VQ * sizeof(double2); }
+
+int vec_blocks(long long n) {
+  long long b = (n + VT * 4 - 1) / (VT * 4);
+  if (b < 1) b = 1;
+  if (b > VMAXB) b = VMAXB;
+  return (int)b;
+}
+
+void krylov_init_ctl(KrylovCtl* ctl, int m, double tau, double cre, double cim, double tol, cudaStream_t s) {
+  k_init_ctl<<<1, 32, 0, s>>>(ctl, m, tau, cre, cim, tol);
+}
+
+void krylov_begin(KrylovCtl* ctl, const double2* y, double2* V0, long long n, double2* part, cudaStream_t s) {
+  int nb = vec_blocks(n);
+  k_norm_partial<<<nb, VT, 0, s>>>(y, n, part);
+  k_begin<<<nb, VT, 0, s>>>(ctl, y, V0, n, part, nb);
+}
+
+void lanczos_orth(KrylovCtl* ctl, int j, double2* V, long long ldv, double2* p, long long n, double2* part,
+                  cudaStream_t s) {
+  int nb = vec_blocks(n);
+  double2* pa = part;
+  double2* pb = part + (size_t)VMAXB * VQ;
+  k_orth1<<<nb, VT, 0, s>>>(V + (long long)j * ldv, p, n, pa);
+  k_orth2<<<nb, VT, 0, s>>>(ctl, j, V, ldv, p, n, pa, nb, pb);
+  k_orth3<<<nb, VT, 0, s>>>(j, V, ldv, p, n, pb, nb, pa);
+  k_orth4<<<nb, VT, 0, s>>>(ctl, j, V, ldv, p, n, pa, nb);
+}
+
+void lanczos_avnorm(KrylovCtl* ctl, const double2* p, long long n, double2* part, cudaStream_t s) {
+  int nb = vec_blocks(n);
+  k_norm_partial<<<nb, VT, 0, s>>>(p, n, part);
+  k_avnorm<<<1, 32, 0, s>>>(ctl, part, nb);
+}
+
+void krylov_control(KrylovCtl* ctl, cudaStream_t s) { k_control<<<1, 32, 0, s>>>(ctl); }
+
+void krylov_combine(KrylovCtl* ctl, const double2* V, long long ldv, double2* y, long long n, int nq,
+                    cudaStream_t s) {
+  int nb = vec_blocks(n);
+  k_combine<<<nb, VT, 0, s>>>(ctl, V, ldv, y, n, nq);
+}
+
+// =====================================================================================
+// Householder QR (single CTA)
+// =====================================================================================
+namespace {
+constexpr int QT = 1024;
+constexpr int QMAXN = 64;
+
+__device__ double block_sum_qr(double v, double* red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
+    red[32] = s;
+  }
+  __syncthreads();
+  s = red[32];
+  __syncthreads();
+  return s;
+}
+
+// Trailing reflector application: for c in (c0, n): w_c = sum_{r >= r0} conj(v_r) M[r][c]
+// with v_{r0} = 1 and v_r = M[r][col] below; then M[r][c] -= v_r * (f * w_c).
+// conjf: use conj(tau) (factorisation) or tau (forming Q).
+__device__ void apply_reflector(double2* M, long long m, int n, int col, long long r0, int c0, double2 tau,
+                                bool conjt, double2 (*wacc)[QMAXN], double2* wsh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int nc = n - c0;
+  if (nc <= 0) return;
+  // per-warp partial sums over a strided set of rows; lanes own columns
+  double2 acc[QMAXN / 32];
+#pragma unroll
+  for (int u = 0; u < QMAXN / 32; ++u) acc[u] = make_double2(0.0, 0.0);
+  for (long long r = r0 + w; r < m; r += nw) {
+    double2 v = (r == r0) ? make_double2(1.0, 0.0) : M[r * n + col];
+#pragma unroll
+    for (int u = 0; u < QMAXN / 32; ++u) {
+      int c = c0 + lane + 32 * u;
+      if (c < n) acc[u] = cadd(acc[u], cmulc(v, M[r * n + c]));
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < QMAXN / 32; ++u) {
+    int c = lane + 32 * u;
+    if (c < nc) wacc[w][c] = acc[u];
+  }
+  __syncthreads();
+  double2 t = conjt ? make_double2(tau.x, -tau.y) : tau;
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int k = 0; k < nw; ++k) s = cadd(s, wacc[k][c]);
+    wsh[c] = cmul(t, s);
+  }
+  __syncthreads();
+  const long long rows = m - r0;
+  for (long long e = threadIdx.x; e < rows * nc; e += blockDim.x) {
+    long long r = r0 + e / nc;
+    int c = c0 + (int)(e % nc);
+    double2 v = (r == r0) ? make_double2(1.0, 0.0) : M[r * n + col];
+    M[r * n + c] = csub(M[r * n + c], cmul(v, wsh[c - c0]));
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(QT) k_householder_qr(double2* M, long long m, int n, double2* R, int Rt,
+                                                       double2* tau) {
+  __shared__ double2 wacc[QT / 32][QMAXN];
+  __shared__ double2 wsh[QMAXN];
+  __shared__ double red[33];
+  __shared__ double2 s_tau, s_scal, s_beta;
+  for (int j = 0; j < n; ++j) {
+    double s = 0.0;
+    for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
+      double2 x = M[i * n + j];
+      s += x.x * x.x + x.y * x.y;
+    }
+    const double xn2 = block_sum_qr(s, red);
+    if (threadIdx.x == 0) {
+      double2 alpha = M[(long long)j * n + j];
+      double xnorm = sqrt(xn2);
+      double ar = alpha.x, ai = alpha.y;
+      if (xnorm == 0.0 && ai == 0.0) {
+        s_tau = make_double2(0.0, 0.0);
+        s_beta = alpha;
+        s_scal = make_double2(0.0, 0.0);
+      } else {
+        double bnorm = sqrt(ar * ar + ai * ai + xn2);
+        double b = (ar >= 0.0) ? -bnorm : bnorm;
+        s_tau = make_double2((b - ar) / b, -ai / b);
+        s_scal = cdiv_d(make_double2(1.0, 0.0), make_double2(ar - b, ai));
+        s_beta = make_double2(b, 0.0);
+      }
+      tau[j] = s_tau;
+    }
+    __syncthreads();
+    const double2 tj = s_tau;
+    if (tj.x != 0.0 || tj.y != 0.0) {
+      for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) M[i * n + j] = cmul(M[i * n + j], s_scal);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) M[(long long)j * n + j] = s_beta;
+    __syncthreads();
+    if (tj.x != 0.0 || tj.y != 0.0) apply_reflector(M, m, n, j, j, j + 1, tj, true, wacc, wsh);
+  }
+  // R
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int i = e / n, k = e % n;
+    double2 v = (k >= i) ? M[(long long)i * n + k] : make_double2(0.0, 0.0);
+    if (Rt) R[(long long)k * n + i] = v;
+    else R[(long long)i * n + k] = v;
+  }
+  __syncthreads();
+  // Q = H_0 ... H_{n-1} [I; 0]  (zung2r ordering)
+  for (int i = n - 1; i >= 0; --i) {
+    const double2 ti = tau[i];
+    if (i < n - 1) {
+      if (threadIdx.x == 0) M[(long long)i * n + i] = make_double2(1.0, 0.0);
+      __syncthreads();
+      if (ti.x != 0.0 || ti.y != 0.0) apply_reflector(M, m, n, i, i, i + 1, ti, false, wacc, wsh);
+    }
+    for (long long r = i + 1 + threadIdx.x; r < m; r += blockDim.x)
+      M[r * n + i] = cmul(make_double2(-ti.x, -ti.y), M[r * n + i]);
+    if (threadIdx.x == 0) M[(long long)i * n + i] = make_double2(1.0 - ti.x, -ti.y);
+    for (int r = threadIdx.x; r < i; r += blockDim.x) M[(long long)r * n + i] = make_double2(0.0, 0.0);
+    __syncthreads();
+  }
+}
+
+__global__ void k_permute_mode_last(const double2* __restrict__ A, double2* __restrict__ M, long long pre, int dm,
+                                    long long post) {
+  long long total = pre * dm * post;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long x = e / ((long long)dm * post);
+    long long rem = e % ((long long)dm * post);
+    long long i = rem / post, y = rem % post;
+    M[(y * pre + x) * dm + i] = A[e];
+  }
+}
+__global__ void k_unpermute_mode_last(const double2* __restrict__ M, double2* __restrict__ A, long long pre, int dm,
+                                      long long post) {
+  long long total = pre * dm * post;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long x = e / ((long long)dm * post);
+    long long rem = e % ((long long)dm * post);
+    long long i = rem / post, y = rem % post;
+    A[e] = M[(y * pre + x) * dm + i];
+  }
+}
+
+__global__ void k_copy(double2* __restrict__ d, const double2* __restrict__ s, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    d[i] = s[i];
+}
+__global__ void k_axpy(double2* __restrict__ out, const double2* __restrict__ x, double2 sc, long long n, int acc) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 r = cmul(sc, x[i]);
+    if (acc) r = cadd(r, out[i]);
+    out[i] = r;
+  }
+}
+__global__ void k_fill(double2* d, double2 v, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    d[i] = v;
+}
+__global__ void k_scale_identity(double2* d, int r, double2 v) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < r * r; e += gridDim.x * blockDim.x)
+    d[e] = (e / r == e % r) ? v : make_double2(0.0, 0.0);
+}
+__global__ void k_trace(const double2* M, int r, double2* out) {
+  if (threadIdx.x != 0) return;
+  double2 s = make_double2(0.0, 0.0);
+  for (int k = 0; k < r; ++k) s = cadd(s, M[(long long)k * r + k]);
+  *out = s;
+}
+__global__ void k_check_finite(const double2* x, long long n, int* status, int code) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 v = x[i];
+    if (!isfinite(v.x) || !isfinite(v.y)) {
+      atomicOr(status, code);
+      return;
+    }
+  }
+}
+
+unsigned grid_for(long long n, int threads = 256) {
+  long long b = (n + threads - 1) / threads;
+  if (b > 4096) b = 4096;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+}  // namespace
+
+void householder_qr(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, cudaStream_t s) {
+  k_householder_qr<<<1, QT, 0, s>>>(M, m, n, R, Rt, tau_ws);
+}
+void permute_mode_last(const double2* A, double2* M, long long pre, int dm, long long post, cudaStream_t s) {
+  k_permute_mode_last<<<grid_for(pre * dm * post), 256, 0, s>>>(A, M, pre, dm, post);
+}
+void unpermute_mode_last(const double2* M, double2* A, long long pre, int dm, long long post, cudaStream_t s) {
+  k_unpermute_mode_last<<<grid_for(pre * dm * post), 256, 0, s>>>(M, A, pre, dm, post);
+}
+void zcopy(double2* dst, const double2* src, long long n, cudaStream_t s) {
+  if (n > 0) k_copy<<<grid_for(n), 256, 0, s>>>(dst, src, n);
+}
+void zaxpy(double2* out, const double2* x, double2 sc, long long n, bool acc, cudaStream_t st) {
+  if (n > 0) k_axpy<<<grid_for(n), 256, 0, st>>>(out, x, sc, n, acc ? 1 : 0);
+}
+void zfill(double2* dst, double2 v, long long n, cudaStream_t s) {
+  if (n > 0) k_fill<<<grid_for(n), 256, 0, s>>>(dst, v, n);
+}
+void zscale_identity(double2* dst, int r, double2 v, cudaStream_t s) {
+  k_scale_identity<<<grid_for((long long)r * r), 256, 0, s>>>(dst, r, v);
+}
+void ztrace(const double2* M, int r, double2* out, cudaStream_t s) { k_trace<<<1, 32, 0, s>>>(M, r, out); }
+void check_finite(const double2* x, long long n, int* status, int code, cudaStream_t s) {
+  if (n > 0) k_check_finite<<<grid_for(n), 256, 0, s>>>(x, n, status, code);
+}
+
+}  // namespace ttn

@@ -1,0 +1,92 @@
+// Internal declarations shared by the host orchestration (ttn_host.cpp) and the
+// device code (ttn_kernels.cu, ttn_tc.cu).  Not part of the public C-ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace ttn {
+
+// Element addressing of a GEMM operand.
+//   A(i,k) = p[i*s0 + (k/kdiv)*k1 + (k%kdiv)*k2]        (conj if cj)
+//   B(k,j) = p[j*s0 + (k/kdiv)*k1 + (k%kdiv)*k2]        (conj if cj)
+// kfast tells the tile loader that consecutive k are contiguous in memory.
+struct ZOperand {
+  const double2* p;
+  long long s0, k1, k2, kdiv;
+  int cj;
+  int kfast;
+};
+
+// C(i,j) at c[i*ci + j*cj]; batch z adds z*bs to every pointer.
+struct ZGemm {
+  int M, N, K;
+  ZOperand A, B;
+  double2* C;
+  long long ci, cj;
+  long long bsA, bsB, bsC;
+  int batch;
+  double2 alpha, beta;
+};
+
+// Workspace needed by zgemm when it splits K (bytes).
+size_t zgemm_split_workspace_bytes(int M, int N, int K);
+// C = alpha * A*B + beta * C on stream s; `ws` is scratch of the size above (may be
+// null when K is short enough that no split happens).
+void zgemm(const ZGemm& g, double2* ws, size_t ws_bytes, cudaStream_t s);
+
+// ---- Lanczos / Krylov exponential on the device --------------------------------
+// Scalar state of one exponential, resident in device memory.
+struct KrylovCtl {
+  double alpha[72];      // Lanczos diagonal
+  double bet[73];        // Lanczos off-diagonal (bet[j] couples j-1 and j)
+  double coef[2 * 72];   // combination coefficients (complex) for y = sum_q c_q V_q
+  double beta;           // ||y|| at the start of the current sub-step
+  double avnorm;         // ||H V_m||
+  double t_now, t_new, t_out, sgn;
+  double cf_re, cf_im;   // coefficient of the exponent (e.g. -i)
+  double tol;
+  int m;                 // Krylov dimension
+  int mb;                // dimension actually used (breakdown)
+  int k1;                // 2 normally, 0 on breakdown
+  int done;              // 1 when t_now >= t_out
+  int err;               // nonzero: step-size rejection limit hit or non-finite values
+  int substeps;
+  long long napps;       // H applications (including the error-estimate one)
+};
+
+// Reduction partial buffers are laid out [nblocks][nq] complex.
+int vec_blocks(long long n);
+void krylov_begin(KrylovCtl* ctl_dev, const double2* y, double2* V0, long long n, double2* part,
+                  cudaStream_t s);
+// after p = H V_j: alpha, CGS pass, beta, V_{j+1}
+void lanczos_orth(KrylovCtl* ctl, int j, double2* V, long long ldv, double2* p, long long n, double2* part,
+                  cudaStream_t s);
+void lanczos_avnorm(KrylovCtl* ctl, const double2* p, long long n, double2* part, cudaStream_t s);
+void krylov_control(KrylovCtl* ctl, cudaStream_t s);
+void krylov_combine(KrylovCtl* ctl, const double2* V, long long ldv, double2* y, long long n, int nq,
+                    cudaStream_t s);
+constexpr int kQrMaxCols = 64;   // widest matrix the device QR accepts
+constexpr int kKrylovMax = 64;   // largest Krylov dimension
+size_t lanczos_partial_bytes();
+void krylov_init_ctl(KrylovCtl* ctl, int m, double tau, double cre, double cim, double tol, cudaStream_t s);
+
+// ---- Householder QR --------------------------------------------------------------
+// In-place Householder QR of an m x n row-major matrix (m >= n): M <- Q, R (n x n) out.
+// Rt != 0 stores R^T instead of R.
+void householder_qr(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, cudaStream_t s);
+// r2l matricisation: M(y*pre + x, i) = A((x*dm + i)*post + y) and its inverse.
+void permute_mode_last(const double2* A, double2* M, long long pre, int dm, long long post, cudaStream_t s);
+void unpermute_mode_last(const double2* M, double2* A, long long pre, int dm, long long post, cudaStream_t s);
+
+// ---- small helpers ------------------------------------------------------------------
+void zcopy(double2* dst, const double2* src, long long n, cudaStream_t s);
+// out = s*x (+ out when acc)
+void zaxpy(double2* out, const double2* x, double2 s, long long n, bool acc, cudaStream_t st);
+void zfill(double2* dst, double2 v, long long n, cudaStream_t s);
+void zscale_identity(double2* dst, int r, double2 v, cudaStream_t s);
+// out = sum_k diag(M)... trace of an r x r matrix into a device double2
+void ztrace(const double2* M, int r, double2* out, cudaStream_t s);
+// status word: set to code if any element is non-finite
+void check_finite(const double2* x, long long n, int* status, int code, cudaStream_t s);
+
+}  // namespace ttn

@@ -116,6 +116,16 @@ int ttn_integrator_reset(ttn_integrator* it);
 /* wait for all queued device work of this integrator */
 int ttn_integrator_synchronize(ttn_integrator* it);
 
+/* Environments and gauge passes of the first step without its evolution (the
+ * prepare_evolution half of the first call).  Subsequent steps are then full dt
+ * steps; used to time steady-state sweeps without the first-step sub-stepping. */
+int ttn_integrator_prepare(ttn_integrator* it, ttn_state* psi);
+/* algorithmic flops enqueued so far (complex multiply-add = 8 flops) */
+int ttn_integrator_flops(const ttn_integrator* it, double* out);
+/* device timer on the integrator's stream: start=1 records, start=0 records and
+ * returns the elapsed milliseconds since the last start */
+int ttn_integrator_timer(ttn_integrator* it, int start, double* ms);
+
 /* ---- observables ----------------------------------------------------------------- */
 /* <psi| O_mode |psi> with a dense d x d operator on one leaf mode */
 int ttn_expect_leaf(ttn_integrator* it, ttn_state* psi, int mode, const double* op, double* re,
@@ -133,6 +143,27 @@ int ttn_debug_expm_node(ttn_integrator* it, int node, double tau, double cre, do
 /* environment matrix of one node group (which: 0 spf, 1 mean field) */
 int ttn_debug_num_groups(ttn_integrator* it, int node, int* out);
 int ttn_debug_get_env(ttn_integrator* it, int node, int group, int which, double* out);
+/* time `reps` repetitions of one node operation on the device (kind 0: H_eff
+ * application, 1: Krylov exponential of the node over dt/2 (persistent kernel),
+ * 2: leaf-to-root Householder QR, 3: Krylov exponential of the node's bond matrix);
+ * returns milliseconds and algorithmic flops per repetition */
+int ttn_bench_node_op(ttn_integrator* it, ttn_state* psi, int node, int kind, int reps, double* ms_per_rep,
+                      double* flops_per_rep);
+/* With TTN_PROFILE set in the environment, synchronising wall-clock seconds and
+ * call counts per operation kind (8: node exponential, bond exponential, root-to-leaf
+ * QR, leaf-to-root QR, mean-field update, spf update, apply-to-parent,
+ * apply-from-parent) and node-size class (4: <1K, <64K, <1M, >=1M elements);
+ * 32 doubles and 32 counts. */
+int ttn_integrator_profile(ttn_integrator* it, double* seconds, long long* counts);
+/* host<->device bytes moved by this integrator's step and observable calls */
+int ttn_integrator_io_bytes(const ttn_integrator* it, long long* h2d, long long* d2h);
+/* page-locked host memory for callers that keep node tensors on the host between steps */
+int ttn_host_alloc(long long bytes, void** out);
+int ttn_host_free(void* p);
+/* kernel launches issued by this library since it was loaded */
+int ttn_launch_count(unsigned long long* out);
+/* FP64 FMA throughput of a device in TFLOP/s (long independent FMA chains) */
+int ttn_device_fp64_peak(int device, double* tflops);
 /* Householder QR of an m x n row-major matrix on the device: a <- Q, r <- R */
 int ttn_debug_qr(int m, int n, double* a, double* r, int device);
 

@@ -59,6 +59,8 @@ def lib():
         L.orc_group_info.argtypes = [P, C.c_int, C.c_int, ip]
         L.orc_get_env.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
         L.orc_qr.argtypes = [C.c_int, C.c_int, dp, dp]
+        L.orc_node_times.argtypes = [P, dp]
+        L.orc_reset_node_times.argtypes = [P]
         L.orc_tql2.argtypes = [C.c_int, dp, dp, dp]
         _lib = L
     return _lib
@@ -120,6 +122,14 @@ class Oracle:
 
     def prepare(self):
         self._check(lib().orc_prepare(self.h))
+
+    def node_times(self):
+        out = np.zeros(self.topo.nnodes)
+        self._check(lib().orc_node_times(self.h, _dp(out)))
+        return out
+
+    def reset_node_times(self):
+        self._check(lib().orc_reset_node_times(self.h))
 
     @property
     def nh_applications(self) -> int:

@@ -35,10 +35,12 @@
 //     re-orthogonalisation and an implicit-QL eigen-solve of the tridiagonal.
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <stdexcept>
@@ -399,24 +401,57 @@ static void compile_plan(const Tree& T, const SOP& H, Plan& P) {
 // ---------------------------------------------------------------- Householder QR
 // LAPACK zlarfg conventions: H = I - tau v v^H, v(0) = 1, H^H (alpha, x) = (beta, 0),
 // beta real with sign opposite to Re(alpha); tau = 0 when x == 0 and Im(alpha) == 0.
+// Scaled 2-norm of a strided complex column (no intermediate underflow / overflow).
+static double scaled_norm(const cd* x, size_t cnt, size_t stride) {
+  double amax = 0.0;
+  for (size_t i = 0; i < cnt; ++i)
+    amax = std::max(amax, std::max(std::fabs(x[i * stride].real()), std::fabs(x[i * stride].imag())));
+  if (amax == 0.0) return 0.0;
+  double s = 0.0;
+  for (size_t i = 0; i < cnt; ++i) {
+    double a = x[i * stride].real() / amax, b = x[i * stride].imag() / amax;
+    s += a * a + b * b;
+  }
+  return amax * std::sqrt(s);
+}
+// sqrt(x^2 + y^2 + z^2) without destructive underflow or overflow (LAPACK dlapy3 scheme)
+static double lapy3(double x, double y, double z) {
+  double w = std::max(std::fabs(x), std::max(std::fabs(y), std::fabs(z)));
+  if (w == 0.0) return 0.0;
+  double a = x / w, b = y / w, c = z / w;
+  return w * std::sqrt(a * a + b * b + c * c);
+}
+
 static void householder_qr(cd* M, size_t m, int n, cd* R, std::vector<cd>& tau) {
+  const double safmin = 2.2250738585072014e-308 / 1.1102230246251565e-16;
   tau.assign(n, 0.0);
   for (int j = 0; j < n; ++j) {
     cd alpha = M[(size_t)j * n + j];
-    double xn2 = 0.0;
-    for (size_t i = j + 1; i < m; ++i) xn2 += std::norm(M[i * n + j]);
-    double xnorm = std::sqrt(xn2);
+    cd* x = M + (size_t)(j + 1) * n + j;
+    const size_t cnt = m - j - 1;
+    double xnorm = scaled_norm(x, cnt, n);
     double ar = alpha.real(), ai = alpha.imag();
     cd beta;
     if (xnorm == 0.0 && ai == 0.0) {
       tau[j] = 0.0; beta = alpha;
-      for (size_t i = j + 1; i < m; ++i) M[i * n + j] = 0.0;
     } else {
-      double bnorm = std::sqrt(ar * ar + ai * ai + xn2);
-      double b = (ar >= 0.0) ? -bnorm : bnorm;
+      double b = -std::copysign(lapy3(ar, ai, xnorm), ar >= 0.0 ? 1.0 : -1.0);
+      int knt = 0;
+      if (std::fabs(b) < safmin) {
+        // rescale tiny columns (zlarfg), at most 20 times
+        const double rs = 1.0 / safmin;
+        do {
+          ++knt;
+          for (size_t i = 0; i < cnt; ++i) x[i * n] *= rs;
+          b *= rs; ar *= rs; ai *= rs;
+        } while (std::fabs(b) < safmin && knt < 20);
+        xnorm = scaled_norm(x, cnt, n);
+        b = -std::copysign(lapy3(ar, ai, xnorm), ar >= 0.0 ? 1.0 : -1.0);
+      }
       tau[j] = cd((b - ar) / b, -ai / b);
-      cd scal = 1.0 / (alpha - cd(b, 0.0));
-      for (size_t i = j + 1; i < m; ++i) M[i * n + j] = cmul(M[i * n + j], scal);
+      cd scal = 1.0 / (cd(ar, ai) - cd(b, 0.0));
+      for (size_t i = 0; i < cnt; ++i) x[i * n] = cmul(x[i * n], scal);
+      for (int q = 0; q < knt; ++q) b *= safmin;
       beta = cd(b, 0.0);
     }
     M[(size_t)j * n + j] = beta;
@@ -470,7 +505,13 @@ static void tql2(int n, double* d, const double* e_in, double* z) {
         if (std::fabs(e[m]) <= 1e-300 + 2.220446049250313e-16 * dd) break;
       }
       if (m == l) break;
-      if (++iter > 60) throw Error(ENUM, "tridiagonal eigensolver did not converge");
+      if (++iter > 60) {
+        std::string msg = "tridiagonal eigensolver did not converge: n=" + std::to_string(n) + " l=" + std::to_string(l) + " d=";
+        for (int q = 0; q < n; ++q) msg += std::to_string(d[q]) + ",";
+        msg += " e=";
+        for (int q = 0; q < n; ++q) { char b[64]; std::snprintf(b, 64, "%.3e,", e[q]); msg += b; }
+        throw Error(ENUM, msg);
+      }
       double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
       double r = std::hypot(g, 1.0);
       g = d[m] - d[l] + e[l] / (g + (g >= 0.0 ? std::fabs(r) : -std::fabs(r)));
@@ -533,6 +574,15 @@ struct Engine {
   long long nsteps = 0, nh = 0;
   std::vector<cd> w1, w2, w3, w4;                       // work buffers (max node size)
   std::vector<std::vector<cd>> V;                       // Krylov basis
+  std::vector<double> node_time;                        // seconds spent per node in sweeps
+  std::chrono::steady_clock::time_point tmark;
+  void tick() { tmark = std::chrono::steady_clock::now(); }
+  void tock(int id) {
+    auto now = std::chrono::steady_clock::now();
+    if ((int)node_time.size() < T.n) node_time.assign(T.n, 0.0);
+    node_time[id] += std::chrono::duration<double>(now - tmark).count();
+    tmark = now;
+  }
 
   void init(const int* par, int nn, const int* hr, const int* lm, const int* ld) {
     T.build(nn, par, hr, lm, ld);
@@ -852,34 +902,54 @@ struct Engine {
     std::copy(tmp.begin(), tmp.end(), R.begin());
   }
 
+  // ---- optional finiteness checks after every operation (ORC_CHECK=1)
+  bool checking = std::getenv("ORC_CHECK") != nullptr;
+  void chk(const char* what, int id) {
+    if (!checking) return;
+    auto bad = [](const std::vector<cd>& v) {
+      for (auto& z : v) if (!std::isfinite(z.real()) || !std::isfinite(z.imag())) return true;
+      return false;
+    };
+    for (int i = 0; i < T.n; ++i) {
+      if (bad(A[i])) throw Error(ENUM, std::string("non-finite tensor at node ") + std::to_string(i) + " after " + what + " on node " + std::to_string(id));
+      if (bad(rmat[i])) throw Error(ENUM, std::string("non-finite R at node ") + std::to_string(i) + " after " + what + " on node " + std::to_string(id));
+      for (auto& e : spf[i]) if (bad(e)) throw Error(ENUM, std::string("non-finite spf at node ") + std::to_string(i) + " after " + what + " on node " + std::to_string(id));
+      for (auto& e : mf[i]) if (bad(e)) throw Error(ENUM, std::string("non-finite mf at node ") + std::to_string(i) + " after " + what + " on node " + std::to_string(id));
+    }
+  }
+
   // ---- half sweeps (tdvp_algorithm_engine.hpp:331-501)
   void forward(bool evolve) {
     std::vector<int> tv(T.n, 0);
+    tick();
     for (int id : T.traversal) {
       int t = tv[id]++;
+      struct Tk { Engine* e; int id; ~Tk() { e->tock(id); } } tk{this, id};
       if (t != T.nmodes[id]) {
         int mode = t;
-        if (t == 0 && id != 0) apply_from_parent(id);
+        if (t == 0 && id != 0) { apply_from_parent(id); chk("apply_from_parent", id); }
         if (!T.leaf(id)) {
-          r2l(id, mode);
-          update_mf(T.children[id][mode]);
+          r2l(id, mode); chk("r2l", id);
+          update_mf(T.children[id][mode]); chk("update_mf", id);
         }
       } else {
-        if (evolve) evolve_node(id);
+        if (evolve) { evolve_node(id); chk("evolve_node", id); }
         if (id != 0) {
-          l2r(id);
-          update_spf(id);
-          if (evolve) evolve_bond(id, rmat[id]);
-          apply_to_parent(id);
+          l2r(id); chk("l2r", id);
+          update_spf(id); chk("update_spf", id);
+          if (evolve) { evolve_bond(id, rmat[id]); chk("evolve_bond", id); }
+          apply_to_parent(id); chk("apply_to_parent", id);
         }
       }
     }
   }
   void backward(bool evolve) {
     std::vector<int> tv(T.n, 0);
+    tick();
     for (auto it = T.traversal.rbegin(); it != T.traversal.rend(); ++it) {
       int id = *it;
       int t = tv[id]++;
+      struct Tk { Engine* e; int id; ~Tk() { e->tock(id); } } tk{this, id};
       if (t != T.nmodes[id]) {
         int mode = T.nmodes[id] - (t + 1);
         if (t == 0) {
@@ -1137,6 +1207,17 @@ int orc_step(void* p, double dt, double cre, double cim) {
 int orc_sweep(void* p, double dt, double cre, double cim) {
   OrcHandle* h = (OrcHandle*)p;
   ORC_TRY(h, { h->E.coeff = cd(cre, cim); h->E.dt = dt; h->E.sweep(); })
+}
+// Per-node seconds accumulated over all sweeps so far (out: nnodes doubles).
+int orc_node_times(void* p, double* out) {
+  OrcHandle* h = (OrcHandle*)p;
+  ORC_TRY(h, {
+    for (int i = 0; i < h->E.T.n; ++i) out[i] = i < (int)h->E.node_time.size() ? h->E.node_time[i] : 0.0;
+  })
+}
+int orc_reset_node_times(void* p) {
+  OrcHandle* h = (OrcHandle*)p;
+  ORC_TRY(h, { h->E.node_time.assign(h->E.T.n, 0.0); })
 }
 int orc_prepare(void* p) {
   OrcHandle* h = (OrcHandle*)p;

@@ -54,6 +54,16 @@ def test_device_qr_rank_deficient_exact_zeros():
     assert np.allclose(qd, qo, rtol=1e-15, atol=1e-15) and np.allclose(rd, ro, rtol=1e-15, atol=1e-15)
 
 
+def test_device_qr_tiny_columns_match_oracle():
+    rng = np.random.default_rng(6)
+    a = (rng.normal(size=(300, 16)) + 1j * rng.normal(size=(300, 16))) * 1e-170
+    a[:, 0] *= 1e-140
+    qd, rd = api.device_qr(a)
+    qo, ro = oracle_qr(a)
+    assert np.isfinite(qd).all() and np.isfinite(rd).all()
+    assert rel(qd, qo) < 1e-12 and rel(rd, ro) < 1e-12
+
+
 def spin_boson_small():
     m, cfg = sb.build_config("c1")
     return m, cfg

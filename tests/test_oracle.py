@@ -77,3 +77,13 @@ def test_householder_conventions():
     q, r = qr(z)
     assert np.array_equal(q, np.eye(6, 3))
     assert r[0, 0] == 1.0
+
+
+def test_householder_tiny_columns_stay_finite():
+    rng = np.random.default_rng(5)
+    a = (rng.normal(size=(50, 6)) + 1j * rng.normal(size=(50, 6))) * 1e-170
+    a[:, 0] *= 1e-140  # below the LAPACK safe minimum: exercises the rescaling loop
+    q, r = qr(a)
+    assert np.isfinite(q).all() and np.isfinite(r).all()
+    assert np.allclose(q.conj().T @ q, np.eye(6), atol=1e-13)
+    assert np.allclose(q @ r, a, rtol=0, atol=1e-13 * np.abs(a).max())

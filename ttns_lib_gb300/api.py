@@ -79,6 +79,16 @@ SIGNATURES = {
     "ttn_integrator_nh_applications": (_I, [_P, _LLP]),
     "ttn_integrator_reset": (_I, [_P]),
     "ttn_integrator_synchronize": (_I, [_P]),
+    "ttn_integrator_prepare": (_I, [_P, _P]),
+    "ttn_integrator_flops": (_I, [_P, _DP]),
+    "ttn_integrator_timer": (_I, [_P, _I, _DP]),
+    "ttn_bench_node_op": (_I, [_P, _P, _I, _I, _I, _DP, _DP]),
+    "ttn_device_fp64_peak": (_I, [_I, _DP]),
+    "ttn_launch_count": (_I, [C.POINTER(C.c_ulonglong)]),
+    "ttn_integrator_io_bytes": (_I, [_P, _LLP, _LLP]),
+    "ttn_integrator_profile": (_I, [_P, _DP, _LLP]),
+    "ttn_host_alloc": (_I, [_LL, _PP]),
+    "ttn_host_free": (_I, [_P]),
     "ttn_expect_leaf": (_I, [_P, _P, _I, _DP, _DP, _DP]),
     "ttn_norm2": (_I, [_P, _P, _DP]),
     "ttn_debug_refresh_env": (_I, [_P, _P]),
@@ -189,6 +199,12 @@ class httensor:
         return [flat[self.offsets[i]:self.offsets[i + 1]].reshape(self.topo.node_shape(i)).copy()
                 for i in range(self.topo.nnodes)]
 
+    def upload_from(self, buf: "PinnedBuffer"):
+        _check(lib().ttn_state_upload(self.h, C.cast(buf.ptr, _DP)))
+
+    def download_to(self, buf: "PinnedBuffer"):
+        _check(lib().ttn_state_download(self.h, C.cast(buf.ptr, _DP)))
+
     def init_product(self, psi0: Optional[np.ndarray] = None, seed: int = 0):
         """Spin-boson start state with std::mt19937(seed) unoccupied SPFs (src/spin_boson.cpp:584-649)."""
         if psi0 is None:
@@ -196,6 +212,23 @@ class httensor:
         else:
             p = _cplx(psi0)
             _check(lib().ttn_state_init_product(self.h, _dp(p.view(np.float64)), seed))
+
+
+class PinnedBuffer:
+    """Page-locked host buffer holding a whole state (numpy view in ``.array``)."""
+
+    def __init__(self, n_complex: int):
+        p = C.c_void_p()
+        _check(lib().ttn_host_alloc(int(n_complex) * 16, C.byref(p)))
+        self.ptr = p
+        self.nbytes = int(n_complex) * 16
+        arr_t = C.c_double * (2 * int(n_complex))
+        self.array = np.frombuffer(arr_t.from_address(p.value), dtype=np.complex128)
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib().ttn_host_free(self.ptr)
+            self.ptr = None
 
 
 class matrix_element:
@@ -263,6 +296,47 @@ class fixed_step_projector_splitting_integrator:
         _check(lib().ttn_integrator_nh_applications(self.h, C.byref(out)))
         return out.value
 
+    def prepare(self, A: httensor):
+        _check(lib().ttn_integrator_prepare(self.h, A.h))
+
+    def flops(self) -> float:
+        out = C.c_double()
+        _check(lib().ttn_integrator_flops(self.h, C.byref(out)))
+        return out.value
+
+    def timer_start(self):
+        _check(lib().ttn_integrator_timer(self.h, 1, None))
+
+    def timer_stop(self) -> float:
+        out = C.c_double()
+        _check(lib().ttn_integrator_timer(self.h, 0, C.byref(out)))
+        return out.value
+
+    PROFILE_KINDS = ["expm_node", "expm_bond", "r2l_qr", "l2r_qr", "mf_update", "spf_update", "apply_to_parent",
+                     "apply_from_parent"]
+    PROFILE_CLASSES = ["<1K", "<64K", "<1M", ">=1M"]
+
+    def profile(self):
+        t = np.zeros(32)
+        n = np.zeros(32, dtype=np.int64)
+        _check(lib().ttn_integrator_profile(self.h, _dp(t), n.ctypes.data_as(_LLP)))
+        out = {}
+        for k, kn in enumerate(self.PROFILE_KINDS):
+            for c, cn in enumerate(self.PROFILE_CLASSES):
+                if n[k * 4 + c]:
+                    out[f"{kn}[{cn}]"] = (float(t[k * 4 + c]), int(n[k * 4 + c]))
+        return out
+
+    def io_bytes(self):
+        a, b = C.c_longlong(), C.c_longlong()
+        _check(lib().ttn_integrator_io_bytes(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def bench_node_op(self, A: httensor, node: int, kind: int, reps: int):
+        ms, fl = C.c_double(), C.c_double()
+        _check(lib().ttn_bench_node_op(self.h, A.h, node, kind, reps, C.byref(ms), C.byref(fl)))
+        return ms.value, fl.value
+
     def mel(self) -> matrix_element:
         return self._mel
 
@@ -296,6 +370,18 @@ class fixed_step_projector_splitting_integrator:
         out = np.zeros((r, r), dtype=np.complex128)
         _check(lib().ttn_debug_get_env(self.h, node, group, 0 if which == "spf" else 1, _dp(out.view(np.float64))))
         return out
+
+
+def launch_count() -> int:
+    out = C.c_ulonglong()
+    _check(lib().ttn_launch_count(C.byref(out)))
+    return out.value
+
+
+def fp64_peak_tflops(device: int = 0) -> float:
+    out = C.c_double()
+    _check(lib().ttn_device_fp64_peak(device, C.byref(out)))
+    return out.value
 
 
 def device_qr(a: np.ndarray, device: int = 0):

@@ -1,0 +1,49 @@
+// Persistent cooperative Krylov exponential (see ttn_expm.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ttn_kernels.cuh"
+
+namespace ttn {
+
+struct GridBarrier;
+
+enum { MV_MODE = 0, MV_MF = 1, MV_AXPY = 2, MV_ZERO = 3 };
+
+// One contraction of a matrix-vector program.  Buffers: 0 = input vector, 1 = output,
+// 2..4 = temporaries.  MODE: out(a,i,b) = alpha sum_j mat(i,j) in(a,j,b) (+ out) with
+// shape (na, d, nb); MF: out(x,k) = alpha sum_l in(x,l) mat(k,l) (+ out) with nx = na,
+// r = d; AXPY: out = alpha in (+ out) over na elements; ZERO: out = 0 over na elements.
+struct MvOp {
+  int kind;
+  int in, out;
+  int barrier_before;
+  const double2* mat;
+  long long na, nb;
+  int d;
+  int beta;  // 1: accumulate into out
+  double2 alpha;
+};
+
+struct ExpmArgs {
+  double2* y;            // vector evolved in place
+  long long n;
+  double2* V;            // Krylov basis, m+1 vectors, stride ldv
+  long long ldv;
+  double2 *p, *t1, *t2, *t3;
+  const MvOp* prog;      // device program
+  int nops;
+  double2* part;         // reduction partials (expm_partial_bytes)
+  KrylovCtl* ctl;
+  GridBarrier* bar;
+  int* err;              // status word (Krylov error bits, barrier timeout)
+  long long* napps_total;  // device counter of H applications (may be null)
+  int m;
+  double tau, cf_re, cf_im, tol;
+};
+
+int expm_coop_max_grid();
+size_t expm_partial_bytes(int max_grid);
+cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s);
+
+}  // namespace ttn

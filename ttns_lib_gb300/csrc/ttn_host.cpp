@@ -12,9 +12,13 @@
 // device-to-host traffic inside a step is one status word per Krylov sub-step.
 #include "../../include/ttn_gb300.h"
 #include "ttn_kernels.cuh"
+#include "ttn_coop.cuh"
+#include "ttn_expm.cuh"
 #include "ttn_tc.cuh"
 
 #include <algorithm>
+#include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -395,15 +399,50 @@ struct Integrator {
   long long maxsize = 0, ldv = 0;
   KrylovCtl* ctl = nullptr;
   int* status = nullptr;
+  // cooperative kernels: barrier state, scratch, grid limits
+  DevBuf coop_buf;
+  GridBarrier* bar = nullptr;
+  double* qr_scratch = nullptr;
+  int num_sms = 0, qr_max_grid = 1, expm_max_grid = 1;
+  // compiled matrix-vector programs for the persistent Krylov kernel
+  DevBuf prog_buf, expm_part_buf;
+  std::vector<int> heff_off, heff_n, kbond_off, kbond_n;
+  long long* nh_dev = nullptr;
   // host mirrors
   struct HostCtl { int done, err; long long napps; };
   HostCtl* hctl = nullptr;  // pinned
   double dt = 0.0, t_engine = 0.0;
   cd coeff = cd(0.0, -1.0);
   long long nsteps = 0, nh = 0;
+  double flops = 0.0;        // algorithmic flops enqueued (complex MAC = 8 flops)
+  long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device traffic issued by the step path
+  // optional breakdown (TTN_PROFILE=1): synchronising wall time per operation kind and
+  // node-size class; slows the sweep down, for analysis only
+  bool profiling = std::getenv("TTN_PROFILE") != nullptr;
+  double prof_t[8][4] = {};
+  long long prof_n[8][4] = {};
+  struct Prof {
+    Integrator* I; int kind, cls; std::chrono::steady_clock::time_point t0;
+    Prof(Integrator* i, int k, int nd) : I(i), kind(k), cls(0) {
+      if (!I->profiling) return;
+      long long sz = I->T.size(nd);
+      cls = sz < 1024 ? 0 : sz < 65536 ? 1 : sz < (1 << 20) ? 2 : 3;
+      cudaStreamSynchronize(I->stream);
+      t0 = std::chrono::steady_clock::now();
+    }
+    ~Prof() {
+      if (!I->profiling) return;
+      cudaStreamSynchronize(I->stream);
+      I->prof_t[kind][cls] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      I->prof_n[kind][cls] += 1;
+    }
+  };
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   TcEngine* tc = nullptr;  // tensor-core contraction engine (mixed precision)
 
   ~Integrator() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
     if (tc) tc_destroy(tc);
     if (hctl) cudaFreeHost(hctl);
     if (stream) cudaStreamDestroy(stream);
@@ -526,6 +565,22 @@ struct Integrator {
     status = (int*)(ctl_buf.as<char>() + align256(sizeof(KrylovCtl)));
     CK(cudaMemsetAsync(ctl_buf.p, 0, ctl_buf.bytes, stream));
     CK(cudaMallocHost((void**)&hctl, sizeof(HostCtl)));
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
+    {
+      CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
+      qr_max_grid = std::max(1, std::min(coop_qr_max_grid(), num_sms));
+      size_t qb = align256(sizeof(GridBarrier)) + align256(coop_qr_scratch_bytes(qr_max_grid));
+      coop_buf.alloc(qb);
+      CK(cudaMemset(coop_buf.p, 0, coop_buf.bytes));
+      bar = coop_buf.as<GridBarrier>();
+      qr_scratch = (double*)(coop_buf.as<char>() + align256(sizeof(GridBarrier)));
+      expm_max_grid = std::max(1, expm_coop_max_grid());
+      expm_part_buf.alloc(expm_partial_bytes(expm_max_grid) + 256);
+      nh_dev = (long long*)(expm_part_buf.as<char>() + expm_partial_bytes(expm_max_grid));
+      CK(cudaMemset(expm_part_buf.p, 0, expm_part_buf.bytes));
+      compile_programs();
+    }
     if (cfg.precision == TTN_PREC_MIXED) {
       try {
         tc = tc_create(device, maxsize, stream);
@@ -549,6 +604,7 @@ struct Integrator {
   // out(a,i,b) = alpha sum_j S(i,j) in(a,j,b) (+ out)
   void mode_apply(const double2* S, int d, const double2* in, double2* out, long long na, long long nb, cd alpha,
                   bool acc) {
+    flops += 8.0 * na * (double)d * d * nb;
     if (tc && tc_mode_apply(tc, S, d, in, out, na, nb, d2(alpha), acc, stream)) return;
     ZGemm g{};
     g.M = d; g.N = (int)nb; g.K = d;
@@ -563,6 +619,7 @@ struct Integrator {
   }
   // out(x,k) = alpha sum_l in(x,l) M(k,l) (+ out)
   void mf_apply(const double2* in, const double2* M, int r, long long nx, double2* out, cd alpha, bool acc) {
+    flops += 8.0 * nx * (double)r * r;
     if (tc && tc_mf_apply(tc, in, M, r, nx, out, d2(alpha), acc, stream)) return;
     ZGemm g{};
     g.M = (int)nx; g.N = r; g.K = r;
@@ -576,6 +633,7 @@ struct Integrator {
   }
   // out(i,j) = alpha sum_x conj(A(x,i)) X(x,j) (+ out)
   void adj_mul(const double2* A, const double2* X, long long nx, int r, double2* out, cd alpha, bool acc) {
+    flops += 8.0 * nx * (double)r * r;
     if (tc && tc_adj_mul(tc, A, X, nx, r, out, d2(alpha), acc, stream)) return;
     ZGemm g{};
     g.M = r; g.N = r; g.K = (int)nx;
@@ -591,6 +649,7 @@ struct Integrator {
   // out(i,j) = alpha sum_{a,b} conj(A(a,i,b)) T(a,j,b) (+ out)
   void mode_contract(const double2* A, const double2* Tt, long long na, int d, long long nb, double2* out, cd alpha,
                      bool acc) {
+    flops += 8.0 * na * nb * (double)d * d;
     if (tc && tc_mode_contract(tc, A, Tt, na, d, nb, out, d2(alpha), acc, stream)) return;
     ZGemm g{};
     g.M = d; g.N = d; g.K = (int)(na * nb);
@@ -606,6 +665,7 @@ struct Integrator {
   }
   // C (m x r) = A (m x r) * R (r x r)
   void right_mul(const double2* A, const double2* R, long long m, int r, double2* C) {
+    flops += 8.0 * m * (double)r * r;
     ZGemm g{};
     g.M = (int)m; g.N = r; g.K = r;
     g.A = op_rowmajor(A, r);
@@ -655,6 +715,7 @@ struct Integrator {
 
   // bottom-up environment (single_particle_operator.hpp:26-103)
   void update_spf(int nd, const double2* A) {
+    Prof pf(this, 5, nd);
     const long long sz = T.size(nd);
     const int r = T.hrank[nd];
     for (auto& g : G[nd]) {
@@ -670,6 +731,7 @@ struct Integrator {
   // top-down environment of child nd (mean_field_operator.hpp:37-184)
   void update_mf(int nd, const double2* Ap) {
     if (nd == 0) return;
+    Prof pf(this, 4, T.parent[nd]);
     const int p = T.parent[nd], mu = T.slot[nd];
     long long na, nb;
     int d;
@@ -768,6 +830,34 @@ struct Integrator {
   void mode_identity_axpy(const double2* x, double2* out, long long sz, cd s, bool acc) {
     zaxpy(out, x, d2(s), sz, acc, stream);
   }
+  // algorithmic flops of one H_eff application at nd
+  double heff_flops(int nd) {
+    double before = flops;
+    // count by dry-running the contraction shapes (no launches)
+    double f = 0.0;
+    const double sz = (double)T.size(nd);
+    const int r = T.hrank[nd];
+    for (auto& g : G[nd]) {
+      if (!g.id_spf)
+        for (const SpfTuple& t : g.spf)
+          for (const Item& it : t.items) {
+            int d = (it.slot < 0) ? T.dims[nd][0] : T.dims[nd][it.slot];
+            f += 8.0 * sz * d;
+          }
+      if (!g.id_mf) f += 8.0 * sz * r;
+    }
+    (void)before;
+    return f;
+  }
+  double kbond_flops(int nd) {
+    const double r = T.hrank[nd];
+    double f = 0.0;
+    for (auto& g : G[nd]) {
+      if (!g.id_spf) f += 8.0 * r * r * r;
+      if (!g.id_mf) f += 8.0 * r * r * r;
+    }
+    return f;
+  }
   // out = K_bond(nd) R (full_hamiltonian_action)
   void kbond(int nd, const double2* R, double2* out) {
     const int r = T.hrank[nd];
@@ -775,6 +865,7 @@ struct Integrator {
     for (auto& g : G[nd]) {
       const double2* X = R;
       if (!g.id_spf) {
+        flops += 8.0 * (double)r * r * r;
         ZGemm gg{};
         gg.M = r; gg.N = r; gg.K = r;
         gg.A = op_rowmajor(g.spf_dev, r);
@@ -793,6 +884,144 @@ struct Integrator {
     if (first) zfill(out, make_double2(0.0, 0.0), (long long)r * r, stream);
   }
 
+  // ---------------------------------------------------------------- matvec programs
+  struct ProgBuilder {
+    std::vector<MvOp> ops;
+    unsigned dirty = 0, read = 0;
+    void emit(MvOp op) {
+      const unsigned in_bit = (op.kind == MV_ZERO) ? 0u : (1u << op.in);
+      const unsigned out_bit = 1u << op.out;
+      op.barrier_before = ((in_bit & dirty) || (out_bit & read)) ? 1 : 0;
+      if (op.barrier_before) { dirty = 0; read = 0; }
+      dirty |= out_bit;
+      read |= in_bit;
+      ops.push_back(op);
+    }
+  };
+  static MvOp mk(int kind, int in, int out, const double2* mat, long long na, int d, long long nb, cd alpha, bool acc) {
+    MvOp o{};
+    o.kind = kind; o.in = in; o.out = out; o.mat = mat; o.na = na; o.d = d; o.nb = nb;
+    o.alpha = d2(alpha); o.beta = acc ? 1 : 0;
+    return o;
+  }
+  void item_shape(int nd, const Item& it, const double2*& S, long long& na, int& d, long long& nb) {
+    if (it.slot < 0) { S = leaf_ops[T.leaf_mode[nd]][it.grp]; na = 1; d = T.dims[nd][0]; nb = T.hrank[nd]; }
+    else { S = G[T.children[nd][it.slot]][it.grp].spf_dev; r3(nd, it.slot, na, d, nb); }
+  }
+  // chain of mode products ending in a temporary; returns its buffer id
+  int emit_chain(ProgBuilder& B, int nd, const std::vector<Item>& items, int in, cd alpha_last) {
+    int cur = in;
+    for (size_t q = 0; q < items.size(); ++q) {
+      const double2* S; long long na, nb; int d;
+      item_shape(nd, items[q], S, na, d, nb);
+      int out = (q % 2 == 0) ? 2 : 3;
+      B.emit(mk(MV_MODE, cur, out, S, na, d, nb, q + 1 == items.size() ? alpha_last : cd(1.0), false));
+      cur = out;
+    }
+    return cur;
+  }
+  std::vector<MvOp> heff_program(int nd) {
+    ProgBuilder B;
+    const long long sz = T.size(nd);
+    const int r = T.hrank[nd];
+    bool first = true;
+    for (auto& g : G[nd]) {
+      const bool direct = g.id_mf;
+      if (g.id_spf) {
+        if (direct) B.emit(mk(MV_AXPY, 0, 1, nullptr, sz, 0, 0, g.s, !first));
+        else B.emit(mk(MV_MF, 0, 1, g.mf_dev, sz / r, r, 0, g.s, !first));
+      } else if (g.spf.size() == 1) {
+        const auto& t = g.spf[0];
+        if (direct && t.items.size() == 1) {
+          const double2* S; long long na, nb; int d;
+          item_shape(nd, t.items[0], S, na, d, nb);
+          B.emit(mk(MV_MODE, 0, 1, S, na, d, nb, g.s * t.a, !first));
+        } else {
+          int X = emit_chain(B, nd, t.items, 0, t.a);
+          if (direct) B.emit(mk(MV_AXPY, X, 1, nullptr, sz, 0, 0, g.s, !first));
+          else B.emit(mk(MV_MF, X, 1, g.mf_dev, sz / r, r, 0, g.s, !first));
+        }
+      } else {
+        bool f2 = true;
+        const int acc_buf = direct ? 1 : 4;
+        for (const SpfTuple& t : g.spf) {
+          const bool accum = direct ? !(first && f2) : !f2;
+          const cd sc = direct ? g.s * t.a : t.a;
+          if (t.items.size() == 1) {
+            const double2* S; long long na, nb; int d;
+            item_shape(nd, t.items[0], S, na, d, nb);
+            B.emit(mk(MV_MODE, 0, acc_buf, S, na, d, nb, sc, accum));
+          } else {
+            int X = emit_chain(B, nd, t.items, 0, t.a);
+            B.emit(mk(MV_AXPY, X, acc_buf, nullptr, sz, 0, 0, direct ? g.s : cd(1.0), accum));
+          }
+          f2 = false;
+        }
+        if (!direct) B.emit(mk(MV_MF, 4, 1, g.mf_dev, sz / r, r, 0, g.s, !first));
+      }
+      first = false;
+    }
+    if (first) B.emit(mk(MV_ZERO, 0, 1, nullptr, sz, 0, 0, 0.0, false));
+    return B.ops;
+  }
+  std::vector<MvOp> kbond_program(int nd) {
+    ProgBuilder B;
+    const int r = T.hrank[nd];
+    bool first = true;
+    for (auto& g : G[nd]) {
+      int X = 0;
+      if (!g.id_spf) {
+        B.emit(mk(MV_MODE, 0, 2, g.spf_dev, 1, r, r, 1.0, false));
+        X = 2;
+      }
+      if (g.id_mf) B.emit(mk(MV_AXPY, X, 1, nullptr, (long long)r * r, 0, 0, g.s, !first));
+      else B.emit(mk(MV_MF, X, 1, g.mf_dev, r, r, 0, g.s, !first));
+      first = false;
+    }
+    if (first) B.emit(mk(MV_ZERO, 0, 1, nullptr, (long long)r * r, 0, 0, 0.0, false));
+    return B.ops;
+  }
+  void compile_programs() {
+    std::vector<MvOp> all;
+    heff_off.assign(T.n, 0); heff_n.assign(T.n, 0); kbond_off.assign(T.n, 0); kbond_n.assign(T.n, 0);
+    for (int i = 0; i < T.n; ++i) {
+      auto h = heff_program(i);
+      heff_off[i] = (int)all.size(); heff_n[i] = (int)h.size();
+      all.insert(all.end(), h.begin(), h.end());
+      auto k = kbond_program(i);
+      kbond_off[i] = (int)all.size(); kbond_n[i] = (int)k.size();
+      all.insert(all.end(), k.begin(), k.end());
+    }
+    prog_buf.alloc(all.size() * sizeof(MvOp) + 16);
+    CK(cudaMemcpy(prog_buf.p, all.data(), all.size() * sizeof(MvOp), cudaMemcpyHostToDevice));
+  }
+  int expm_grid(long long n) const {
+    long long g = (n + 63) / 64;
+    if (g < 1) g = 1;
+    if (g > expm_max_grid) g = expm_max_grid;
+    return (int)g;
+  }
+  // persistent Krylov exponential of one node tensor (kind 0) or bond matrix (kind 1)
+  void expm_dev(int nd, int kind, double2* y, long long n, double tau, cd cf, bool count) {
+    if (tau == 0.0) return;
+    ExpmArgs a{};
+    a.y = y; a.n = n; a.V = V; a.ldv = ldv; a.p = p; a.t1 = w1; a.t2 = w2; a.t3 = w3;
+    a.prog = prog_buf.as<MvOp>() + (kind == 0 ? heff_off[nd] : kbond_off[nd]);
+    a.nops = kind == 0 ? heff_n[nd] : kbond_n[nd];
+    a.part = expm_part_buf.as<double2>();
+    a.ctl = ctl; a.bar = bar; a.err = status;
+    a.napps_total = count ? nh_dev : nullptr;
+    a.m = cfg.krylov_dim; a.tau = tau; a.cf_re = cf.real(); a.cf_im = cf.imag(); a.tol = cfg.krylov_tol;
+    CK(expm_coop(a, expm_grid(n), stream));
+    // algorithmic flops of the Lanczos vector passes (one sub-step assumed; the
+    // matvec flops are counted by heff_flops at report time)
+    const int m = cfg.krylov_dim;
+    double vec = 0.0;
+    for (int j = 0; j < m; ++j) vec += (8.0 + 8.0 + 16.0 * (j + 1) + 4.0 + 2.0) * n;
+    vec += (4.0 + 8.0 * (m + 1)) * n;
+    flops += vec;
+  }
+
   // ---------------------------------------------------------------- Krylov exponential
   template <typename Op>
   void expm(Op&& hop, double2* y, long long n, double tau, cd cf, bool count) {
@@ -808,10 +1037,14 @@ struct Integrator {
       }
       hop(V + (long long)m * ldv, p);
       lanczos_avnorm(ctl, p, n, part, stream);
+      // vector passes: per iteration j: <V_j,p>, two real axpys, (j+1) dots and axpys, a norm
+      for (int j = 0; j < m; ++j) flops += (8.0 + 8.0 + 16.0 * (j + 1) + 4.0 + 2.0) * n;
+      flops += (4.0 + 8.0 * (m + 1)) * n;
       krylov_control(ctl, stream);
       krylov_combine(ctl, V, ldv, y, n, m + 1, stream);
       CK(cudaMemcpyAsync(&hctl->done, &ctl->done, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream));
       CK(cudaMemcpyAsync(&hctl->napps, &ctl->napps, sizeof(long long), cudaMemcpyDeviceToHost, stream));
+      d2h_bytes += sizeof(int) * 2 + sizeof(long long);
       CK(cudaStreamSynchronize(stream));
       TTN_REQUIRE(hctl->err == 0, TTN_ENUMERIC, "Krylov exponential failed (tolerance unreachable or non-finite values)");
       if (hctl->done) break;
@@ -820,12 +1053,21 @@ struct Integrator {
   }
 
   // ---------------------------------------------------------------- gauge moves
+  // Householder QR on as many CTAs as the height allows (one row block per CTA)
+  void qr(double2* M, long long m, int n, double2* R, int Rt) {
+    int g = std::min(coop_qr_grid(m, num_sms), qr_max_grid);
+    CK(householder_qr_coop(M, m, n, R, Rt, qtau, qr_scratch, bar, status, g, stream));
+  }
+  static double qr_flops(double m, double n) { return 2.0 * 8.0 * (m * n * n - n * n * n / 3.0); }
   void l2r(int nd, double2* A) {
+    Prof pf(this, 3, nd);
     const long long m = T.dimen[nd];
     const int r = T.hrank[nd];
-    householder_qr(A, m, r, rmat[nd], 0, qtau, stream);
+    flops += qr_flops((double)m, (double)r);
+    qr(A, m, r, rmat[nd], 0);
   }
   void apply_to_parent(int nd, double2* Ap, int p) {
+    Prof pf(this, 6, p);
     long long na, nb;
     int d;
     r3(p, T.slot[nd], na, d, nb);
@@ -833,15 +1075,18 @@ struct Integrator {
     zcopy(Ap, w4, T.size(p), stream);
   }
   void r2l(int nd, int mu, double2* A) {
+    Prof pf(this, 2, nd);
     long long pre = 1, post = T.hrank[nd];
     for (int i = 0; i < mu; ++i) pre *= T.dims[nd][i];
     const int dm = T.dims[nd][mu];
     for (int i = mu + 1; i < T.nmodes[nd]; ++i) post *= T.dims[nd][i];
+    flops += qr_flops((double)(pre * post), (double)dm);
     permute_mode_last(A, w4, pre, dm, post, stream);
-    householder_qr(w4, pre * post, dm, rmat[nd], 1, qtau, stream);
+    qr(w4, pre * post, dm, rmat[nd], 1);
     unpermute_mode_last(w4, A, pre, dm, post, stream);
   }
   void apply_from_parent(int nd, double2* A) {
+    Prof pf(this, 7, nd);
     const int p = T.parent[nd], r = T.hrank[nd];
     right_mul(A, rmat[p], T.dimen[nd], r, w4);
     zcopy(A, w4, T.size(nd), stream);
@@ -849,12 +1094,13 @@ struct Integrator {
 
   // ---------------------------------------------------------------- sweep
   void evolve_node(ttn_state* S, int nd) {
-    double2* A = S->node(nd);
-    expm([&](const double2* v, double2* o) { heff(nd, v, o); }, A, T.size(nd), dt / 2.0, coeff, true);
+    Prof pf(this, 0, nd);
+    expm_dev(nd, 0, S->node(nd), T.size(nd), dt / 2.0, coeff, true);
   }
   void evolve_bond(int nd, double2* R) {
+    Prof pf(this, 1, nd);
     const long long rr = (long long)T.hrank[nd] * T.hrank[nd];
-    expm([&](const double2* v, double2* o) { kbond(nd, v, o); }, R, rr, -dt / 2.0, coeff, false);
+    expm_dev(nd, 1, R, rr, -dt / 2.0, coeff, false);
   }
   void forward(ttn_state* S, bool evolve) {
     std::vector<int> tv(T.n, 0);
@@ -937,13 +1183,28 @@ struct Integrator {
     dt = step_dt;
     finish_check(S);
   }
+  // environments and gauge passes of the first step without its evolution; later
+  // steps are then full dt steps (used to time steady-state sweeps)
+  void prepare_only(ttn_state* S) {
+    prepare(S);
+    nsteps = std::max<long long>(nsteps, 1);
+    finish_check(S);
+  }
   void finish_check(ttn_state* S) {
-    CK(cudaMemsetAsync(status, 0, sizeof(int), stream));
-    check_finite(S->arena.as<double2>(), (long long)(S->arena.bytes / sizeof(double2)), status, 1, stream);
+    check_finite(S->arena.as<double2>(), (long long)(S->arena.bytes / sizeof(double2)), status, kErrNonFinite, stream);
     int h = 0;
+    long long napps = 0;
     CK(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(&napps, nh_dev, sizeof(long long), cudaMemcpyDeviceToHost, stream));
+    d2h_bytes += sizeof(int) + sizeof(long long);
     CK(cudaStreamSynchronize(stream));
     CK(cudaGetLastError());
+    nh = napps;
+    CK(cudaMemsetAsync(status, 0, sizeof(int), stream));
+    TTN_REQUIRE(!(h & kErrBarrierTimeout), TTN_ETIMEOUT, "a device-side grid barrier gave up waiting");
+    TTN_REQUIRE(!(h >> kKrylovErrShift), TTN_ENUMERIC,
+                "Krylov exponential failed (status " + std::to_string(h >> kKrylovErrShift) +
+                    ": 1 tolerance unreachable, 2 non-finite vector, 4 eigen-solve, 8 step size, 16 sub-step limit)");
     TTN_REQUIRE(h == 0, TTN_ENUMERIC, "the state holds non-finite values after the step");
   }
 
@@ -977,6 +1238,7 @@ struct Integrator {
     ztrace(mel[0], T.hrank[0], scal + 1, stream);
     double2 h;
     CK(cudaMemcpyAsync(&h, scal + 1, sizeof(double2), cudaMemcpyDeviceToHost, stream));
+    d2h_bytes += sizeof(double2);
     CK(cudaStreamSynchronize(stream));
     return cd(h.x, h.y);
   }
@@ -1303,6 +1565,7 @@ int ttn_integrator_reset(ttn_integrator* it) {
   TTN_REQUIRE(it, TTN_EINVAL, "null argument");
   it->I.nsteps = 0;
   it->I.nh = 0;
+  CK(cudaMemset(it->I.nh_dev, 0, sizeof(long long)));
   TTN_API_END
 }
 int ttn_integrator_synchronize(ttn_integrator* it) {
@@ -1323,6 +1586,7 @@ int ttn_expect_leaf(ttn_integrator* it, ttn_state* psi, int mode, const double* 
     int d = it->I.H.mode_dim[mode];
     TTN_REQUIRE((long long)d * d <= it->I.ldv, TTN_ECAPACITY, "observable operator larger than the work buffer");
     CK(cudaMemcpyAsync(it->I.w3, op, (size_t)d * d * sizeof(double2), cudaMemcpyHostToDevice, it->I.stream));
+    it->I.h2d_bytes += (long long)d * d * sizeof(double2);
     dop = it->I.w3;
   }
   ttn::cd v = it->I.expect(psi, mode, dop);
@@ -1335,6 +1599,136 @@ int ttn_norm2(ttn_integrator* it, ttn_state* psi, double* out) {
   int rc = ttn_expect_leaf(it, psi, 0, nullptr, &re, &im);
   if (rc == TTN_OK && out) *out = re;
   return rc;
+}
+
+int ttn_integrator_prepare(ttn_integrator* it, ttn_state* psi) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi, TTN_EINVAL, "null argument");
+  ttn::check_same_tree(it->I.T, psi->T);
+  CK(cudaSetDevice(it->I.device));
+  it->I.prepare_only(psi);
+  TTN_API_END
+}
+int ttn_integrator_flops(const ttn_integrator* it, double* out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && out, TTN_EINVAL, "null argument");
+  *out = it->I.flops;
+  TTN_API_END
+}
+int ttn_integrator_timer(ttn_integrator* it, int start, double* ms) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it, TTN_EINVAL, "null argument");
+  CK(cudaSetDevice(it->I.device));
+  if (start) {
+    CK(cudaEventRecord(it->I.ev0, it->I.stream));
+  } else {
+    CK(cudaEventRecord(it->I.ev1, it->I.stream));
+    CK(cudaEventSynchronize(it->I.ev1));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, it->I.ev0, it->I.ev1));
+    if (ms) *ms = f;
+  }
+  TTN_API_END
+}
+int ttn_bench_node_op(ttn_integrator* it, ttn_state* psi, int node, int kind, int reps, double* ms_per_rep,
+                      double* flops_per_rep) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi && reps >= 1, TTN_EINVAL, "bad argument");
+  auto& I = it->I;
+  TTN_REQUIRE(node >= 0 && node < I.T.n, TTN_EINVAL, "node out of range");
+  ttn::check_same_tree(I.T, psi->T);
+  CK(cudaSetDevice(I.device));
+  const long long n = I.T.size(node);
+  double f0 = I.flops;
+  ttn::zcopy(I.w4, psi->node(node), n, I.stream);
+  auto run = [&]() {
+    switch (kind) {
+      case 0: I.heff(node, psi->node(node), I.p); break;
+      case 1: {
+        ttn::zcopy(I.w4, psi->node(node), n, I.stream);
+        I.expm_dev(node, 0, I.w4, n, I.dt > 0 ? I.dt / 2 : 0.01, ttn::cd(0.0, -1.0), false);
+        break;
+      }
+      case 3: {
+        const long long rr = (long long)I.T.hrank[node] * I.T.hrank[node];
+        ttn::zcopy(I.w4, I.rmat[node], rr, I.stream);
+        I.expm_dev(node, 1, I.w4, rr, I.dt > 0 ? -I.dt / 2 : -0.01, ttn::cd(0.0, -1.0), false);
+        break;
+      }
+      case 2: {
+        ttn::zcopy(I.w4, psi->node(node), n, I.stream);
+        I.flops += I.qr_flops((double)I.T.dimen[node], (double)I.T.hrank[node]);
+        I.qr(I.w4, I.T.dimen[node], I.T.hrank[node], I.w3, 0);
+        break;
+      }
+      default: throw ttn::Err(TTN_EINVAL, "unknown benchmark kind");
+    }
+  };
+  run();  // warm-up
+  CK(cudaStreamSynchronize(I.stream));
+  f0 = I.flops;
+  CK(cudaEventRecord(I.ev0, I.stream));
+  for (int k = 0; k < reps; ++k) run();
+  CK(cudaEventRecord(I.ev1, I.stream));
+  CK(cudaEventSynchronize(I.ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, I.ev0, I.ev1));
+  CK(cudaGetLastError());
+  double fl = (I.flops - f0) / reps;
+  if (kind == 1 || kind == 3) {
+    // the persistent kernel's matvecs: H applications of the last repetition times the
+    // flops of one application, plus the Lanczos vector passes already counted
+    long long k = 0;
+    int subs = 0;
+    CK(cudaMemcpy(&k, &I.ctl->napps, sizeof(long long), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&subs, &I.ctl->substeps, sizeof(int), cudaMemcpyDeviceToHost));
+    fl = fl * (subs > 0 ? subs : 1) + (double)k * (kind == 1 ? I.heff_flops(node) : I.kbond_flops(node));
+  }
+  if (ms_per_rep) *ms_per_rep = ms / reps;
+  if (flops_per_rep) *flops_per_rep = fl;
+  I.flops = f0;
+  TTN_API_END
+}
+int ttn_integrator_profile(ttn_integrator* it, double* seconds, long long* counts) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && seconds && counts, TTN_EINVAL, "null argument");
+  for (int k = 0; k < 8; ++k)
+    for (int c = 0; c < 4; ++c) {
+      seconds[k * 4 + c] = it->I.prof_t[k][c];
+      counts[k * 4 + c] = it->I.prof_n[k][c];
+    }
+  TTN_API_END
+}
+int ttn_integrator_io_bytes(const ttn_integrator* it, long long* h2d, long long* d2h) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it, TTN_EINVAL, "null argument");
+  if (h2d) *h2d = it->I.h2d_bytes;
+  if (d2h) *d2h = it->I.d2h_bytes;
+  TTN_API_END
+}
+int ttn_host_alloc(long long bytes, void** out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(out && bytes > 0, TTN_EINVAL, "bad argument");
+  CK(cudaMallocHost(out, (size_t)bytes));
+  TTN_API_END
+}
+int ttn_host_free(void* p) {
+  TTN_API_BEGIN
+  if (p) CK(cudaFreeHost(p));
+  TTN_API_END
+}
+int ttn_launch_count(unsigned long long* out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(out, TTN_EINVAL, "null argument");
+  *out = ttn::g_launches;
+  TTN_API_END
+}
+int ttn_device_fp64_peak(int device, double* tflops) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(tflops, TTN_EINVAL, "null argument");
+  CK(cudaSetDevice(device));
+  *tflops = ttn::measure_fp64_fma_tflops();
+  TTN_API_END
 }
 
 int ttn_debug_refresh_env(ttn_integrator* it, ttn_state* psi) {
@@ -1370,12 +1764,16 @@ int ttn_debug_expm_node(ttn_integrator* it, int node, double tau, double cre, do
   const long long n = I.T.size(node);
   CK(cudaMemcpyAsync(I.w4, v, n * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
   // w4 is a gauge scratch; the exponential itself uses V, p, w1-w3
-  long long before = I.nh;
-  I.expm([&](const double2* a, double2* o) { I.heff(node, a, o); }, I.w4, n, tau, ttn::cd(cre, cim), true);
+  long long k = 0;
+  I.expm_dev(node, 0, I.w4, n, tau, ttn::cd(cre, cim), false);
   CK(cudaMemcpyAsync(v, I.w4, n * sizeof(double2), cudaMemcpyDeviceToHost, I.stream));
+  CK(cudaMemcpyAsync(&k, &I.ctl->napps, sizeof(long long), cudaMemcpyDeviceToHost, I.stream));
   CK(cudaStreamSynchronize(I.stream));
-  if (napps) *napps = I.nh - before;
-  I.nh = before;
+  int h = 0;
+  CK(cudaMemcpy(&h, I.status, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemset(I.status, 0, sizeof(int)));
+  TTN_REQUIRE(h == 0, TTN_ENUMERIC, "Krylov exponential failed on the device");
+  if (napps) *napps = (tau == 0.0) ? 0 : k;
   TTN_API_END
 }
 int ttn_debug_num_groups(ttn_integrator* it, int node, int* out) {
@@ -1406,8 +1804,21 @@ int ttn_debug_qr(int m, int n, double* a, double* r, int device) {
   double2* dR = dA + (size_t)m * n;
   double2* dt = dR + (size_t)n * n;
   CK(cudaMemcpy(dA, a, (size_t)m * n * sizeof(double2), cudaMemcpyHostToDevice));
-  ttn::householder_qr(dA, m, n, dR, 0, dt, 0);
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  int g = std::min(ttn::coop_qr_grid(m, sms), std::max(1, std::min(ttn::coop_qr_max_grid(), sms)));
+  ttn::DevBuf cb;
+  cb.alloc(ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(ttn::coop_qr_scratch_bytes(g)) + 256);
+  CK(cudaMemset(cb.p, 0, cb.bytes));
+  auto* bar = cb.as<ttn::GridBarrier>();
+  double* scr = (double*)(cb.as<char>() + ttn::align256(sizeof(ttn::GridBarrier)));
+  int* err = (int*)(cb.as<char>() + ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(ttn::coop_qr_scratch_bytes(g)));
+  CK(ttn::householder_qr_coop(dA, m, n, dR, 0, dt, scr, bar, err, g, 0));
   CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  int herr = 0;
+  CK(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
+  TTN_REQUIRE(herr == 0, TTN_ETIMEOUT, "device QR barrier gave up waiting");
   CK(cudaGetLastError());
   CK(cudaMemcpy(a, dA, (size_t)m * n * sizeof(double2), cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(r, dR, (size_t)n * n * sizeof(double2), cudaMemcpyDeviceToHost));

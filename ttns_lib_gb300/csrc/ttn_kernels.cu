@@ -13,11 +13,15 @@
 //   * Householder QR with LAPACK zlarfg conventions for the gauge moves of
 //     root_to_leaf_decomposition.hpp:113-183 and leaf_to_root_decomposition.hpp:57-101.
 #include "ttn_kernels.cuh"
+#include "ttn_coop.cuh"
 
 #include <cmath>
 #include <cstdio>
 
 namespace ttn {
+
+// kernel launches issued by this library (host-side counter)
+unsigned long long g_launches = 0;
 
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
@@ -99,14 +103,15 @@ __global__ void __launch_bounds__(GT_THREADS) k_zgemm(ZGemm g, double2* part, in
       Bs[kk][jj] = (j < g.N && k < ke) ? ld_op(B, j, k) : make_double2(0.0, 0.0);
     }
     __syncthreads();
+    const bool r1 = i0 + ty + 16 < g.M, c1 = j0 + tx + 16 < g.N;
 #pragma unroll
     for (int kk = 0; kk < GT_K; ++kk) {
       double2 a0 = As[kk][ty], a1 = As[kk][ty + 16];
       double2 b0 = Bs[kk][tx], b1 = Bs[kk][tx + 16];
       acc[0][0] = cfma(a0, b0, acc[0][0]);
-      acc[0][1] = cfma(a0, b1, acc[0][1]);
-      acc[1][0] = cfma(a1, b0, acc[1][0]);
-      acc[1][1] = cfma(a1, b1, acc[1][1]);
+      if (c1) acc[0][1] = cfma(a0, b1, acc[0][1]);
+      if (r1) acc[1][0] = cfma(a1, b0, acc[1][0]);
+      if (r1 && c1) acc[1][1] = cfma(a1, b1, acc[1][1]);
     }
     __syncthreads();
   }
@@ -128,6 +133,58 @@ __global__ void __launch_bounds__(GT_THREADS) k_zgemm(ZGemm g, double2* part, in
     }
 }
 
+// 16x16 output tile, one output per thread: small contractions spread over more SMs.
+__global__ void __launch_bounds__(256) k_zgemm16(ZGemm g, double2* part, int ksplit) {
+  __shared__ double2 As[16][17];
+  __shared__ double2 Bs[16][17];
+  const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+  const long long i0 = (long long)blockIdx.y * 16, j0 = (long long)blockIdx.x * 16;
+  const int z = blockIdx.z;
+  ZOperand A = g.A, B = g.B;
+  double2* C = g.C;
+  long long kb = 0, ke = g.K;
+  if (ksplit > 1) {
+    long long chunk = (g.K + ksplit - 1) / ksplit;
+    kb = (long long)z * chunk;
+    ke = min((long long)g.K, kb + chunk);
+  } else {
+    A.p += (long long)z * g.bsA;
+    B.p += (long long)z * g.bsB;
+    C += (long long)z * g.bsC;
+  }
+  const bool valid = (i0 + ty < g.M) && (j0 + tx < g.N);
+  double2 acc = make_double2(0.0, 0.0);
+  for (long long k0 = kb; k0 < ke; k0 += 16) {
+    {
+      int ii, kk;
+      if (A.kfast) { kk = tid % 16; ii = tid / 16; } else { ii = tid % 16; kk = tid / 16; }
+      long long i = i0 + ii, k = k0 + kk;
+      As[kk][ii] = (i < g.M && k < ke) ? ld_op(A, i, k) : make_double2(0.0, 0.0);
+      int jj;
+      if (B.kfast) { kk = tid % 16; jj = tid / 16; } else { jj = tid % 16; kk = tid / 16; }
+      long long j = j0 + jj;
+      k = k0 + kk;
+      Bs[kk][jj] = (j < g.N && k < ke) ? ld_op(B, j, k) : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    if (valid) {
+#pragma unroll
+      for (int kk = 0; kk < 16; ++kk) acc = cfma(As[kk][ty], Bs[kk][tx], acc);
+    }
+    __syncthreads();
+  }
+  if (!valid) return;
+  long long i = i0 + ty, j = j0 + tx;
+  if (ksplit > 1) {
+    part[((long long)z * g.M + i) * g.N + j] = acc;
+  } else {
+    double2* c = C + i * g.ci + j * g.cj;
+    double2 r = cmul(g.alpha, acc);
+    if (g.beta.x != 0.0 || g.beta.y != 0.0) r = cfma(g.beta, *c, r);
+    *c = r;
+  }
+}
+
 __global__ void k_zgemm_reduce(ZGemm g, const double2* part, int ksplit) {
   long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long total = (long long)g.M * g.N;
@@ -141,16 +198,22 @@ __global__ void k_zgemm_reduce(ZGemm g, const double2* part, int ksplit) {
   *c = r;
 }
 
-int choose_split(int M, int N, int K, int batch) {
-  if (batch != 1) return 1;
-  long long tiles = (long long)((M + GT_M - 1) / GT_M) * ((N + GT_N - 1) / GT_N);
-  if (tiles >= 304 || K < 256) return 1;
-  long long want = (608 + tiles - 1) / tiles;
-  long long maxs = (K + 127) / 128;
+// Tile size and K split: big outputs use 32x32 tiles; small ones 16x16 tiles with K
+// split so that roughly two CTAs per SM take part (FP64 runs at ~2 FMA/clk/SM here).
+struct GemmPlan { int tile; int ksplit; };
+GemmPlan plan_gemm(int M, int N, int K, int batch) {
+  long long t32 = (long long)((M + GT_M - 1) / GT_M) * ((N + GT_N - 1) / GT_N) * batch;
+  if (t32 >= 304) return {32, 1};
+  long long t16 = (long long)((M + 15) / 16) * ((N + 15) / 16) * batch;
+  if (batch != 1) return {t16 >= 2 * t32 ? 16 : 32, 1};
+  long long want = (304 + t16 - 1) / t16;
+  long long maxs = (K + 15) / 16;
   long long s = want < maxs ? want : maxs;
   if (s > 512) s = 512;
-  return s < 1 ? 1 : (int)s;
+  if (s < 1) s = 1;
+  return {16, (int)s};
 }
+int choose_split(int M, int N, int K, int batch) { return plan_gemm(M, N, K, batch).ksplit; }
 }  // namespace
 
 size_t zgemm_split_workspace_bytes(int M, int N, int K) {
@@ -160,7 +223,8 @@ size_t zgemm_split_workspace_bytes(int M, int N, int K) {
 
 void zgemm(const ZGemm& g, double2* ws, size_t ws_bytes, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return;
-  int ksplit = choose_split(g.M, g.N, g.K, g.batch);
+  GemmPlan pl = plan_gemm(g.M, g.N, g.K, g.batch);
+  int ksplit = pl.ksplit;
   while (ksplit > 1 && (size_t)ksplit * g.M * g.N * sizeof(double2) > ws_bytes) ksplit /= 2;
   if (ksplit == 1 && g.batch > 65535) {
     // grid.z is limited to 65535: issue the batch in chunks
@@ -174,10 +238,18 @@ void zgemm(const ZGemm& g, double2* ws, size_t ws_bytes, cudaStream_t s) {
     }
     return;
   }
-  dim3 grid((g.N + GT_N - 1) / GT_N, (g.M + GT_M - 1) / GT_M, ksplit > 1 ? ksplit : g.batch);
-  k_zgemm<<<grid, GT_THREADS, 0, s>>>(g, ws, ksplit);
+  if (pl.tile == 16) {
+    dim3 grid16((g.N + 15) / 16, (g.M + 15) / 16, ksplit > 1 ? ksplit : g.batch);
+    ++g_launches;
+    k_zgemm16<<<grid16, 256, 0, s>>>(g, ws, ksplit);
+  } else {
+    dim3 grid((g.N + GT_N - 1) / GT_N, (g.M + GT_M - 1) / GT_M, ksplit > 1 ? ksplit : g.batch);
+    ++g_launches;
+    k_zgemm<<<grid, GT_THREADS, 0, s>>>(g, ws, ksplit);
+  }
   if (ksplit > 1) {
     long long total = (long long)g.M * g.N;
+    ++g_launches;
     k_zgemm_reduce<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(g, ws, ksplit);
   }
 }
@@ -413,9 +485,15 @@ __device__ double2 cexp_d(double2 x) {
   return make_double2(ex * cs, ex * sn);
 }
 __device__ double cabs_d(double2 x) { return hypot(x.x, x.y); }
+// a / b by Smith's algorithm (CACM 5(8), 1962): no squared magnitudes, so no spurious
+// underflow or overflow for very small or very large b.
 __device__ double2 cdiv_d(double2 a, double2 b) {
-  double den = b.x * b.x + b.y * b.y;
-  return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+  if (fabs(b.x) >= fabs(b.y)) {
+    double r = b.y / b.x, den = b.x + b.y * r;
+    return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+  }
+  double r = b.x / b.y, den = b.x * r + b.y;
+  return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
 }
 // phi_1(x) = (e^x - 1)/x, phi_2(x) = (e^x - 1 - x)/x^2
 __device__ double2 dphi1(double2 x) {
@@ -588,12 +666,15 @@ int vec_blocks(long long n) {
 }
 
 void krylov_init_ctl(KrylovCtl* ctl, int m, double tau, double cre, double cim, double tol, cudaStream_t s) {
+  ++g_launches;
   k_init_ctl<<<1, 32, 0, s>>>(ctl, m, tau, cre, cim, tol);
 }
 
 void krylov_begin(KrylovCtl* ctl, const double2* y, double2* V0, long long n, double2* part, cudaStream_t s) {
   int nb = vec_blocks(n);
+  ++g_launches;
   k_norm_partial<<<nb, VT, 0, s>>>(y, n, part);
+  ++g_launches;
   k_begin<<<nb, VT, 0, s>>>(ctl, y, V0, n, part, nb);
 }
 
@@ -602,23 +683,33 @@ void lanczos_orth(KrylovCtl* ctl, int j, double2* V, long long ldv, double2* p, 
   int nb = vec_blocks(n);
   double2* pa = part;
   double2* pb = part + (size_t)VMAXB * VQ;
+  ++g_launches;
   k_orth1<<<nb, VT, 0, s>>>(V + (long long)j * ldv, p, n, pa);
+  ++g_launches;
   k_orth2<<<nb, VT, 0, s>>>(ctl, j, V, ldv, p, n, pa, nb, pb);
+  ++g_launches;
   k_orth3<<<nb, VT, 0, s>>>(j, V, ldv, p, n, pb, nb, pa);
+  ++g_launches;
   k_orth4<<<nb, VT, 0, s>>>(ctl, j, V, ldv, p, n, pa, nb);
 }
 
 void lanczos_avnorm(KrylovCtl* ctl, const double2* p, long long n, double2* part, cudaStream_t s) {
   int nb = vec_blocks(n);
+  ++g_launches;
   k_norm_partial<<<nb, VT, 0, s>>>(p, n, part);
+  ++g_launches;
   k_avnorm<<<1, 32, 0, s>>>(ctl, part, nb);
 }
 
-void krylov_control(KrylovCtl* ctl, cudaStream_t s) { k_control<<<1, 32, 0, s>>>(ctl); }
+void krylov_control(KrylovCtl* ctl, cudaStream_t s) {
+  ++g_launches;
+  k_control<<<1, 32, 0, s>>>(ctl);
+}
 
 void krylov_combine(KrylovCtl* ctl, const double2* V, long long ldv, double2* y, long long n, int nq,
                     cudaStream_t s) {
   int nb = vec_blocks(n);
+  ++g_launches;
   k_combine<<<nb, VT, 0, s>>>(ctl, V, ldv, y, n, nq);
 }
 
@@ -688,32 +779,94 @@ __device__ void apply_reflector(double2* M, long long m, int n, int col, long lo
   __syncthreads();
 }
 
+__device__ double block_max_qr(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s = fmax(s, red[k]);
+    red[32] = s;
+  }
+  __syncthreads();
+  double s = red[32];
+  __syncthreads();
+  return s;
+}
+
+// sqrt(x^2 + y^2 + z^2) without destructive underflow or overflow (LAPACK dlapy3 scheme)
+__device__ double dlapy3_d(double x, double y, double z) {
+  double w = fmax(fabs(x), fmax(fabs(y), fabs(z)));
+  if (w == 0.0) return 0.0;
+  double a = x / w, b = y / w, c = z / w;
+  return w * sqrt(a * a + b * b + c * c);
+}
+
 __global__ void __launch_bounds__(QT) k_householder_qr(double2* M, long long m, int n, double2* R, int Rt,
                                                        double2* tau) {
   __shared__ double2 wacc[QT / 32][QMAXN];
   __shared__ double2 wsh[QMAXN];
   __shared__ double red[33];
   __shared__ double2 s_tau, s_scal, s_beta;
+  __shared__ double s_xscale;
+  const double safmin = 2.2250738585072014e-308 / 1.1102230246251565e-16;  // 2^-969
   for (int j = 0; j < n; ++j) {
-    double s = 0.0;
+    // scaled norm of the sub-column: max first, then the sum of scaled squares
+    double amax = 0.0;
     for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
       double2 x = M[i * n + j];
-      s += x.x * x.x + x.y * x.y;
+      amax = fmax(amax, fmax(fabs(x.x), fabs(x.y)));
     }
-    const double xn2 = block_sum_qr(s, red);
+    amax = block_max_qr(amax, red);
+    double s = 0.0;
+    if (amax > 1e-290) {
+      const double inv = 1.0 / amax;
+      for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
+        double2 x = M[i * n + j];
+        double a = x.x * inv, b = x.y * inv;
+        s += a * a + b * b;
+      }
+    } else if (amax > 0.0) {
+      // 1/amax would overflow for denormal columns: divide instead
+      for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
+        double2 x = M[i * n + j];
+        double a = x.x / amax, b = x.y / amax;
+        s += a * a + b * b;
+      }
+    }
+    s = block_sum_qr(s, red);
     if (threadIdx.x == 0) {
       double2 alpha = M[(long long)j * n + j];
-      double xnorm = sqrt(xn2);
+      double xnorm = amax * sqrt(s);
       double ar = alpha.x, ai = alpha.y;
+      s_xscale = 1.0;
       if (xnorm == 0.0 && ai == 0.0) {
         s_tau = make_double2(0.0, 0.0);
         s_beta = alpha;
         s_scal = make_double2(0.0, 0.0);
       } else {
-        double bnorm = sqrt(ar * ar + ai * ai + xn2);
-        double b = (ar >= 0.0) ? -bnorm : bnorm;
+        double b = -copysign(dlapy3_d(ar, ai, xnorm), ar >= 0.0 ? 1.0 : -1.0);
+        int knt = 0;
+        double xs = 1.0;
+        if (fabs(b) < safmin) {
+          // rescale tiny columns by the exact power of two 1/safmin (zlarfg), at most 20 times
+          const double rs = 1.0 / safmin;
+          do {
+            ++knt;
+            xs *= rs;
+            b *= rs;
+            ar *= rs;
+            ai *= rs;
+            xnorm *= rs;
+          } while (fabs(b) < safmin && knt < 20);
+          b = -copysign(dlapy3_d(ar, ai, xnorm), ar >= 0.0 ? 1.0 : -1.0);
+        }
         s_tau = make_double2((b - ar) / b, -ai / b);
         s_scal = cdiv_d(make_double2(1.0, 0.0), make_double2(ar - b, ai));
+        s_xscale = xs;
+        for (int q = 0; q < knt; ++q) b *= safmin;
         s_beta = make_double2(b, 0.0);
       }
       tau[j] = s_tau;
@@ -721,7 +874,13 @@ __global__ void __launch_bounds__(QT) k_householder_qr(double2* M, long long m, 
     __syncthreads();
     const double2 tj = s_tau;
     if (tj.x != 0.0 || tj.y != 0.0) {
-      for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) M[i * n + j] = cmul(M[i * n + j], s_scal);
+      const double xs = s_xscale;
+      for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
+        double2 x = M[i * n + j];
+        x.x *= xs;
+        x.y *= xs;
+        M[i * n + j] = cmul(x, s_scal);
+      }
     }
     __syncthreads();
     if (threadIdx.x == 0) M[(long long)j * n + j] = s_beta;
@@ -816,30 +975,399 @@ unsigned grid_for(long long n, int threads = 256) {
 }
 }  // namespace
 
+
+// =====================================================================================
+// Cooperative Householder QR: every CTA owns a contiguous block of rows; two grid
+// barriers per column in the factorisation and one per column when forming Q.  The
+// arithmetic per element is that of k_householder_qr (scaled zlarfg); only the order
+// of the partial sums differs.
+// =====================================================================================
+namespace {
+constexpr int CQT = 256;           // threads per CTA
+constexpr int CQN = kQrMaxCols;    // widest matrix
+
+struct CoopQrArgs {
+  double2* M;
+  long long m;
+  int n;
+  double2* R;
+  int Rt;
+  double2* tau_out;
+  double* part;        // [3 + 2*CQN*2][gridDim] scratch, see offsets below
+  GridBarrier* bar;
+  int* err;
+};
+
+// per-CTA scaled partial norm of rows in (j, m) of column j, over my rows
+__device__ void coop_partial_norm(const CoopQrArgs& a, int j, long long r0, long long r1, double* red,
+                                  double* out_max, double* out_sum) {
+  double lmax = 0.0;
+  for (long long i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+    if (i > j) {
+      double2 x = a.M[i * a.n + j];
+      lmax = fmax(lmax, fmax(fabs(x.x), fabs(x.y)));
+    }
+  lmax = block_max_qr(lmax, red);
+  double s = 0.0;
+  if (lmax > 0.0) {
+    for (long long i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+      if (i > j) {
+        double2 x = a.M[i * a.n + j];
+        double p = x.x / lmax, q = x.y / lmax;
+        s += p * p + q * q;
+      }
+  }
+  s = block_sum_qr(s, red);
+  *out_max = lmax;
+  *out_sum = s;
+}
+
+// w_c = f * sum_q pw[q][c] for c < nc, all threads: CQT/CQN partial subsets per column
+__device__ void reduce_w_partials(const double* pw, int G, int nc, double2 f, double2 (*s_part)[CQN], double2* s_w) {
+  const int c = threadIdx.x % CQN, sub = threadIdx.x / CQN, nsub = blockDim.x / CQN;
+  double2 t = make_double2(0.0, 0.0);
+  if (c < nc)
+    for (int q = sub; q < G; q += nsub)
+      t = cadd(t, make_double2(pw[(size_t)q * 2 * CQN + 2 * c], pw[(size_t)q * 2 * CQN + 2 * c + 1]));
+  __syncthreads();
+  s_part[sub][c] = t;
+  __syncthreads();
+  if (threadIdx.x < nc) {
+    double2 u = make_double2(0.0, 0.0);
+    for (int k = 0; k < nsub; ++k) u = cadd(u, s_part[k][threadIdx.x]);
+    s_w[threadIdx.x] = cmul(f, u);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(CQT) k_qr_coop(CoopQrArgs a) {
+  __shared__ double red[33];
+  __shared__ double2 s_tau[CQN];
+  __shared__ double2 s_scal, s_beta;
+  __shared__ double s_xs;
+  __shared__ double2 s_w[CQN];
+  __shared__ double2 s_part[CQT / CQN > 0 ? CQT / CQN : 1][CQN];
+  const int G = gridDim.x, b = blockIdx.x;
+  const long long m = a.m;
+  const int n = a.n;
+  const long long r0 = b * m / G, r1 = (b + 1) * m / G;
+  const double safmin = 2.2250738585072014e-308 / 1.1102230246251565e-16;
+  // scratch layout (doubles): norm partials 2x[G][2], alpha slots 2x[2], w partials 2x[G][2*CQN];
+  // the norm / alpha slots alternate with the column parity so that a CTA running ahead
+  // never overwrites values a slower CTA still has to read
+  double* pn_buf[2] = {a.part, a.part + 2 * G};
+  double* pa_buf[2] = {a.part + 4 * G, a.part + 4 * G + 2};
+  double* pw0 = a.part + 4 * G + 4;
+  double* pw1 = pw0 + (size_t)G * 2 * CQN;
+  const int nsub = CQT / CQN;  // row subsets per CTA in the partial products
+
+  {
+    double lm, ls;
+    coop_partial_norm(a, 0, r0, r1, red, &lm, &ls);
+    if (threadIdx.x == 0) {
+      pn_buf[0][2 * b] = lm;
+      pn_buf[0][2 * b + 1] = ls;
+      if (0 >= r0 && 0 < r1) {
+        pa_buf[0][0] = a.M[0].x;
+        pa_buf[0][1] = a.M[0].y;
+      }
+    }
+  }
+  for (int j = 0; j < n; ++j) {
+    grid_barrier(a.bar, a.err);
+    const double* pn = pn_buf[j & 1];
+    const double* palpha = pa_buf[j & 1];
+    double* pn_next = pn_buf[(j + 1) & 1];
+    double* pa_next = pa_buf[(j + 1) & 1];
+    // reflector scalars, computed identically by every CTA (block-parallel reductions
+    // over the per-CTA partials)
+    double amax, ssum;
+    {
+      double lm = 0.0;
+      for (int q = threadIdx.x; q < G; q += blockDim.x) lm = fmax(lm, pn[2 * q]);
+      amax = block_max_qr(lm, red);
+      double ls = 0.0;
+      if (amax > 0.0)
+        for (int q = threadIdx.x; q < G; q += blockDim.x) {
+          double l = pn[2 * q];
+          if (l > 0.0) {
+            double f = l / amax;
+            ls += pn[2 * q + 1] * f * f;
+          }
+        }
+      ssum = block_sum_qr(ls, red);
+    }
+    if (threadIdx.x == 0) {
+      double xnorm = amax * sqrt(ssum);
+      double ar = palpha[0], ai = palpha[1];
+      s_xs = 1.0;
+      if (xnorm == 0.0 && ai == 0.0) {
+        s_tau[j] = make_double2(0.0, 0.0);
+        s_beta = make_double2(ar, ai);
+        s_scal = make_double2(0.0, 0.0);
+      } else {
+        double bb = -copysign(dlapy3_d(ar, ai, xnorm), ar >= 0.0 ? 1.0 : -1.0);
+        int knt = 0;
+        double xs = 1.0;
+        if (fabs(bb) < safmin) {
+          const double rs = 1.0 / safmin;
+          do {
+            ++knt;
+            xs *= rs;
+            bb *= rs;
+            ar *= rs;
+            ai *= rs;
+            xnorm *= rs;
+          } while (fabs(bb) < safmin && knt < 20);
+          bb = -copysign(dlapy3_d(ar, ai, xnorm), ar >= 0.0 ? 1.0 : -1.0);
+        }
+        s_tau[j] = make_double2((bb - ar) / bb, -ai / bb);
+        s_scal = cdiv_d(make_double2(1.0, 0.0), make_double2(ar - bb, ai));
+        s_xs = xs;
+        for (int q = 0; q < knt; ++q) bb *= safmin;
+        s_beta = make_double2(bb, 0.0);
+      }
+      if (b == 0) a.tau_out[j] = s_tau[j];
+    }
+    __syncthreads();
+    const double2 tj = s_tau[j];
+    const bool active = (tj.x != 0.0 || tj.y != 0.0);
+    if (active) {
+      const double xs = s_xs;
+      const double2 sc = s_scal;
+      for (long long i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+        if (i > j) {
+          double2 x = a.M[i * n + j];
+          x.x *= xs;
+          x.y *= xs;
+          a.M[i * n + j] = cmul(x, sc);
+        }
+    }
+    __syncthreads();
+    if (j >= r0 && j < r1 && threadIdx.x == 0) a.M[(long long)j * n + j] = s_beta;
+    const int nc = n - j - 1;
+    if (!active || nc == 0) {
+      // no reflector: next column's norm partial over my (unchanged) rows
+      __syncthreads();
+      if (j + 1 < n) {
+        double lm, ls;
+        coop_partial_norm(a, j + 1, r0, r1, red, &lm, &ls);
+        if (threadIdx.x == 0) {
+          pn_next[2 * b] = lm;
+          pn_next[2 * b + 1] = ls;
+          if (j + 1 >= r0 && j + 1 < r1) {
+            pa_next[0] = a.M[(long long)(j + 1) * n + j + 1].x;
+            pa_next[1] = a.M[(long long)(j + 1) * n + j + 1].y;
+          }
+        }
+      }
+      continue;
+    }
+    // w partials over my rows r >= j: sum conj(v_r) M[r][c], v_j = 1
+    {
+      const int c = j + 1 + (threadIdx.x % CQN);
+      const int sub = threadIdx.x / CQN;
+      double2 acc = make_double2(0.0, 0.0);
+      if (c < n) {
+        for (long long r = r0 + sub; r < r1; r += nsub) {
+          if (r < j) continue;
+          double2 v = (r == j) ? make_double2(1.0, 0.0) : a.M[r * n + j];
+          acc = cadd(acc, cmulc(v, a.M[r * n + c]));
+        }
+      }
+      s_part[sub][threadIdx.x % CQN] = acc;
+      __syncthreads();
+      if (threadIdx.x < CQN) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int q = 0; q < nsub; ++q) t = cadd(t, s_part[q][threadIdx.x]);
+        pw0[(size_t)b * 2 * CQN + 2 * threadIdx.x] = t.x;
+        pw0[(size_t)b * 2 * CQN + 2 * threadIdx.x + 1] = t.y;
+      }
+    }
+    grid_barrier(a.bar, a.err);
+    // reduce w (block order), apply to my rows, next column's norm partial
+    reduce_w_partials(pw0, G, nc, make_double2(tj.x, -tj.y), s_part, s_w);
+    {
+      const long long lo = r0 > j ? r0 : j;
+      const long long rows = r1 > lo ? r1 - lo : 0;
+      for (long long e = threadIdx.x; e < rows * nc; e += blockDim.x) {
+        long long r = lo + e / nc;
+        int c = j + 1 + (int)(e % nc);
+        double2 v = (r == j) ? make_double2(1.0, 0.0) : a.M[r * n + j];
+        a.M[r * n + c] = csub(a.M[r * n + c], cmul(v, s_w[c - j - 1]));
+      }
+    }
+    __syncthreads();
+    if (j + 1 < n) {
+      double lm, ls;
+      coop_partial_norm(a, j + 1, r0, r1, red, &lm, &ls);
+      if (threadIdx.x == 0) {
+        pn_next[2 * b] = lm;
+        pn_next[2 * b + 1] = ls;
+        if (j + 1 >= r0 && j + 1 < r1) {
+          pa_next[0] = a.M[(long long)(j + 1) * n + j + 1].x;
+          pa_next[1] = a.M[(long long)(j + 1) * n + j + 1].y;
+        }
+      }
+    }
+  }
+  grid_barrier(a.bar, a.err);
+  // R from my rows
+  for (long long e = threadIdx.x; e < (r1 - r0) * n; e += blockDim.x) {
+    long long i = r0 + e / n;
+    int k = (int)(e % n);
+    if (i >= n) continue;
+    double2 v = (k >= i) ? a.M[i * n + k] : make_double2(0.0, 0.0);
+    if (a.Rt) a.R[(long long)k * n + i] = v;
+    else a.R[i * n + k] = v;
+  }
+  __syncthreads();
+  // Q = H_0 ... H_{n-1} [I; 0]
+  for (int i = n - 1; i >= 0; --i) {
+    const double2 ti = s_tau[i];
+    const bool act = (ti.x != 0.0 || ti.y != 0.0) && i < n - 1;
+    const int nc = n - i - 1;
+    double* pw = (i & 1) ? pw1 : pw0;
+    if (act) {
+      const int c = i + 1 + (threadIdx.x % CQN);
+      const int sub = threadIdx.x / CQN;
+      double2 acc = make_double2(0.0, 0.0);
+      if (c < n) {
+        for (long long r = r0 + sub; r < r1; r += nsub) {
+          if (r < i) continue;
+          double2 v = (r == i) ? make_double2(1.0, 0.0) : a.M[r * n + i];
+          acc = cadd(acc, cmulc(v, a.M[r * n + c]));
+        }
+      }
+      s_part[sub][threadIdx.x % CQN] = acc;
+      __syncthreads();
+      if (threadIdx.x < CQN) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int q = 0; q < nsub; ++q) t = cadd(t, s_part[q][threadIdx.x]);
+        pw[(size_t)b * 2 * CQN + 2 * threadIdx.x] = t.x;
+        pw[(size_t)b * 2 * CQN + 2 * threadIdx.x + 1] = t.y;
+      }
+    }
+    grid_barrier(a.bar, a.err);
+    if (act) {
+      reduce_w_partials(pw, G, nc, ti, s_part, s_w);
+      const long long lo = r0 > i ? r0 : i;
+      const long long rows = r1 > lo ? r1 - lo : 0;
+      for (long long e = threadIdx.x; e < rows * nc; e += blockDim.x) {
+        long long r = lo + e / nc;
+        int c = i + 1 + (int)(e % nc);
+        double2 v = (r == i) ? make_double2(1.0, 0.0) : a.M[r * n + i];
+        a.M[r * n + c] = csub(a.M[r * n + c], cmul(v, s_w[c - i - 1]));
+      }
+      __syncthreads();
+    }
+    for (long long r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+      if (r > i) a.M[r * n + i] = cmul(make_double2(-ti.x, -ti.y), a.M[r * n + i]);
+      else if (r == i) a.M[r * n + i] = make_double2(1.0 - ti.x, -ti.y);
+      else a.M[r * n + i] = make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+  }
+}
+}  // namespace
+
+size_t coop_qr_scratch_bytes(int max_grid) {
+  return (size_t)(4 * max_grid + 4 + 2 * (size_t)max_grid * 2 * CQN) * sizeof(double);
+}
+
+int coop_qr_max_grid() {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_qr_coop, CQT, 0);
+  return sms * (per < 1 ? 1 : per);
+}
+
+int coop_qr_grid(long long m, int num_sms) {
+  long long g = m / 32;
+  if (g < 1) g = 1;
+  if (g > num_sms) g = num_sms;
+  return (int)g;
+}
+
+cudaError_t householder_qr_coop(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, double* scratch,
+                                GridBarrier* bar, int* err, int grid, cudaStream_t s) {
+  CoopQrArgs a{M, m, n, R, Rt, tau_ws, scratch, bar, err};
+  void* args[] = {&a};
+  ++g_launches;
+  return cudaLaunchCooperativeKernel((const void*)k_qr_coop, dim3(grid), dim3(CQT), args, 0, s);
+}
+
 void householder_qr(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, cudaStream_t s) {
+  ++g_launches;
   k_householder_qr<<<1, QT, 0, s>>>(M, m, n, R, Rt, tau_ws);
 }
 void permute_mode_last(const double2* A, double2* M, long long pre, int dm, long long post, cudaStream_t s) {
+  ++g_launches;
   k_permute_mode_last<<<grid_for(pre * dm * post), 256, 0, s>>>(A, M, pre, dm, post);
 }
 void unpermute_mode_last(const double2* M, double2* A, long long pre, int dm, long long post, cudaStream_t s) {
+  ++g_launches;
   k_unpermute_mode_last<<<grid_for(pre * dm * post), 256, 0, s>>>(M, A, pre, dm, post);
 }
 void zcopy(double2* dst, const double2* src, long long n, cudaStream_t s) {
-  if (n > 0) k_copy<<<grid_for(n), 256, 0, s>>>(dst, src, n);
+  if (n > 0) { ++g_launches; k_copy<<<grid_for(n), 256, 0, s>>>(dst, src, n); }
 }
 void zaxpy(double2* out, const double2* x, double2 sc, long long n, bool acc, cudaStream_t st) {
-  if (n > 0) k_axpy<<<grid_for(n), 256, 0, st>>>(out, x, sc, n, acc ? 1 : 0);
+  if (n > 0) { ++g_launches; k_axpy<<<grid_for(n), 256, 0, st>>>(out, x, sc, n, acc ? 1 : 0); }
 }
 void zfill(double2* dst, double2 v, long long n, cudaStream_t s) {
-  if (n > 0) k_fill<<<grid_for(n), 256, 0, s>>>(dst, v, n);
+  if (n > 0) { ++g_launches; k_fill<<<grid_for(n), 256, 0, s>>>(dst, v, n); }
 }
 void zscale_identity(double2* dst, int r, double2 v, cudaStream_t s) {
+  ++g_launches;
   k_scale_identity<<<grid_for((long long)r * r), 256, 0, s>>>(dst, r, v);
 }
-void ztrace(const double2* M, int r, double2* out, cudaStream_t s) { k_trace<<<1, 32, 0, s>>>(M, r, out); }
+void ztrace(const double2* M, int r, double2* out, cudaStream_t s) {
+  ++g_launches;
+  k_trace<<<1, 32, 0, s>>>(M, r, out);
+}
 void check_finite(const double2* x, long long n, int* status, int code, cudaStream_t s) {
-  if (n > 0) k_check_finite<<<grid_for(n), 256, 0, s>>>(x, n, status, code);
+  if (n > 0) { ++g_launches; k_check_finite<<<grid_for(n), 256, 0, s>>>(x, n, status, code); }
+}
+
+// ---- FP64 FMA peak probe: 8 independent FMA chains per thread, all SMs busy
+namespace {
+__global__ void k_fma_probe(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-9, x1 = x0 + 1e-9, x2 = x0 + 2e-9, x3 = x0 + 3e-9;
+  double x4 = x0 + 4e-9, x5 = x0 + 5e-9, x6 = x0 + 6e-9, x7 = x0 + 7e-9;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == 12345.678) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+double measure_fp64_fma_tflops() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  double* out = nullptr;
+  const int threads = 256, blocks = sms * 8, iters = 4096;
+  if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return 0.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fma_probe<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+  cudaEventRecord(e0);
+  const int reps = 5;
+  for (int r = 0; r < reps; ++r) k_fma_probe<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  double flops = 2.0 * 8.0 * iters * (double)blocks * threads * reps;
+  return ms > 0 ? flops / (ms * 1e-3) / 1e12 : 0.0;
 }
 
 }  // namespace ttn

@@ -6,6 +6,8 @@
 
 namespace ttn {
 
+extern unsigned long long g_launches;  // kernel launches issued by this library
+
 // Element addressing of a GEMM operand.
 //   A(i,k) = p[i*s0 + (k/kdiv)*k1 + (k%kdiv)*k2]        (conj if cj)
 //   B(k,j) = p[j*s0 + (k/kdiv)*k1 + (k%kdiv)*k2]        (conj if cj)
@@ -74,6 +76,16 @@ void krylov_init_ctl(KrylovCtl* ctl, int m, double tau, double cre, double cim, 
 // In-place Householder QR of an m x n row-major matrix (m >= n): M <- Q, R (n x n) out.
 // Rt != 0 stores R^T instead of R.
 void householder_qr(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, cudaStream_t s);
+// Cooperative multi-CTA version (grid <= co-resident CTAs); scratch of
+// coop_qr_scratch_bytes(grid) bytes, barrier state zero-initialised once, err is a
+// device status word (kErrBarrierTimeout on a barrier that gave up).
+struct GridBarrier;
+size_t coop_qr_scratch_bytes(int max_grid);
+int coop_qr_grid(long long m, int num_sms);
+// co-resident CTAs of the cooperative QR on the current device
+int coop_qr_max_grid();
+cudaError_t householder_qr_coop(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, double* scratch,
+                                GridBarrier* bar, int* err, int grid, cudaStream_t s);
 // r2l matricisation: M(y*pre + x, i) = A((x*dm + i)*post + y) and its inverse.
 void permute_mode_last(const double2* A, double2* M, long long pre, int dm, long long post, cudaStream_t s);
 void unpermute_mode_last(const double2* M, double2* A, long long pre, int dm, long long post, cudaStream_t s);
@@ -88,5 +100,8 @@ void zscale_identity(double2* dst, int r, double2 v, cudaStream_t s);
 void ztrace(const double2* M, int r, double2* out, cudaStream_t s);
 // status word: set to code if any element is non-finite
 void check_finite(const double2* x, long long n, int* status, int code, cudaStream_t s);
+
+// FP64 FMA throughput of the current device (TFLOP/s), from a long FMA-chain kernel.
+double measure_fp64_fma_tflops();
 
 }  // namespace ttn

@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--override-n", type=int, default=None,
+                    help="physical bath modes of a smaller tree of the same shape (profiling runs)")
     return ap.parse_args()
 
 
@@ -151,6 +153,25 @@ def traffic_from_profiles(kernel_tag: str):
     return None if e is None else e.get("dram_bytes_per_launch")
 
 
+class Nvtx:
+    """NVTX range around the timed region (lets ncu capture exactly the timed step)."""
+
+    def __init__(self):
+        try:
+            import torch.cuda.nvtx as nv
+            self.nv = nv
+        except Exception:
+            self.nv = None
+
+    def push(self, name):
+        if self.nv:
+            self.nv.range_push(name)
+
+    def pop(self):
+        if self.nv:
+            self.nv.range_pop()
+
+
 def upper_node(topo):
     """A node with the largest tensor: the dominant contraction happens there."""
     sizes = [topo.node_size(i) for i in range(topo.nnodes)]
@@ -221,9 +242,9 @@ def run_reference(args):
     return 0
 
 
-def workload_config(name, cfg, precision):
+def workload_config(name, cfg, precision, over=None):
     from ttns_lib_gb300 import spin_boson as sb
-    m, _ = sb.build_config(name)
+    m, _ = sb.build_config(name, **(over or {}))
     modes = len(m.omega)
     return {
         "workload": f"spin-boson ({'thermofield beta=' + str(cfg['beta']) if cfg.get('beta') else 'T=0'}), "
@@ -242,7 +263,8 @@ def run_ours(args):
     rank, world, local = dist_env()
     dist = Dist(world)
     device = local
-    m, cfg = sb.build_config(args.config)
+    over = {} if args.override_n is None else {"N": args.override_n}
+    m, cfg = sb.build_config(args.config, **over)
     topo = m.topology
     psi0 = np.array([1.0, 0.0])
 
@@ -268,6 +290,27 @@ def run_ours(args):
     else:
         A, tdvp = make(api.PREC_FP64)
 
+    # roofline of the dominant kernel: the persistent Krylov exponential on the largest
+    # node (it runs every H_eff contraction of the node update)
+    node = upper_node(topo)
+    k_ms, k_fl = tdvp.bench_node_op(A, node, 1, 5)
+    achieved = k_fl / (k_ms * 1e-3) / 1e12
+    peaks, src = measured_peaks()
+    if prec_name == "fp64":
+        peak = api.fp64_peak_tflops(device)
+        roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": traffic_from_profiles("expm_fp64"),
+                "kernel": f"k_expm_coop: Krylov exponential of a {topo.node_shape(node)[0]}x{topo.node_shape(node)[1]} node",
+                "peak_source": "FP64 FMA throughput measured in-run (MEASURED_PEAKS.json has no FP64 figure)",
+                "ms_per_launch": k_ms, "flops_per_launch": k_fl}
+    else:
+        peak = peaks["bf16_tflops"]
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": traffic_from_profiles("heff_mixed"),
+                "kernel": f"Krylov exponential of a {topo.node_shape(node)[0]}x{topo.node_shape(node)[1]} node",
+                "peak_source": f"bf16 dense, {src} (MEASURED_PEAKS.json)",
+                "ms_per_launch": k_ms, "flops_per_launch": k_fl}
+
     sz_trace = []
     for _ in range(args.warmup):
         tdvp(A, m.sop, -1j)
@@ -277,11 +320,14 @@ def run_ours(args):
     clocks = Clocks(device)
     l0 = api.launch_count()
     f0 = tdvp.flops()
+    nvtx = Nvtx()
     clocks.start()
+    nvtx.push("ttn_timed")
     tdvp.timer_start()
     for _ in range(args.steps):
         tdvp(A, m.sop, -1j)
     ms = tdvp.timer_stop()
+    nvtx.pop()
     clk = clocks.stop()
     launches = api.launch_count() - l0
     flops_step = (tdvp.flops() - f0) / args.steps
@@ -307,34 +353,13 @@ def run_ours(args):
     h2d = host.nbytes + (io1[0] - io0[0]) // args.steps
     d2h = host.nbytes + (io1[1] - io0[1]) // args.steps
 
-    # roofline of the dominant kernel: the persistent Krylov exponential on the largest
-    # node (it runs every H_eff contraction of the node update)
-    node = upper_node(topo)
-    k_ms, k_fl = tdvp.bench_node_op(A, node, 1, 5)
-    achieved = k_fl / (k_ms * 1e-3) / 1e12
-    peaks, src = measured_peaks()
-    if prec_name == "fp64":
-        peak = api.fp64_peak_tflops(device)
-        roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": traffic_from_profiles("expm_fp64"),
-                "kernel": f"k_expm_coop: Krylov exponential of a {topo.node_shape(node)[0]}x{topo.node_shape(node)[1]} node",
-                "peak_source": "FP64 FMA throughput measured in-run (MEASURED_PEAKS.json has no FP64 figure)",
-                "ms_per_launch": k_ms, "flops_per_launch": k_fl}
-    else:
-        peak = peaks["bf16_tflops"]
-        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": traffic_from_profiles("heff_mixed"),
-                "kernel": f"Krylov exponential of a {topo.node_shape(node)[0]}x{topo.node_shape(node)[1]} node",
-                "peak_source": f"bf16 dense, {src} (MEASURED_PEAKS.json)",
-                "ms_per_launch": k_ms, "flops_per_launch": k_fl}
-
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "c128" if prec_name == "fp64" else "c128 state, split bf16/tf32 contractions",
         "data": "synthetic (formula-generated spin-boson bath; std::mt19937 unoccupied SPFs)",
-        "config": workload_config(args.config, cfg, prec_name),
+        "config": workload_config(args.config, cfg, prec_name, over),
         "roofline": roof,
         "e2e": {"value": world * args.steps / e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},

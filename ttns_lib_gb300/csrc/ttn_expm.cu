@@ -563,6 +563,7 @@ __global__ void __launch_bounds__(ET) k_expm_coop(ExpmArgs a) {
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     if (a.napps_total) atomicAdd((unsigned long long*)a.napps_total, (unsigned long long)ctl->napps);
+    if (a.flops_total) atomicAdd(a.flops_total, a.flops_per_app * (double)ctl->napps);
     int e = ctl->err;
     if (!ctl->done) e |= 16;  // sub-step limit reached
     if (e) atomicOr(a.err, e << kKrylovErrShift);

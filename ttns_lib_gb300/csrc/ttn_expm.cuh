@@ -38,6 +38,8 @@ struct ExpmArgs {
   GridBarrier* bar;
   int* err;              // status word (Krylov error bits, barrier timeout)
   long long* napps_total;  // device counter of H applications (may be null)
+  double* flops_total;     // device counter of algorithmic matvec flops (may be null)
+  double flops_per_app;    // flops of one application of the program
   int m;
   double tau, cf_re, cf_im, tol;
 };

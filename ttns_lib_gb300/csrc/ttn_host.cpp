@@ -408,6 +408,7 @@ struct Integrator {
   DevBuf prog_buf, expm_part_buf;
   std::vector<int> heff_off, heff_n, kbond_off, kbond_n;
   long long* nh_dev = nullptr;
+  double* flops_dev = nullptr;   // matvec flops executed by the persistent kernels
   // host mirrors
   struct HostCtl { int done, err; long long napps; };
   HostCtl* hctl = nullptr;  // pinned
@@ -415,6 +416,7 @@ struct Integrator {
   cd coeff = cd(0.0, -1.0);
   long long nsteps = 0, nh = 0;
   double flops = 0.0;        // algorithmic flops enqueued (complex MAC = 8 flops)
+  double flops_seen = 0.0;   // device matvec flops already folded into `flops`
   long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device traffic issued by the step path
   // optional breakdown (TTN_PROFILE=1): synchronising wall time per operation kind and
   // node-size class; slows the sweep down, for analysis only
@@ -576,8 +578,9 @@ struct Integrator {
       bar = coop_buf.as<GridBarrier>();
       qr_scratch = (double*)(coop_buf.as<char>() + align256(sizeof(GridBarrier)));
       expm_max_grid = std::max(1, expm_coop_max_grid());
-      expm_part_buf.alloc(expm_partial_bytes(expm_max_grid) + 256);
+      expm_part_buf.alloc(expm_partial_bytes(expm_max_grid) + 512);
       nh_dev = (long long*)(expm_part_buf.as<char>() + expm_partial_bytes(expm_max_grid));
+      flops_dev = (double*)(expm_part_buf.as<char>() + expm_partial_bytes(expm_max_grid) + 256);
       CK(cudaMemset(expm_part_buf.p, 0, expm_part_buf.bytes));
       compile_programs();
     }
@@ -1002,7 +1005,7 @@ struct Integrator {
     return (int)g;
   }
   // persistent Krylov exponential of one node tensor (kind 0) or bond matrix (kind 1)
-  void expm_dev(int nd, int kind, double2* y, long long n, double tau, cd cf, bool count) {
+  void expm_dev(int nd, int kind, double2* y, long long n, double tau, cd cf, bool count, bool tally = true) {
     if (tau == 0.0) return;
     ExpmArgs a{};
     a.y = y; a.n = n; a.V = V; a.ldv = ldv; a.p = p; a.t1 = w1; a.t2 = w2; a.t3 = w3;
@@ -1011,15 +1014,19 @@ struct Integrator {
     a.part = expm_part_buf.as<double2>();
     a.ctl = ctl; a.bar = bar; a.err = status;
     a.napps_total = count ? nh_dev : nullptr;
+    a.flops_total = tally ? flops_dev : nullptr;
+    a.flops_per_app = (kind == 0) ? heff_flops(nd) : kbond_flops(nd);
     a.m = cfg.krylov_dim; a.tau = tau; a.cf_re = cf.real(); a.cf_im = cf.imag(); a.tol = cfg.krylov_tol;
     CK(expm_coop(a, expm_grid(n), stream));
-    // algorithmic flops of the Lanczos vector passes (one sub-step assumed; the
-    // matvec flops are counted by heff_flops at report time)
+    // Lanczos vector passes of one sub-step (the matvec flops are tallied on the device)
+    if (tally) flops += lanczos_vec_flops(n);
+  }
+  double lanczos_vec_flops(long long n) const {
     const int m = cfg.krylov_dim;
     double vec = 0.0;
     for (int j = 0; j < m; ++j) vec += (8.0 + 8.0 + 16.0 * (j + 1) + 4.0 + 2.0) * n;
     vec += (4.0 + 8.0 * (m + 1)) * n;
-    flops += vec;
+    return vec;
   }
 
   // ---------------------------------------------------------------- Krylov exponential
@@ -1194,12 +1201,16 @@ struct Integrator {
     check_finite(S->arena.as<double2>(), (long long)(S->arena.bytes / sizeof(double2)), status, kErrNonFinite, stream);
     int h = 0;
     long long napps = 0;
+    double mvf = 0.0;
     CK(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(&napps, nh_dev, sizeof(long long), cudaMemcpyDeviceToHost, stream));
-    d2h_bytes += sizeof(int) + sizeof(long long);
+    CK(cudaMemcpyAsync(&mvf, flops_dev, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    d2h_bytes += sizeof(int) + sizeof(long long) + sizeof(double);
     CK(cudaStreamSynchronize(stream));
     CK(cudaGetLastError());
     nh = napps;
+    flops += mvf - flops_seen;
+    flops_seen = mvf;
     CK(cudaMemsetAsync(status, 0, sizeof(int), stream));
     TTN_REQUIRE(!(h & kErrBarrierTimeout), TTN_ETIMEOUT, "a device-side grid barrier gave up waiting");
     TTN_REQUIRE(!(h >> kKrylovErrShift), TTN_ENUMERIC,
@@ -1646,13 +1657,13 @@ int ttn_bench_node_op(ttn_integrator* it, ttn_state* psi, int node, int kind, in
       case 0: I.heff(node, psi->node(node), I.p); break;
       case 1: {
         ttn::zcopy(I.w4, psi->node(node), n, I.stream);
-        I.expm_dev(node, 0, I.w4, n, I.dt > 0 ? I.dt / 2 : 0.01, ttn::cd(0.0, -1.0), false);
+        I.expm_dev(node, 0, I.w4, n, I.dt > 0 ? I.dt / 2 : 0.01, ttn::cd(0.0, -1.0), false, false);
         break;
       }
       case 3: {
         const long long rr = (long long)I.T.hrank[node] * I.T.hrank[node];
         ttn::zcopy(I.w4, I.rmat[node], rr, I.stream);
-        I.expm_dev(node, 1, I.w4, rr, I.dt > 0 ? -I.dt / 2 : -0.01, ttn::cd(0.0, -1.0), false);
+        I.expm_dev(node, 1, I.w4, rr, I.dt > 0 ? -I.dt / 2 : -0.01, ttn::cd(0.0, -1.0), false, false);
         break;
       }
       case 2: {
@@ -1682,7 +1693,8 @@ int ttn_bench_node_op(ttn_integrator* it, ttn_state* psi, int node, int kind, in
     int subs = 0;
     CK(cudaMemcpy(&k, &I.ctl->napps, sizeof(long long), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&subs, &I.ctl->substeps, sizeof(int), cudaMemcpyDeviceToHost));
-    fl = fl * (subs > 0 ? subs : 1) + (double)k * (kind == 1 ? I.heff_flops(node) : I.kbond_flops(node));
+    const long long nn = (kind == 1) ? n : (long long)I.T.hrank[node] * I.T.hrank[node];
+    fl = I.lanczos_vec_flops(nn) * (subs > 0 ? subs : 1) + (double)k * (kind == 1 ? I.heff_flops(node) : I.kbond_flops(node));
   }
   if (ms_per_rep) *ms_per_rep = ms / reps;
   if (flops_per_rep) *flops_per_rep = fl;
@@ -1765,7 +1777,7 @@ int ttn_debug_expm_node(ttn_integrator* it, int node, double tau, double cre, do
   CK(cudaMemcpyAsync(I.w4, v, n * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
   // w4 is a gauge scratch; the exponential itself uses V, p, w1-w3
   long long k = 0;
-  I.expm_dev(node, 0, I.w4, n, tau, ttn::cd(cre, cim), false);
+  I.expm_dev(node, 0, I.w4, n, tau, ttn::cd(cre, cim), false, false);
   CK(cudaMemcpyAsync(v, I.w4, n * sizeof(double2), cudaMemcpyDeviceToHost, I.stream));
   CK(cudaMemcpyAsync(&k, &I.ctl->napps, sizeof(long long), cudaMemcpyDeviceToHost, I.stream));
   CK(cudaStreamSynchronize(I.stream));

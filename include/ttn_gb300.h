@@ -137,6 +137,10 @@ int ttn_norm2(ttn_integrator* it, ttn_state* psi, double* out);
 int ttn_debug_refresh_env(ttn_integrator* it, ttn_state* psi);
 /* out = H_eff(node) v with the current environments; v, out are host buffers */
 int ttn_debug_heff(ttn_integrator* it, int node, const double* v, double* out);
+/* out = the compiled matrix-vector program of a node (kind 0: H_eff, kind 1: bond
+ * Hamiltonian on the node's R matrix) applied once by the persistent kernel, in the
+ * integrator's precision */
+int ttn_debug_program_apply(ttn_integrator* it, int node, int kind, const double* v, double* out);
 /* v <- exp(coeff * tau * H_eff(node)) v; returns the number of H applications */
 int ttn_debug_expm_node(ttn_integrator* it, int node, double tau, double cre, double cim,
                         double* v, long long* napps);
@@ -164,6 +168,9 @@ int ttn_host_free(void* p);
 int ttn_launch_count(unsigned long long* out);
 /* FP64 FMA throughput of a device in TFLOP/s (long independent FMA chains) */
 int ttn_device_fp64_peak(int device, double* tflops);
+/* tensor-core check: D (128 x N) = A (128 x K) B^T with B stored N x K, real fp64 in and out,
+ * computed with split-TF32 tcgen05 MMAs and FP32 accumulation */
+int ttn_debug_tc_gemm(const double* A, const double* B, double* D, int K, int N, int device);
 /* Householder QR of an m x n row-major matrix on the device: a <- Q, r <- R */
 int ttn_debug_qr(int m, int n, double* a, double* r, int device);
 

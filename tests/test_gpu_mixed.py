@@ -1,0 +1,101 @@
+"""Mixed precision (split-TF32 tcgen05 contractions) against the oracle and the FP64 path.
+
+The mixed form runs the rank-64 mode and mean-field contractions of the Krylov matvec
+on the tensor cores with operands split into two TF32 parts and FP32 accumulation
+(relative error per contraction about 1e-7); everything else stays FP64.  Tolerances:
+one H_eff application within 5e-6 relative of the oracle, one node exponential within
+2e-5, and <sigma_z> after several sweeps within 1e-6 absolute of the FP64 device path,
+the accuracy bar the mixed form is measured at.
+"""
+import numpy as np
+import pytest
+
+from helpers import generic_state
+from oracle.oracle import Oracle
+from ttns_lib_gb300 import api
+from ttns_lib_gb300 import spin_boson as sb
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def rank64_tree():
+    # thermofield spin-boson, 2 x 8 bath modes of dimension 16, bonds of 64: the
+    # headline workload's node shapes (16 x 16 x 64 and 64 x 64 x 64) on a small tree
+    return sb.build_config("c3", N=8)
+
+
+def integrators(topo, sop, state, m):
+    out = {}
+    for name, prec in (("fp64", api.PREC_FP64), ("mixed", api.PREC_MIXED)):
+        A = api.httensor(topo)
+        A.set(state)
+        out[name] = (A, api.fixed_step_projector_splitting_integrator(A, sop, krylov_dim=m, krylov_tolerance=1e-12,
+                                                                     precision=prec))
+    return out
+
+
+def test_mixed_program_apply_matches_oracle():
+    m, cfg = rank64_tree()
+    topo = m.topology
+    st = generic_state(topo, np.random.default_rng(11))
+    orc = Oracle(topo, m.sop, krylov_dim=cfg["krylov_dim"])
+    orc.set_state(st)
+    orc.refresh_env()
+    its = integrators(topo, m.sop, st, cfg["krylov_dim"])
+    for A, it in its.values():
+        it.refresh_env(A)
+    rng = np.random.default_rng(12)
+    n_tc = 0
+    for node in range(topo.nnodes):
+        v = rng.normal(size=topo.node_shape(node)) + 1j * rng.normal(size=topo.node_shape(node))
+        ref = orc.heff(node, v)
+        y64 = its["fp64"][1].program_apply(node, v)
+        ymx = its["mixed"][1].program_apply(node, v)
+        assert rel(y64, ref) < 1e-12, node
+        e = rel(ymx, ref)
+        assert e < 5e-6, (node, e)
+        if e > 1e-11:
+            n_tc += 1
+    # every interior node of bond dimension 64 ran contractions on the tensor cores
+    rank64 = sum(1 for i in range(topo.nnodes) if not topo.is_leaf(i) and topo.hrank[i] == 64)
+    assert rank64 > 0 and n_tc >= rank64
+
+
+def test_mixed_expm_node_matches_oracle():
+    m, cfg = rank64_tree()
+    topo = m.topology
+    st = generic_state(topo, np.random.default_rng(13))
+    orc = Oracle(topo, m.sop, krylov_dim=cfg["krylov_dim"])
+    orc.set_state(st)
+    orc.refresh_env()
+    its = integrators(topo, m.sop, st, cfg["krylov_dim"])
+    A, it = its["mixed"]
+    it.refresh_env(A)
+    for node in range(2, topo.nnodes, 3):
+        yo, _ = orc.expm_node(node, st[node], cfg["dt"])
+        yd, _ = it.expm_node(node, st[node], cfg["dt"])
+        assert rel(yd, yo) < 2e-5, node
+
+
+def test_mixed_sweeps_track_fp64():
+    m, cfg = rank64_tree()
+    topo = m.topology
+    st = generic_state(topo, np.random.default_rng(14))
+    its = integrators(topo, m.sop, st, cfg["krylov_dim"])
+    worst = 0.0
+    for A, it in its.values():
+        it.dt = cfg["dt"]
+    for k in range(6):
+        sz = {}
+        for name, (A, it) in its.items():
+            it(A, m.sop, -1j)
+            sz[name] = it.mel()(sb.SZ, 0, A).real
+        worst = max(worst, abs(sz["mixed"] - sz["fp64"]))
+    assert worst <= 1e-6, worst
+    A, it = its["mixed"]
+    assert abs(it.mel()(A) - 1.0) < 1e-6

@@ -94,9 +94,11 @@ SIGNATURES = {
     "ttn_debug_refresh_env": (_I, [_P, _P]),
     "ttn_debug_heff": (_I, [_P, _I, _DP, _DP]),
     "ttn_debug_expm_node": (_I, [_P, _I, _D, _D, _D, _DP, _LLP]),
+    "ttn_debug_program_apply": (_I, [_P, _I, _I, _DP, _DP]),
     "ttn_debug_num_groups": (_I, [_P, _I, _IP]),
     "ttn_debug_get_env": (_I, [_P, _I, _I, _I, _DP]),
     "ttn_debug_qr": (_I, [_I, _I, _DP, _DP, _I]),
+    "ttn_debug_tc_gemm": (_I, [_DP, _DP, _DP, _I, _I, _I]),
 }
 
 _lib = None
@@ -353,6 +355,13 @@ class fixed_step_projector_splitting_integrator:
         _check(lib().ttn_debug_heff(self.h, node, _dp(x.view(np.float64)), _dp(y.view(np.float64))))
         return y.reshape(self.topo.node_shape(node))
 
+    def program_apply(self, node: int, v: np.ndarray, kind: int = 0) -> np.ndarray:
+        """The node's compiled matvec program (kind 0 H_eff, 1 bond) applied once."""
+        x = _cplx(v).ravel()
+        y = np.zeros_like(x)
+        _check(lib().ttn_debug_program_apply(self.h, node, kind, _dp(x.view(np.float64)), _dp(y.view(np.float64))))
+        return y.reshape(v.shape)
+
     def expm_node(self, node: int, v: np.ndarray, tau: float, coeff: complex = -1j):
         x = _cplx(v).ravel().copy()
         n = C.c_longlong()
@@ -382,6 +391,16 @@ def fp64_peak_tflops(device: int = 0) -> float:
     out = C.c_double()
     _check(lib().ttn_device_fp64_peak(device, C.byref(out)))
     return out.value
+
+
+def device_tc_gemm(a: np.ndarray, b: np.ndarray, device: int = 0) -> np.ndarray:
+    """D = A B^T on the tensor cores (A 128 x K, B N x K, real)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    assert a.shape[0] == 128 and a.shape[1] == b.shape[1]
+    d = np.zeros((128, b.shape[0]), dtype=np.float64)
+    _check(lib().ttn_debug_tc_gemm(_dp(a), _dp(b), _dp(d), a.shape[1], b.shape[0], device))
+    return d
 
 
 def device_qr(a: np.ndarray, device: int = 0):

@@ -9,6 +9,7 @@
 #include "ttn_expm.cuh"
 #include "ttn_coop.cuh"
 #include "ttn_kernels.cuh"
+#include "ttn_tc_core.cuh"
 
 #include <cmath>
 
@@ -103,11 +104,167 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
   }
 }
 
-__device__ void run_program(const ExpmArgs& a, const double2* x) {
+// ---- tensor-core contractions (mixed precision).  Per tile D(128 x 64) = A(128 x 128) B(64 x 128)^T
+// in split TF32 with two FP32 accumulators in TMEM (hi*hi and hi*lo + lo*hi).
+struct TcState {
+  uint32_t tmem;      // TMEM base (128 columns)
+  uint32_t phase;     // mbarrier parity
+  uint64_t* mbar;
+  uint32_t* a_hi;     // 128 x 128 tf32
+  uint32_t* a_lo;
+  uint32_t* b_hi;     // 64 x 128 tf32
+  uint32_t* b_lo;
+};
+constexpr int TC_A_WORDS = 128 * 128, TC_B_WORDS = 64 * 128;
+constexpr size_t TC_SMEM = (size_t)(2 * TC_A_WORDS + 2 * TC_B_WORDS) * 4;
+
+__device__ __forceinline__ void put_a(TcState& t, int row, int k, double v) {
+  uint32_t h, l;
+  tc::split_tf32(v, h, l);
+  const uint32_t o = tc::tf32_offset(row, k, 128) / 4;
+  t.a_hi[o] = h;
+  t.a_lo[o] = l;
+}
+__device__ __forceinline__ void put_b(TcState& t, int row, int k, double v) {
+  uint32_t h, l;
+  tc::split_tf32(v, h, l);
+  const uint32_t o = tc::tf32_offset(row, k, 64) / 4;
+  t.b_hi[o] = h;
+  t.b_lo[o] = l;
+}
+
+// issue the 48 MMAs of one tile, wait for them; returns false on a timed-out wait
+__device__ bool tc_tile_mma(TcState& t) {
+  tc::fence_proxy_async();
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  if (threadIdx.x == 0) {
+    const uint32_t idesc = tc::idesc_tf32(128, 64);
+    const uint32_t lboA = 16 * 128, lboB = 8 * 128, sbo = 128;
+    for (int kk = 0; kk < 16; ++kk) {
+      const uint32_t offA = (uint32_t)kk * 2 * 16 * 128, offB = (uint32_t)kk * 2 * 8 * 128;
+      const uint64_t ah = tc::smem_desc(tc::smem_u32(t.a_hi) + offA, lboA, sbo);
+      const uint64_t al = tc::smem_desc(tc::smem_u32(t.a_lo) + offA, lboA, sbo);
+      const uint64_t bh = tc::smem_desc(tc::smem_u32(t.b_hi) + offB, lboB, sbo);
+      const uint64_t bl = tc::smem_desc(tc::smem_u32(t.b_lo) + offB, lboB, sbo);
+      tc::mma_tf32(t.tmem, ah, bh, idesc, kk > 0);
+      tc::mma_tf32(t.tmem + 64, ah, bl, idesc, kk > 0);
+      tc::mma_tf32(t.tmem + 64, al, bh, idesc, 1);
+    }
+    tc::mma_commit(t.mbar);
+  }
+  __syncwarp();
+  const bool ok = tc::mbar_wait(t.mbar, t.phase);
+  t.phase ^= 1u;
+  tc::fence_after();
+  return ok;
+}
+
+// this thread's row (warps 0-3: rows 0..127) of the tile result, 16 columns starting at c0
+__device__ __forceinline__ void tc_tile_row16(const TcState& t, int c0, double* v) {
+  const int warp = threadIdx.x >> 5;
+  float mv[16], cv[16];
+  tc::tmem_ld16(t.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, mv);
+  tc::tmem_ld16(t.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(64 + c0), cv);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = (double)mv[i] + (double)cv[i];
+}
+
+__device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, TcState& t) {
+  const double2* in = buf_of(a, op.in, x);
+  double2* out = buf_of(a, op.out, x);
+  const int warp = threadIdx.x >> 5;
+  const bool acc = (op.beta != 0);
+  if (op.kind == MV_MODE) {
+    // out(aa, i, b) = sum_j (alpha S)(i, j) in(aa, j, b); tiles of 64 columns b
+    const long long nb = op.nb, tiles = op.na * (nb / 64);
+    if ((long long)blockIdx.x >= tiles) return;
+    // A = real block form of alpha*S, loaded once per op by every CTA that has a tile
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+      const int i = e / 64, j = e % 64;
+      const double2 sv = cmul(op.alpha, op.mat[e]);
+      put_a(t, i, j, sv.x);
+      put_a(t, i, 64 + j, -sv.y);
+      put_a(t, 64 + i, j, sv.y);
+      put_a(t, 64 + i, 64 + j, sv.x);
+    }
+    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+      const long long aa = tile / (nb / 64), b0 = (tile % (nb / 64)) * 64;
+      const double2* src = in + aa * 64 * nb + b0;
+      for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+        const int j = e / 64, n = e % 64;  // consecutive threads read consecutive b
+        const double2 v = src[(long long)j * nb + n];
+        put_b(t, n, j, v.x);
+        put_b(t, n, 64 + j, v.y);
+      }
+      if (!tc_tile_mma(t) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
+      if (warp < 4) {
+        const int row = threadIdx.x;  // 0..127: rows < 64 real parts, >= 64 imaginary parts
+        const int i = row & 63;
+        double* dst = (double*)(out + aa * 64 * nb + (long long)i * nb + b0) + (row >> 6);
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+          double v[16];
+          tc_tile_row16(t, c0, v);
+#pragma unroll
+          for (int n = 0; n < 16; ++n) dst[2 * (c0 + n)] = acc ? dst[2 * (c0 + n)] + v[n] : v[n];
+        }
+      }
+      tc::fence_before();
+      __syncthreads();
+    }
+  } else {
+    // MF: out(x, k) = sum_l in(x, l) (alpha M)(k, l); tiles of 128 rows x, two column halves
+    const long long nx = op.na, tiles = (nx / 128) * 2;
+    if ((long long)blockIdx.x >= tiles) return;
+    int loaded_half = -1;
+    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+      const long long xb = tile / 2;
+      const int half = (int)(tile % 2);
+      if (half != loaded_half) {
+        for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+          const int k = e / 64, l = e % 64;
+          const double2 mv = cmul(op.alpha, op.mat[e]);
+          if (half == 0) {
+            put_b(t, k, l, mv.x);
+            put_b(t, k, 64 + l, -mv.y);
+          } else {
+            put_b(t, k, l, mv.y);
+            put_b(t, k, 64 + l, mv.x);
+          }
+        }
+        loaded_half = half;
+      }
+      const double2* src = in + xb * 128 * 64;
+      for (int e = threadIdx.x; e < 128 * 64; e += blockDim.x) {
+        const int r = e / 64, l = e % 64;
+        const double2 v = src[e];
+        put_a(t, r, l, v.x);
+        put_a(t, r, 64 + l, v.y);
+      }
+      if (!tc_tile_mma(t) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
+      if (warp < 4) {
+        const int row = threadIdx.x;
+        double* dst = (double*)(out + (xb * 128 + row) * 64) + half;
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+          double v[16];
+          tc_tile_row16(t, c0, v);
+#pragma unroll
+          for (int k = 0; k < 16; ++k) dst[2 * (c0 + k)] = acc ? dst[2 * (c0 + k)] + v[k] : v[k];
+        }
+      }
+      tc::fence_before();
+      __syncthreads();
+    }
+  }
+}
+
+__device__ void run_program(const ExpmArgs& a, const double2* x, TcState* t) {
   for (int k = 0; k < a.nops; ++k) {
     const MvOp& op = a.prog[k];
     if (op.barrier_before) grid_barrier(a.bar, a.err);
-    run_op(a, op, x);
+    if (op.tc && t) run_op_tc(a, op, x, *t);
+    else run_op(a, op, x);
   }
 }
 
@@ -387,11 +544,33 @@ __device__ void control(const ExpmArgs& a, CtlSmem& S) {
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(ET) k_expm_coop(ExpmArgs a) {
+__global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
   __shared__ Red sm;
   __shared__ double2 red[EQ];
-  __shared__ CtlSmem cs;
   __shared__ int s_done;
+  __shared__ __align__(8) uint64_t s_mbar;
+  __shared__ uint32_t s_tmem;
+  extern __shared__ __align__(1024) unsigned char dsm[];
+  // the controller's scratch and the tensor-core operands share the dynamic buffer: they
+  // are used in different phases
+  CtlSmem& cs = *reinterpret_cast<CtlSmem*>(dsm);
+  TcState tcs;
+  TcState* tcp = nullptr;
+  if (a.mixed) {
+    if (threadIdx.x == 0) tc::mbar_init(&s_mbar, 1);
+    if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&s_tmem, 128);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    tcs.tmem = s_tmem;
+    tcs.phase = 0;
+    tcs.mbar = &s_mbar;
+    tcs.a_hi = reinterpret_cast<uint32_t*>(dsm);
+    tcs.a_lo = tcs.a_hi + TC_A_WORDS;
+    tcs.b_hi = tcs.a_lo + TC_A_WORDS;
+    tcs.b_lo = tcs.b_hi + TC_B_WORDS;
+    tcp = &tcs;
+  }
   KrylovCtl* ctl = a.ctl;
   const long long n = a.n;
   const long long nthreads = (long long)gridDim.x * blockDim.x;
@@ -416,7 +595,12 @@ __global__ void __launch_bounds__(ET) k_expm_coop(ExpmArgs a) {
     ctl->napps = 0;
     for (int q = 0; q < 73; ++q) ctl->bet[q] = 0.0;
   }
-  for (int sub = 0; sub < 100000; ++sub) {
+  if (a.apply_only) {
+    grid_barrier(a.bar, a.err);
+    run_program(a, a.y, tcp);
+    grid_barrier(a.bar, a.err);
+  }
+  for (int sub = 0; sub < (a.apply_only ? 0 : 100000); ++sub) {
     grid_barrier(a.bar, a.err);
     if (threadIdx.x == 0) s_done = *(volatile int*)&ctl->done;
     __syncthreads();
@@ -452,7 +636,7 @@ __global__ void __launch_bounds__(ET) k_expm_coop(ExpmArgs a) {
     for (int j = 0; j < m; ++j) {
       const double2* Vj = a.V + (long long)j * a.ldv;
       grid_barrier(a.bar, a.err);
-      run_program(a, Vj);
+      run_program(a, Vj, tcp);
       // partial <V_j, p> over my elements (same element ownership as the last writes of p)
       {
         double2 s = make_double2(0.0, 0.0);
@@ -529,7 +713,7 @@ __global__ void __launch_bounds__(ET) k_expm_coop(ExpmArgs a) {
     }
     // ---- ||H V_m|| for the error estimate
     grid_barrier(a.bar, a.err);
-    run_program(a, a.V + (long long)m * a.ldv);
+    run_program(a, a.V + (long long)m * a.ldv, tcp);
     {
       double s = 0.0;
       for (long long i = tid; i < n; i += nthreads) {
@@ -561,7 +745,15 @@ __global__ void __launch_bounds__(ET) k_expm_coop(ExpmArgs a) {
       __syncthreads();
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (a.mixed) {
+    tc::fence_before();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) {
+      tc::fence_after();
+      tc::tmem_dealloc(tcs.tmem, 128);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && !a.apply_only) {
     if (a.napps_total) atomicAdd((unsigned long long*)a.napps_total, (unsigned long long)ctl->napps);
     if (a.flops_total) atomicAdd(a.flops_total, a.flops_per_app * (double)ctl->napps);
     int e = ctl->err;
@@ -571,11 +763,14 @@ __global__ void __launch_bounds__(ET) k_expm_coop(ExpmArgs a) {
 }
 }  // namespace
 
-int expm_coop_max_grid() {
+static size_t dyn_smem(int mixed) { return mixed ? (TC_SMEM > sizeof(CtlSmem) ? TC_SMEM : sizeof(CtlSmem)) : sizeof(CtlSmem); }
+
+int expm_coop_max_grid(int mixed) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expm_coop, ET, 0);
+  cudaFuncSetAttribute(k_expm_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem(1));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expm_coop, ET, dyn_smem(mixed));
   return sms * (per < 1 ? 1 : per);
 }
 
@@ -585,7 +780,7 @@ cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s) {
   ExpmArgs b = a;
   void* args[] = {&b};
   ++g_launches;
-  return cudaLaunchCooperativeKernel((const void*)k_expm_coop, dim3(grid), dim3(ET), args, 0, s);
+  return cudaLaunchCooperativeKernel((const void*)k_expm_coop, dim3(grid), dim3(ET), args, dyn_smem(a.mixed), s);
 }
 
 }  // namespace ttn

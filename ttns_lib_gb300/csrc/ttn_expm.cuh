@@ -22,6 +22,7 @@ struct MvOp {
   long long na, nb;
   int d;
   int beta;  // 1: accumulate into out
+  int tc;    // 1: run on the tensor cores (mixed precision; MODE with d = 64, MF with r = 64)
   double2 alpha;
 };
 
@@ -42,10 +43,19 @@ struct ExpmArgs {
   double flops_per_app;    // flops of one application of the program
   int m;
   double tau, cf_re, cf_im, tol;
+  int mixed;             // 1: the program contains tensor-core contractions (TMEM + big smem)
+  int apply_only;        // 1: apply the program once to y (result in p) and return
 };
 
-int expm_coop_max_grid();
+// co-resident CTAs for the plain (mixed = 0) or tensor-core (mixed = 1) configuration
+int expm_coop_max_grid(int mixed);
 size_t expm_partial_bytes(int max_grid);
 cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s);
+// whether a contraction can run on the tensor cores
+inline bool tc_eligible(int kind, int d, long long na, long long nb) {
+  if (kind == MV_MODE) return d == 64 && nb % 64 == 0;
+  if (kind == MV_MF) return d == 64 && na % 128 == 0;
+  return false;
+}
 
 }  // namespace ttn

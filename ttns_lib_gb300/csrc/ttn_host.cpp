@@ -403,7 +403,9 @@ struct Integrator {
   DevBuf coop_buf;
   GridBarrier* bar = nullptr;
   double* qr_scratch = nullptr;
-  int num_sms = 0, qr_max_grid = 1, expm_max_grid = 1;
+  int num_sms = 0, qr_max_grid = 1, expm_max_grid = 1, expm_max_grid_tc = 1;
+  bool mixed = false;                      // tensor-core contractions in the matvec programs
+  std::vector<char> heff_tc, kbond_tc;     // program contains tensor-core contractions
   // compiled matrix-vector programs for the persistent Krylov kernel
   DevBuf prog_buf, expm_part_buf;
   std::vector<int> heff_off, heff_n, kbond_off, kbond_n;
@@ -577,22 +579,22 @@ struct Integrator {
       CK(cudaMemset(coop_buf.p, 0, coop_buf.bytes));
       bar = coop_buf.as<GridBarrier>();
       qr_scratch = (double*)(coop_buf.as<char>() + align256(sizeof(GridBarrier)));
-      expm_max_grid = std::max(1, expm_coop_max_grid());
+      mixed = (cfg.precision == TTN_PREC_MIXED);
+      expm_max_grid = std::max(1, expm_coop_max_grid(0));
+      expm_max_grid_tc = std::max(1, expm_coop_max_grid(1));
+      if (mixed) {
+        // the tensor-core contractions need sm_100-family tensor memory
+        cudaDeviceProp prop{};
+        CK(cudaGetDeviceProperties(&prop, device));
+        TTN_REQUIRE(prop.major >= 10, TTN_ENOTSUP, "mixed precision needs a tcgen05 device (sm_100 family)");
+      }
       expm_part_buf.alloc(expm_partial_bytes(expm_max_grid) + 512);
       nh_dev = (long long*)(expm_part_buf.as<char>() + expm_partial_bytes(expm_max_grid));
       flops_dev = (double*)(expm_part_buf.as<char>() + expm_partial_bytes(expm_max_grid) + 256);
       CK(cudaMemset(expm_part_buf.p, 0, expm_part_buf.bytes));
       compile_programs();
     }
-    if (cfg.precision == TTN_PREC_MIXED) {
-      try {
-        tc = tc_create(device, maxsize, stream);
-      } catch (const Err&) {
-        throw;
-      } catch (const std::exception& e) {
-        throw Err(TTN_ENOTSUP, e.what());
-      }
-    }
+
     CK(cudaStreamSynchronize(stream));
   }
 
@@ -888,16 +890,25 @@ struct Integrator {
   }
 
   // ---------------------------------------------------------------- matvec programs
+  // Barriers go where one contraction reads a buffer another wrote (or overwrites one
+  // another read) since the last barrier.  The element-wise FP64 contractions give output
+  // element e to the same thread whatever the shape, so two of them may accumulate into
+  // one buffer back to back; a tensor-core contraction distributes its output by tiles,
+  // so an accumulation that involves one is a hazard too.
   struct ProgBuilder {
+    bool mixed = false;
     std::vector<MvOp> ops;
-    unsigned dirty = 0, read = 0;
+    unsigned dirty = 0, read = 0, dirty_tc = 0;
     void emit(MvOp op) {
+      op.tc = (mixed && tc_eligible(op.kind, op.d, op.na, op.nb)) ? 1 : 0;
       const unsigned in_bit = (op.kind == MV_ZERO) ? 0u : (1u << op.in);
       const unsigned out_bit = 1u << op.out;
-      op.barrier_before = ((in_bit & dirty) || (out_bit & read)) ? 1 : 0;
-      if (op.barrier_before) { dirty = 0; read = 0; }
+      const bool waw = (out_bit & dirty) && (op.tc || (out_bit & dirty_tc));
+      op.barrier_before = ((in_bit & dirty) || (out_bit & read) || waw) ? 1 : 0;
+      if (op.barrier_before) { dirty = 0; read = 0; dirty_tc = 0; }
       dirty |= out_bit;
       read |= in_bit;
+      if (op.tc) dirty_tc |= out_bit;
       ops.push_back(op);
     }
   };
@@ -925,6 +936,7 @@ struct Integrator {
   }
   std::vector<MvOp> heff_program(int nd) {
     ProgBuilder B;
+    B.mixed = mixed;
     const long long sz = T.size(nd);
     const int r = T.hrank[nd];
     bool first = true;
@@ -969,6 +981,7 @@ struct Integrator {
   }
   std::vector<MvOp> kbond_program(int nd) {
     ProgBuilder B;
+    B.mixed = mixed;
     const int r = T.hrank[nd];
     bool first = true;
     for (auto& g : G[nd]) {
@@ -987,26 +1000,36 @@ struct Integrator {
   void compile_programs() {
     std::vector<MvOp> all;
     heff_off.assign(T.n, 0); heff_n.assign(T.n, 0); kbond_off.assign(T.n, 0); kbond_n.assign(T.n, 0);
+    heff_tc.assign(T.n, 0); kbond_tc.assign(T.n, 0);
+    auto mark = [&](const std::vector<MvOp>& ops) {
+      bool any = false;
+      for (const auto& o : ops) any = any || o.tc;
+      return any;
+    };
     for (int i = 0; i < T.n; ++i) {
       auto h = heff_program(i);
+      heff_tc[i] = mark(h);
       heff_off[i] = (int)all.size(); heff_n[i] = (int)h.size();
       all.insert(all.end(), h.begin(), h.end());
       auto k = kbond_program(i);
+      kbond_tc[i] = mark(k);
       kbond_off[i] = (int)all.size(); kbond_n[i] = (int)k.size();
       all.insert(all.end(), k.begin(), k.end());
     }
     prog_buf.alloc(all.size() * sizeof(MvOp) + 16);
     CK(cudaMemcpy(prog_buf.p, all.data(), all.size() * sizeof(MvOp), cudaMemcpyHostToDevice));
   }
-  int expm_grid(long long n) const {
+  int expm_grid(long long n, bool tc) const {
     long long g = (n + 63) / 64;
     if (g < 1) g = 1;
-    if (g > expm_max_grid) g = expm_max_grid;
+    const int mx = tc ? expm_max_grid_tc : expm_max_grid;
+    if (g > mx) g = mx;
     return (int)g;
   }
   // persistent Krylov exponential of one node tensor (kind 0) or bond matrix (kind 1)
-  void expm_dev(int nd, int kind, double2* y, long long n, double tau, cd cf, bool count, bool tally = true) {
-    if (tau == 0.0) return;
+  void expm_dev(int nd, int kind, double2* y, long long n, double tau, cd cf, bool count, bool tally = true,
+                bool apply_only = false) {
+    if (tau == 0.0 && !apply_only) return;
     ExpmArgs a{};
     a.y = y; a.n = n; a.V = V; a.ldv = ldv; a.p = p; a.t1 = w1; a.t2 = w2; a.t3 = w3;
     a.prog = prog_buf.as<MvOp>() + (kind == 0 ? heff_off[nd] : kbond_off[nd]);
@@ -1017,7 +1040,9 @@ struct Integrator {
     a.flops_total = tally ? flops_dev : nullptr;
     a.flops_per_app = (kind == 0) ? heff_flops(nd) : kbond_flops(nd);
     a.m = cfg.krylov_dim; a.tau = tau; a.cf_re = cf.real(); a.cf_im = cf.imag(); a.tol = cfg.krylov_tol;
-    CK(expm_coop(a, expm_grid(n), stream));
+    a.mixed = (kind == 0 ? heff_tc[nd] : kbond_tc[nd]) ? 1 : 0;
+    a.apply_only = apply_only ? 1 : 0;
+    CK(expm_coop(a, expm_grid(n, a.mixed), stream));
     // Lanczos vector passes of one sub-step (the matvec flops are tallied on the device)
     if (tally) flops += lanczos_vec_flops(n);
   }
@@ -1788,6 +1813,23 @@ int ttn_debug_expm_node(ttn_integrator* it, int node, double tau, double cre, do
   if (napps) *napps = (tau == 0.0) ? 0 : k;
   TTN_API_END
 }
+int ttn_debug_program_apply(ttn_integrator* it, int node, int kind, const double* v, double* out) {
+  TTN_API_BEGIN
+  auto& I = it->I;
+  TTN_REQUIRE(node >= 0 && node < I.T.n && v && out && (kind == 0 || kind == 1), TTN_EINVAL, "bad argument");
+  CK(cudaSetDevice(I.device));
+  const long long n = kind == 0 ? I.T.size(node) : (long long)I.T.hrank[node] * I.T.hrank[node];
+  CK(cudaMemcpyAsync(I.w4, v, n * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  I.expm_dev(node, kind, I.w4, n, 0.0, ttn::cd(0.0, -1.0), false, false, true);
+  CK(cudaMemcpyAsync(out, I.p, n * sizeof(double2), cudaMemcpyDeviceToHost, I.stream));
+  CK(cudaStreamSynchronize(I.stream));
+  CK(cudaGetLastError());
+  int h = 0;
+  CK(cudaMemcpy(&h, I.status, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemset(I.status, 0, sizeof(int)));
+  TTN_REQUIRE(h == 0, TTN_ETIMEOUT, "program application reported a device-side wait failure");
+  TTN_API_END
+}
 int ttn_debug_num_groups(ttn_integrator* it, int node, int* out) {
   TTN_API_BEGIN
   TTN_REQUIRE(it && out && node >= 0 && node < it->I.T.n, TTN_EINVAL, "bad argument");
@@ -1804,6 +1846,30 @@ int ttn_debug_get_env(ttn_integrator* it, int node, int group, int which, double
   const int r = I.T.hrank[node];
   CK(cudaMemcpyAsync(out, p, (size_t)r * r * sizeof(double2), cudaMemcpyDeviceToHost, I.stream));
   CK(cudaStreamSynchronize(I.stream));
+  TTN_API_END
+}
+int ttn_debug_tc_gemm(const double* A, const double* B, double* D, int K, int N, int device) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(A && B && D, TTN_EINVAL, "null argument");
+  TTN_REQUIRE(K >= 8 && K % 8 == 0 && N >= 16 && N <= 256 && N % 16 == 0, TTN_EINVAL, "bad tensor-core test shape");
+  TTN_REQUIRE((size_t)2 * (128 + N) * K * 4 <= 196608, TTN_EINVAL, "operands do not fit in shared memory");
+  CK(cudaSetDevice(device));
+  ttn::DevBuf buf;
+  size_t na = (size_t)128 * K, nb = (size_t)N * K, nd = (size_t)128 * N;
+  buf.alloc((na + nb + nd) * sizeof(double) + 256);
+  double* dA = buf.as<double>();
+  double* dB = dA + na;
+  double* dD = dB + nb;
+  int* derr = (int*)(dD + nd);
+  CK(cudaMemcpy(dA, A, na * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dB, B, nb * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemset(derr, 0, sizeof(int)));
+  CK(ttn::tc_gemm_test(dA, dB, dD, K, N, derr, 0));
+  CK(cudaDeviceSynchronize());
+  int herr = 0;
+  CK(cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost));
+  TTN_REQUIRE(herr == 0, TTN_ETIMEOUT, "tensor-core test: MMA completion wait gave up");
+  CK(cudaMemcpy(D, dD, nd * sizeof(double), cudaMemcpyDeviceToHost));
   TTN_API_END
 }
 int ttn_debug_qr(int m, int n, double* a, double* r, int device) {

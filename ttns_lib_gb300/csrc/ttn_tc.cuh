@@ -21,4 +21,9 @@ bool tc_adj_mul(TcEngine* e, const double2* A, const double2* X, long long nx, i
 bool tc_mode_contract(TcEngine* e, const double2* A, const double2* T, long long na, int d, long long nb, double2* out,
                       double2 alpha, bool acc, cudaStream_t s);
 
+// One-CTA check of the tcgen05 path: D (128 x N) = A (128 x K) * B (N x K)^T, fp64 in/out,
+// split-TF32 products with FP32 accumulation.  N in {16, 32, ..., 256}, K a multiple of 8,
+// 2*(128+N)*K*4 bytes of operands must fit in shared memory.
+cudaError_t tc_gemm_test(const double* A, const double* B, double* D, int K, int N, int* err, cudaStream_t s);
+
 }  // namespace ttn

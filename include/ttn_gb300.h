@@ -174,6 +174,21 @@ int ttn_debug_tc_gemm(const double* A, const double* B, double* D, int K, int N,
 /* Householder QR of an m x n row-major matrix on the device: a <- Q, r <- R */
 int ttn_debug_qr(int m, int n, double* a, double* r, int device);
 
+/* No counterpart in the reference: it is the one entry point that allocates no device
+ * memory, for callers that cannot allocate where they factorise (all their device memory
+ * comes from their own pool or arena, or a cudaMalloc/cudaFree device synchronisation
+ * is not affordable).  Householder QR (LAPACK zgeqrf/zungqr conventions, the same
+ * cooperative kernel as the sweep's gauge moves) of an m x n row-major complex matrix
+ * already on `device`: a <- Q (m x n), r <- R (n x n, upper triangular); a and r are
+ * device pointers to interleaved complex doubles, 16-byte aligned; stream is a
+ * cudaStream_t (NULL: the legacy default stream).  The workspace (about 0.52 MB) is one
+ * static device array holding the partials of up to 256 CTAs and 64 columns: n > 64
+ * returns TTN_ECAPACITY.  The first call on a device looks the array up (set-up); make
+ * it before any stream capture.  All calls share the array, so calls that overlap on
+ * the GPU race.  Returns after the stream has finished the QR (TTN_ETIMEOUT if a grid
+ * barrier gave up). */
+int ttn_qr_noalloc(int m, int n, double* a, double* r, void* stream, int device);
+
 #ifdef __cplusplus
 }
 #endif

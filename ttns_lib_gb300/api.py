@@ -98,6 +98,7 @@ SIGNATURES = {
     "ttn_debug_num_groups": (_I, [_P, _I, _IP]),
     "ttn_debug_get_env": (_I, [_P, _I, _I, _I, _DP]),
     "ttn_debug_qr": (_I, [_I, _I, _DP, _DP, _I]),
+    "ttn_qr_noalloc": (_I, [_I, _I, _P, _P, _P, _I]),
     "ttn_debug_tc_gemm": (_I, [_DP, _DP, _DP, _I, _I, _I]),
 }
 

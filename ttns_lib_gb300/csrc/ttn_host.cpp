@@ -32,6 +32,7 @@
 namespace ttn {
 
 static thread_local std::string g_err;
+void set_error_message(const std::string& msg) { g_err = msg; }
 
 struct Err : std::runtime_error {
   int code;

@@ -95,6 +95,7 @@ SIGNATURES = {
     "ttn_debug_heff": (_I, [_P, _I, _DP, _DP]),
     "ttn_debug_expm_node": (_I, [_P, _I, _D, _D, _D, _DP, _LLP]),
     "ttn_debug_program_apply": (_I, [_P, _I, _I, _DP, _DP]),
+    "ttn_integrator_kernel_phases": (_I, [_P, _DP]),
     "ttn_debug_num_groups": (_I, [_P, _I, _IP]),
     "ttn_debug_get_env": (_I, [_P, _I, _I, _I, _DP]),
     "ttn_debug_qr": (_I, [_I, _I, _DP, _DP, _I]),
@@ -329,6 +330,17 @@ class fixed_step_projector_splitting_integrator:
                 if n[k * 4 + c]:
                     out[f"{kn}[{cn}]"] = (float(t[k * 4 + c]), int(n[k * 4 + c]))
         return out
+
+    KERNEL_PHASES = ["begin", "matvec", "alpha", "reorth_coef", "reorth_norm", "avnorm", "control", "combine"]
+
+    def kernel_phases(self):
+        """ms per phase of the Krylov kernel since the last call (needs TTN_PROFILE)."""
+        out = np.zeros(10)
+        _check(lib().ttn_integrator_kernel_phases(self.h, _dp(out)))
+        d = {k: float(out[i]) for i, k in enumerate(self.KERNEL_PHASES)}
+        d["substeps"] = int(out[8])
+        d["launches"] = int(out[9])
+        return d
 
     def io_bytes(self):
         a, b = C.c_longlong(), C.c_longlong()

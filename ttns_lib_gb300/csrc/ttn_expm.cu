@@ -104,36 +104,85 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
   }
 }
 
-// ---- tensor-core contractions (mixed precision).  Per tile D(128 x 64) = A(128 x 128) B(64 x 128)^T
-// in split TF32 with two FP32 accumulators in TMEM (hi*hi and hi*lo + lo*hi).
+// ---- tensor-core contractions (mixed precision)
+//
+// Both kinds are D(128 x 64) = A B^T per tile on split TF32 operands with FP32
+// accumulation in TMEM (columns 0-63: hi*hi, 64-127: hi*lo + lo*hi; Ootomo-Yokota):
+//   A (128 x 128) = real block form [[Re, -Im], [Im, Re]] of alpha * mat (64 x 64, row =
+//     output index, column = input index), the same for every tile of the op; built once
+//     per launch into a global image in the shared-memory operand layout and brought in
+//     by one bulk copy per op and CTA;
+//   B (64 x 128) = 64 input columns (real parts in k < 64, imaginary in k >= 64):
+//     MODE tile (aa, b0): in(aa, j, b0 + n) for n < 64;  MF tile x0: in(x0 + n, l).
+// Rows of D are (re/im, output index), columns the 64 tile positions n; the epilogue adds
+// the two accumulators in FP32, stages the tile in shared memory and writes coalesced
+// complex doubles (MODE: out(aa, i, b0 + n), MF: out(x0 + n, i)).
 struct TcState {
   uint32_t tmem;      // TMEM base (128 columns)
-  uint32_t phase;     // mbarrier parity
+  uint32_t phase;     // MMA mbarrier parity
+  uint32_t lphase;    // bulk-load mbarrier parity
   uint64_t* mbar;
-  uint32_t* a_hi;     // 128 x 128 tf32
-  uint32_t* a_lo;
-  uint32_t* b_hi;     // 64 x 128 tf32
-  uint32_t* b_lo;
+  uint64_t* lbar;
+  uint32_t* a;        // 128 x 128 tf32, hi then lo (kTcImageBytes)
+  uint32_t* b;        // 64 x 128 tf32, hi then lo; also the epilogue stage
 };
 constexpr int TC_A_WORDS = 128 * 128, TC_B_WORDS = 64 * 128;
+constexpr int TC_STAGE_LD = 65;   // floats per staged row (padding against bank conflicts)
 constexpr size_t TC_SMEM = (size_t)(2 * TC_A_WORDS + 2 * TC_B_WORDS) * 4;
+static_assert(128 * TC_STAGE_LD * 4 <= 2 * TC_B_WORDS * 4, "epilogue stage must fit in the B buffer");
+static_assert(kTcImageBytes == 2 * TC_A_WORDS * 4, "image size");
 
-__device__ __forceinline__ void put_a(TcState& t, int row, int k, double v) {
-  uint32_t h, l;
-  tc::split_tf32(v, h, l);
-  const uint32_t o = tc::tf32_offset(row, k, 128) / 4;
-  t.a_hi[o] = h;
-  t.a_lo[o] = l;
-}
-__device__ __forceinline__ void put_b(TcState& t, int row, int k, double v) {
-  uint32_t h, l;
-  tc::split_tf32(v, h, l);
-  const uint32_t o = tc::tf32_offset(row, k, 64) / 4;
-  t.b_hi[o] = h;
-  t.b_lo[o] = l;
+// operator images of every tensor-core op of the program (all CTAs, grid-stride)
+__device__ void build_tc_images(const ExpmArgs& a) {
+  const long long nthreads = (long long)gridDim.x * blockDim.x;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int k = 0; k < a.nops; ++k) {
+    const MvOp& op = a.prog[k];
+    if (!op.tc) continue;
+    uint32_t* img = a.tc_img + (size_t)op.img * (2 * TC_A_WORDS);
+    for (long long e = tid; e < 64 * 64; e += nthreads) {
+      const int i = (int)(e / 64), j = (int)(e % 64);
+      const double2 sv = cmul(op.alpha, op.mat[e]);
+      const float re = tc::f64_to_f32_int(sv.x), im = tc::f64_to_f32_int(sv.y);
+      uint32_t h, l;
+      tc::split_tf32_f(re, h, l);
+      img[tc::tf32_offset(i, j, 128) / 4] = h;
+      img[TC_A_WORDS + tc::tf32_offset(i, j, 128) / 4] = l;
+      img[tc::tf32_offset(64 + i, 64 + j, 128) / 4] = h;
+      img[TC_A_WORDS + tc::tf32_offset(64 + i, 64 + j, 128) / 4] = l;
+      tc::split_tf32_f(im, h, l);
+      img[tc::tf32_offset(64 + i, j, 128) / 4] = h;
+      img[TC_A_WORDS + tc::tf32_offset(64 + i, j, 128) / 4] = l;
+      tc::split_tf32_f(-im, h, l);
+      img[tc::tf32_offset(i, 64 + j, 128) / 4] = h;
+      img[TC_A_WORDS + tc::tf32_offset(i, 64 + j, 128) / 4] = l;
+    }
+  }
+  // the images are read by bulk copies (async proxy) after the next grid barrier
+  tc::fence_proxy_async_all();
 }
 
-// issue the 48 MMAs of one tile, wait for them; returns false on a timed-out wait
+// stage the B tile: thread task (n, j4) converts in[n-th column, k = 4 j4 .. 4 j4 + 3]
+// (element offset src(n, j) = base + n * sn + j * sj) into 16-byte core-matrix rows
+__device__ __forceinline__ void tc_stage_b(const TcState& t, const double2* base, long long sn, long long sj) {
+  for (int task = threadIdx.x; task < 64 * 16; task += blockDim.x) {
+    const int n = task & 63, j4 = task >> 6;
+    uint32_t rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const double2 v = base[(long long)n * sn + (long long)(4 * j4 + q) * sj];
+      tc::split_tf32_f(tc::f64_to_f32_int(v.x), rh[q], rl[q]);
+      tc::split_tf32_f(tc::f64_to_f32_int(v.y), ih[q], il[q]);
+    }
+    const uint32_t ore = tc::tf32_offset(n, 4 * j4, 64) / 4, oim = tc::tf32_offset(n, 64 + 4 * j4, 64) / 4;
+    *reinterpret_cast<uint4*>(t.b + ore) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+    *reinterpret_cast<uint4*>(t.b + TC_B_WORDS + ore) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+    *reinterpret_cast<uint4*>(t.b + oim) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+    *reinterpret_cast<uint4*>(t.b + TC_B_WORDS + oim) = make_uint4(il[0], il[1], il[2], il[3]);
+  }
+}
+
+// issue the 48 MMAs of one tile and wait for them; false on a timed-out wait
 __device__ bool tc_tile_mma(TcState& t) {
   tc::fence_proxy_async();
   tc::fence_before();
@@ -142,12 +191,14 @@ __device__ bool tc_tile_mma(TcState& t) {
   if (threadIdx.x == 0) {
     const uint32_t idesc = tc::idesc_tf32(128, 64);
     const uint32_t lboA = 16 * 128, lboB = 8 * 128, sbo = 128;
+    const uint32_t a_hi = tc::smem_u32(t.a), a_lo = a_hi + TC_A_WORDS * 4;
+    const uint32_t b_hi = tc::smem_u32(t.b), b_lo = b_hi + TC_B_WORDS * 4;
     for (int kk = 0; kk < 16; ++kk) {
       const uint32_t offA = (uint32_t)kk * 2 * 16 * 128, offB = (uint32_t)kk * 2 * 8 * 128;
-      const uint64_t ah = tc::smem_desc(tc::smem_u32(t.a_hi) + offA, lboA, sbo);
-      const uint64_t al = tc::smem_desc(tc::smem_u32(t.a_lo) + offA, lboA, sbo);
-      const uint64_t bh = tc::smem_desc(tc::smem_u32(t.b_hi) + offB, lboB, sbo);
-      const uint64_t bl = tc::smem_desc(tc::smem_u32(t.b_lo) + offB, lboB, sbo);
+      const uint64_t ah = tc::smem_desc(a_hi + offA, lboA, sbo);
+      const uint64_t al = tc::smem_desc(a_lo + offA, lboA, sbo);
+      const uint64_t bh = tc::smem_desc(b_hi + offB, lboB, sbo);
+      const uint64_t bl = tc::smem_desc(b_lo + offB, lboB, sbo);
       tc::mma_tf32(t.tmem, ah, bh, idesc, kk > 0);
       tc::mma_tf32(t.tmem + 64, ah, bl, idesc, kk > 0);
       tc::mma_tf32(t.tmem + 64, al, bh, idesc, 1);
@@ -161,101 +212,75 @@ __device__ bool tc_tile_mma(TcState& t) {
   return ok;
 }
 
-// this thread's row (warps 0-3: rows 0..127) of the tile result, 16 columns starting at c0
-__device__ __forceinline__ void tc_tile_row16(const TcState& t, int c0, double* v) {
+// TMEM -> stage (float [128][TC_STAGE_LD], in the B buffer) by warps 0-3, one row each
+__device__ __forceinline__ void tc_drain_to_stage(const TcState& t) {
   const int warp = threadIdx.x >> 5;
-  float mv[16], cv[16];
-  tc::tmem_ld16(t.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, mv);
-  tc::tmem_ld16(t.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(64 + c0), cv);
+  if (warp < 4) {
+    float* row = reinterpret_cast<float*>(t.b) + threadIdx.x * TC_STAGE_LD;
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+      float mv[16], cv[16];
+      tc::tmem_ld16(t.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, mv);
+      tc::tmem_ld16(t.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(64 + c0), cv);
 #pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = (double)mv[i] + (double)cv[i];
+      for (int q = 0; q < 16; ++q) row[c0 + q] = mv[q] + cv[q];
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
 }
 
 __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, TcState& t) {
   const double2* in = buf_of(a, op.in, x);
   double2* out = buf_of(a, op.out, x);
-  const int warp = threadIdx.x >> 5;
   const bool acc = (op.beta != 0);
-  if (op.kind == MV_MODE) {
-    // out(aa, i, b) = sum_j (alpha S)(i, j) in(aa, j, b); tiles of 64 columns b
-    const long long nb = op.nb, tiles = op.na * (nb / 64);
-    if ((long long)blockIdx.x >= tiles) return;
-    // A = real block form of alpha*S, loaded once per op by every CTA that has a tile
-    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
-      const int i = e / 64, j = e % 64;
-      const double2 sv = cmul(op.alpha, op.mat[e]);
-      put_a(t, i, j, sv.x);
-      put_a(t, i, 64 + j, -sv.y);
-      put_a(t, 64 + i, j, sv.y);
-      put_a(t, 64 + i, 64 + j, sv.x);
+  const bool mode = (op.kind == MV_MODE);
+  const long long nb = op.nb;
+  const long long tiles = mode ? op.na * (nb / 64) : op.na / 64;
+  if ((long long)blockIdx.x >= tiles) return;
+  // operator image -> shared memory (one bulk copy), overlapped with the first B tile
+  if (threadIdx.x == 0) {
+    tc::fence_proxy_async_all();
+    tc::mbar_expect_tx(t.lbar, (uint32_t)kTcImageBytes);
+    tc::bulk_g2s(t.a, a.tc_img + (size_t)op.img * (2 * TC_A_WORDS), (uint32_t)kTcImageBytes, t.lbar);
+  }
+  bool loaded = false;
+  const float* stage = reinterpret_cast<const float*>(t.b);
+  for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    long long aa = 0, b0 = 0;
+    if (mode) {
+      aa = tile / (nb / 64);
+      b0 = (tile % (nb / 64)) * 64;
+      tc_stage_b(t, in + aa * 64 * nb + b0, 1, nb);
+    } else {
+      b0 = tile * 64;
+      tc_stage_b(t, in + b0 * 64, 64, 1);
     }
-    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-      const long long aa = tile / (nb / 64), b0 = (tile % (nb / 64)) * 64;
-      const double2* src = in + aa * 64 * nb + b0;
-      for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
-        const int j = e / 64, n = e % 64;  // consecutive threads read consecutive b
-        const double2 v = src[(long long)j * nb + n];
-        put_b(t, n, j, v.x);
-        put_b(t, n, 64 + j, v.y);
-      }
-      if (!tc_tile_mma(t) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
-      if (warp < 4) {
-        const int row = threadIdx.x;  // 0..127: rows < 64 real parts, >= 64 imaginary parts
-        const int i = row & 63;
-        double* dst = (double*)(out + aa * 64 * nb + (long long)i * nb + b0) + (row >> 6);
-        for (int c0 = 0; c0 < 64; c0 += 16) {
-          double v[16];
-          tc_tile_row16(t, c0, v);
-#pragma unroll
-          for (int n = 0; n < 16; ++n) dst[2 * (c0 + n)] = acc ? dst[2 * (c0 + n)] + v[n] : v[n];
-        }
-      }
-      tc::fence_before();
-      __syncthreads();
+    if (!loaded) {
+      if (!tc::mbar_wait(t.lbar, t.lphase) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
+      t.lphase ^= 1u;
+      loaded = true;
     }
-  } else {
-    // MF: out(x, k) = sum_l in(x, l) (alpha M)(k, l); tiles of 128 rows x, two column halves
-    const long long nx = op.na, tiles = (nx / 128) * 2;
-    if ((long long)blockIdx.x >= tiles) return;
-    int loaded_half = -1;
-    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-      const long long xb = tile / 2;
-      const int half = (int)(tile % 2);
-      if (half != loaded_half) {
-        for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
-          const int k = e / 64, l = e % 64;
-          const double2 mv = cmul(op.alpha, op.mat[e]);
-          if (half == 0) {
-            put_b(t, k, l, mv.x);
-            put_b(t, k, 64 + l, -mv.y);
-          } else {
-            put_b(t, k, l, mv.y);
-            put_b(t, k, 64 + l, mv.x);
-          }
-        }
-        loaded_half = half;
+    if (!tc_tile_mma(t) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
+    tc_drain_to_stage(t);
+    // stage -> out: element (i, n) = (stage[i][n], stage[64 + i][n])
+    for (int task = threadIdx.x; task < 64 * 64; task += blockDim.x) {
+      int i, n;
+      double2* dst;
+      if (mode) {
+        n = task & 63;
+        i = task >> 6;
+        dst = out + aa * 64 * nb + (long long)i * nb + b0 + n;
+      } else {
+        i = task & 63;
+        n = task >> 6;
+        dst = out + (b0 + n) * 64 + i;
       }
-      const double2* src = in + xb * 128 * 64;
-      for (int e = threadIdx.x; e < 128 * 64; e += blockDim.x) {
-        const int r = e / 64, l = e % 64;
-        const double2 v = src[e];
-        put_a(t, r, l, v.x);
-        put_a(t, r, 64 + l, v.y);
-      }
-      if (!tc_tile_mma(t) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
-      if (warp < 4) {
-        const int row = threadIdx.x;
-        double* dst = (double*)(out + (xb * 128 + row) * 64) + half;
-        for (int c0 = 0; c0 < 64; c0 += 16) {
-          double v[16];
-          tc_tile_row16(t, c0, v);
-#pragma unroll
-          for (int k = 0; k < 16; ++k) dst[2 * (c0 + k)] = acc ? dst[2 * (c0 + k)] + v[k] : v[k];
-        }
-      }
-      tc::fence_before();
-      __syncthreads();
+      double2 v = make_double2(tc::f32_to_f64_int(stage[i * TC_STAGE_LD + n]),
+                               tc::f32_to_f64_int(stage[(64 + i) * TC_STAGE_LD + n]));
+      if (acc) v = cadd(v, *dst);
+      *dst = v;
     }
+    __syncthreads();
   }
 }
 
@@ -293,133 +318,87 @@ __device__ void reduce_partials(const double2* part, int nq, double2* out, Red& 
   __syncthreads();
 }
 
-__device__ double2 cexp_d(double2 x) {
-  double ex = exp(x.x), sn, cs;
-  sincos(x.y, &sn, &cs);
-  return make_double2(ex * cs, ex * sn);
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
-__device__ double cabs_d(double2 x) { return hypot(x.x, x.y); }
-__device__ double2 cdiv_s(double2 a, double2 b) {
-  if (fabs(b.x) >= fabs(b.y)) {
-    double r = b.y / b.x, den = b.x + b.y * r;
-    return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
-  }
-  double r = b.x / b.y, den = b.x * r + b.y;
-  return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
-}
-__device__ double2 phi1(double2 x) {
-  if (cabs_d(x) < 0.5) {
-    double2 s = make_double2(0.0, 0.0), t = make_double2(1.0, 0.0);
-    for (int k = 1; k <= 18; ++k) {
-      s = cadd(s, t);
-      t = cscale(1.0 / double(k + 1), cmul(t, x));
+// wall time per phase as seen by one thread of CTA 0 (barrier waits included)
+struct PhaseClock {
+  unsigned long long* acc;
+  unsigned long long t;
+  __device__ void mark(int k) {
+    if (acc) {
+      const unsigned long long now = gtimer();
+      acc[k] += now - t;
+      t = now;
     }
-    return s;
   }
-  double2 ex = cexp_d(x);
-  return cdiv_s(make_double2(ex.x - 1.0, ex.y), x);
-}
-__device__ double2 phi2(double2 x) {
-  if (cabs_d(x) < 0.5) {
-    double2 s = make_double2(0.0, 0.0), t = make_double2(0.5, 0.0);
-    for (int k = 2; k <= 20; ++k) {
-      s = cadd(s, t);
-      t = cscale(1.0 / double(k + 1), cmul(t, x));
-    }
-    return s;
-  }
-  double2 ex = cexp_d(x);
-  return cdiv_s(make_double2(ex.x - 1.0 - x.x, ex.y - x.y), cmul(x, x));
-}
-
-// Implicit-QL eigen-decomposition (EISPACK tql2 scheme) by one warp: lane 0 runs the
-// scalar recurrences and records the plane rotations, all lanes apply them to their
-// rows of the eigenvector matrix.  Per element the operations are those of the
-// sequential routine, in the same order.
-struct CtlSmem {
-  double z[64 * 64];
-  double d[64], e[64];
-  double rs[64], rc[64];
-  int rot_lo, rot_hi, status;
-  double2 F[66];
 };
 
-__device__ int warp_tql2(int n, CtlSmem& S) {
+// The small exponential of the step control, F = exp(zc * Haug) e1, by one warp.
+// Haug is the Lanczos tridiagonal (d on the diagonal, e[i] coupling rows i-1 and i) of
+// size mb, bordered when aug is set by row mb = betm at column mb-1 and row mb+1 = 1 at
+// column mb (Sidje's augmented matrix, whose rows mb and mb+1 of exp(zc Haug) e1 are
+// betm zc e_mb^T phi1(zc T) e1 and betm zc^2 e_mb^T phi2(zc T) e1, the two terms of the
+// error estimate).  Evaluated as (sum_{k<=kTaylor} (zc Haug / s)^k / k!)^s e1 with s
+// chosen so that ||zc Haug / s||_inf <= 1: truncation below 1e-17 relative, and every
+// row is one lane, so the dependent chain per term is a handful of FP64 operations
+// (FP64 latency, not throughput, bounds this phase on GB300).
+struct CtlSmem {
+  double d[EQ], e[EQ + 1];
+  double2 x[EQ + 2];
+  double2 t[2][EQ + 2];
+};
+constexpr int kTaylor = 18;
+constexpr int kMaxScaling = 4096;   // ||zc Haug||_inf above this fails the step (error bit 4)
+
+__device__ bool warp_expm_e1(int mb, bool aug, double betm, double2 zc, CtlSmem& S) {
   const int lane = threadIdx.x & 31;
-  for (int i = lane; i < n * n; i += 32) S.z[i] = ((i / n) == (i % n)) ? 1.0 : 0.0;
+  const int mx = mb + (aug ? 2 : 0);
+  double rn = 0.0;
+  for (int i = lane; i < mx; i += 32) {
+    double r;
+    if (i < mb) r = fabs(S.d[i]) + (i > 0 ? fabs(S.e[i]) : 0.0) + (i + 1 < mb ? fabs(S.e[i + 1]) : 0.0);
+    else if (i == mb) r = fabs(betm);
+    else r = 1.0;
+    rn = fmax(rn, r);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) rn = fmax(rn, __shfl_xor_sync(0xffffffffu, rn, o));
+  const double nrm = rn * hypot(zc.x, zc.y);
+  if (!(nrm <= (double)kMaxScaling)) return false;
+  const int s = nrm > 1.0 ? (int)ceil(nrm) : 1;
+  const double inv_s = 1.0 / (double)s;
+  for (int i = lane; i < mx; i += 32) S.x[i] = make_double2(i == 0 ? 1.0 : 0.0, 0.0);
   __syncwarp();
-  for (int l = 0; l < n; ++l) {
-    int iter = 0;
-    for (;;) {
-      if (lane == 0) {
-        int m;
-        double* d = S.d;
-        double* e = S.e;
-        for (m = l; m < n - 1; ++m) {
-          double dd = fabs(d[m]) + fabs(d[m + 1]);
-          if (fabs(e[m]) <= 1e-300 + 2.220446049250313e-16 * dd) break;
-        }
-        S.status = 0;
-        S.rot_lo = S.rot_hi = 0;
-        if (m == l) {
-          S.status = 1;  // converged
-        } else if (++iter > 60) {
-          S.status = 2;  // failed
+  for (int rep = 0; rep < s; ++rep) {
+    for (int i = lane; i < mx; i += 32) S.t[0][i] = S.x[i];
+    __syncwarp();
+    int cur = 0;
+    for (int k = 1; k <= kTaylor; ++k) {
+      const double2 ck = cscale(inv_s / (double)k, zc);
+      const double2* tc = S.t[cur];
+      for (int i = lane; i < mx; i += 32) {
+        double2 u;
+        if (i < mb) {
+          u = cscale(S.d[i], tc[i]);
+          if (i > 0) u = make_double2(fma(S.e[i], tc[i - 1].x, u.x), fma(S.e[i], tc[i - 1].y, u.y));
+          if (i + 1 < mb) u = make_double2(fma(S.e[i + 1], tc[i + 1].x, u.x), fma(S.e[i + 1], tc[i + 1].y, u.y));
+        } else if (i == mb) {
+          u = cscale(betm, tc[mb - 1]);
         } else {
-          double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-          double r = hypot(g, 1.0);
-          g = d[m] - d[l] + e[l] / (g + (g >= 0.0 ? fabs(r) : -fabs(r)));
-          double s = 1.0, c = 1.0, p = 0.0;
-          int i;
-          bool underflow = false;
-          S.rot_hi = m - 1;
-          for (i = m - 1; i >= l; --i) {
-            double f = s * e[i], b = c * e[i];
-            r = hypot(f, g);
-            e[i + 1] = r;
-            if (r == 0.0) {
-              d[i + 1] -= p;
-              e[m] = 0.0;
-              underflow = true;
-              break;
-            }
-            s = f / r;
-            c = g / r;
-            g = d[i + 1] - p;
-            r = (d[i] - g) * s + 2.0 * c * b;
-            p = s * r;
-            d[i + 1] = g + p;
-            g = c * r - b;
-            S.rs[i] = s;
-            S.rc[i] = c;
-          }
-          S.rot_lo = underflow ? i + 1 : l;
-          if (!underflow) {
-            d[l] -= p;
-            e[l] = g;
-            e[m] = 0.0;
-          }
-          S.status = underflow ? 3 : 0;
+          u = tc[mb];
         }
+        const double2 v = cmul(ck, u);
+        S.t[cur ^ 1][i] = v;
+        S.x[i] = cadd(S.x[i], v);
       }
       __syncwarp();
-      const int st = S.status;
-      if (st == 1) break;
-      if (st == 2) return 1;
-      // apply the recorded rotations i = rot_hi .. rot_lo to every row k (lane-parallel)
-      const int hi = S.rot_hi, lo = S.rot_lo;
-      for (int k = lane; k < n; k += 32) {
-        for (int i = hi; i >= lo; --i) {
-          double s = S.rs[i], c = S.rc[i];
-          double f = S.z[k * n + i + 1];
-          S.z[k * n + i + 1] = s * S.z[k * n + i] + c * f;
-          S.z[k * n + i] = c * S.z[k * n + i] - s * f;
-        }
-      }
-      __syncwarp();
+      cur ^= 1;
     }
   }
-  return 0;
+  return true;
 }
 
 // Expokit step control by warp 0 of block 0.
@@ -435,16 +414,9 @@ __device__ void control(const ExpmArgs& a, CtlSmem& S) {
   const double beta = ctl->beta, avnorm = ctl->avnorm;
   for (int i = lane; i < mb; i += 32) {
     S.d[i] = ctl->alpha[i];
-    S.e[i] = (i + 1 < mb) ? ctl->bet[i + 1] : 0.0;
+    S.e[i] = ctl->bet[i];
   }
   __syncwarp();
-  if (warp_tql2(mb, S)) {
-    if (lane == 0) {
-      ctl->err |= 4;
-      ctl->done = 1;
-    }
-    return;
-  }
   __shared__ double s_tstep, s_err, s_xm;
   __shared__ int s_accept, s_fail;
   if (lane == 0) {
@@ -455,19 +427,19 @@ __device__ void control(const ExpmArgs& a, CtlSmem& S) {
   }
   __syncwarp();
   const double2 cf = make_double2(ctl->cf_re, ctl->cf_im);
+  const double betm = ctl->bet[mb];
   int ireject = 0;
   for (;;) {
     const double t_step = s_tstep;
     const double2 zc = cscale(ctl->sgn * t_step, cf);
-    for (int i = lane; i < mb; i += 32) {
-      double2 s = make_double2(0.0, 0.0);
-      for (int q = 0; q < mb; ++q) {
-        double2 ex = cexp_d(cscale(S.d[q], zc));
-        s = cadd(s, cscale(S.z[i * mb + q] * S.z[q], ex));
+    const bool ok = warp_expm_e1(mb, k1 != 0, betm, zc, S);
+    if (!ok) {
+      if (lane == 0) {
+        ctl->err |= 4;
+        ctl->done = 1;
       }
-      S.F[i] = s;
+      return;
     }
-    __syncwarp();
     if (lane == 0) {
       double err_loc, xm = 1.0 / m;
       int accept = 0;
@@ -475,16 +447,7 @@ __device__ void control(const ExpmArgs& a, CtlSmem& S) {
         err_loc = 1e-14;
         accept = 1;
       } else {
-        double2 f1 = make_double2(0.0, 0.0), f2 = make_double2(0.0, 0.0);
-        for (int q = 0; q < mb; ++q) {
-          double2 x = cscale(S.d[q], zc);
-          double w = S.z[(mb - 1) * mb + q] * S.z[q];
-          f1 = cadd(f1, cscale(w, cmul(zc, phi1(x))));
-          f2 = cadd(f2, cscale(w, cmul(cmul(zc, zc), phi2(x))));
-        }
-        S.F[mb] = cscale(ctl->bet[mb], f1);
-        S.F[mb + 1] = cscale(ctl->bet[mb], f2);
-        double p1 = cabs_d(S.F[mb]) * beta, p2 = cabs_d(S.F[mb + 1]) * beta * avnorm;
+        double p1 = hypot(S.x[mb].x, S.x[mb].y) * beta, p2 = hypot(S.x[mb + 1].x, S.x[mb + 1].y) * beta * avnorm;
         if (p1 > 10.0 * p2) {
           err_loc = p2;
           xm = 1.0 / m;
@@ -525,7 +488,7 @@ __device__ void control(const ExpmArgs& a, CtlSmem& S) {
     } else {
       const int mx = mb + (k1 > 1 ? k1 - 1 : 0);
       for (int q = 0; q < 72; ++q) {
-        double2 c = (q < mx) ? cscale(beta, S.F[q]) : make_double2(0.0, 0.0);
+        double2 c = (q < mx) ? cscale(beta, S.x[q]) : make_double2(0.0, 0.0);
         ctl->coef[2 * q] = c.x;
         ctl->coef[2 * q + 1] = c.y;
       }
@@ -549,6 +512,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
   __shared__ double2 red[EQ];
   __shared__ int s_done;
   __shared__ __align__(8) uint64_t s_mbar;
+  __shared__ __align__(8) uint64_t s_lbar;
   __shared__ uint32_t s_tmem;
   extern __shared__ __align__(1024) unsigned char dsm[];
   // the controller's scratch and the tensor-core operands share the dynamic buffer: they
@@ -557,19 +521,24 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
   TcState tcs;
   TcState* tcp = nullptr;
   if (a.mixed) {
-    if (threadIdx.x == 0) tc::mbar_init(&s_mbar, 1);
+    if (threadIdx.x == 0) {
+      tc::mbar_init(&s_mbar, 1);
+      tc::mbar_init(&s_lbar, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&s_tmem, 128);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     tcs.tmem = s_tmem;
     tcs.phase = 0;
+    tcs.lphase = 0;
     tcs.mbar = &s_mbar;
-    tcs.a_hi = reinterpret_cast<uint32_t*>(dsm);
-    tcs.a_lo = tcs.a_hi + TC_A_WORDS;
-    tcs.b_hi = tcs.a_lo + TC_A_WORDS;
-    tcs.b_lo = tcs.b_hi + TC_B_WORDS;
+    tcs.lbar = &s_lbar;
+    tcs.a = reinterpret_cast<uint32_t*>(dsm);
+    tcs.b = tcs.a + 2 * TC_A_WORDS;
     tcp = &tcs;
+    build_tc_images(a);
   }
   KrylovCtl* ctl = a.ctl;
   const long long n = a.n;
@@ -599,6 +568,11 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
     grid_barrier(a.bar, a.err);
     run_program(a, a.y, tcp);
     grid_barrier(a.bar, a.err);
+  }
+  PhaseClock pc{(a.phase && blockIdx.x == 0 && threadIdx.x == 0) ? a.phase : nullptr, 0ull};
+  if (pc.acc) {
+    pc.t = gtimer();
+    pc.acc[9] += 1;
   }
   for (int sub = 0; sub < (a.apply_only ? 0 : 100000); ++sub) {
     grid_barrier(a.bar, a.err);
@@ -632,11 +606,14 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
         }
       }
     }
+    if (pc.acc) pc.acc[8] += 1;
+    pc.mark(0);
     // ---- Lanczos with full re-orthogonalisation
     for (int j = 0; j < m; ++j) {
       const double2* Vj = a.V + (long long)j * a.ldv;
       grid_barrier(a.bar, a.err);
       run_program(a, Vj, tcp);
+      pc.mark(1);
       // partial <V_j, p> over my elements (same element ownership as the last writes of p)
       {
         double2 s = make_double2(0.0, 0.0);
@@ -662,6 +639,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
         }
         a.p[i] = x;
       }
+      pc.mark(2);
       for (int q = 0; q <= j; ++q) {
         const double2* Vq = a.V + (long long)q * a.ldv;
         double2 s = make_double2(0.0, 0.0);
@@ -674,6 +652,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
       if (blockIdx.x == 0 && threadIdx.x == 0) ctl->alpha[j] = alpha;
       grid_barrier(a.bar, a.err);
       reduce_partials(pb, j + 1, red, sm);
+      pc.mark(3);
       {
         double s = 0.0;
         for (long long i = tid; i < n; i += nthreads) {
@@ -710,6 +689,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
         }
         __syncthreads();
       }
+      pc.mark(4);
     }
     // ---- ||H V_m|| for the error estimate
     grid_barrier(a.bar, a.err);
@@ -725,6 +705,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
       store_partials(sm, 1, pa);
     }
     grid_barrier(a.bar, a.err);
+    pc.mark(5);
     if (blockIdx.x == 0) {
       reduce_partials(pa, 1, red, sm);
       if (threadIdx.x == 0) ctl->avnorm = sqrt(red[0].x);
@@ -732,6 +713,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
       if (warp == 0) control(a, cs);
     }
     grid_barrier(a.bar, a.err);
+    pc.mark(6);
     // ---- y = sum_q c_q V_q
     {
       for (int q = threadIdx.x; q <= m; q += blockDim.x)
@@ -744,6 +726,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
       }
       __syncthreads();
     }
+    pc.mark(7);
   }
   if (a.mixed) {
     tc::fence_before();

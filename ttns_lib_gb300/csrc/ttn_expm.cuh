@@ -1,6 +1,7 @@
 // Persistent cooperative Krylov exponential (see ttn_expm.cu).
 #pragma once
 #include <cuda_runtime.h>
+#include <cstdint>
 
 #include "ttn_kernels.cuh"
 
@@ -23,8 +24,11 @@ struct MvOp {
   int d;
   int beta;  // 1: accumulate into out
   int tc;    // 1: run on the tensor cores (mixed precision; MODE with d = 64, MF with r = 64)
+  int img;   // tensor-core ops: slot of the operator image (split TF32 block form of alpha mat)
   double2 alpha;
 };
+// bytes of one operator image: a 128 x 128 TF32 operand, high and low parts
+constexpr size_t kTcImageBytes = (size_t)2 * 128 * 128 * 4;
 
 struct ExpmArgs {
   double2* y;            // vector evolved in place
@@ -45,7 +49,11 @@ struct ExpmArgs {
   double tau, cf_re, cf_im, tol;
   int mixed;             // 1: the program contains tensor-core contractions (TMEM + big smem)
   int apply_only;        // 1: apply the program once to y (result in p) and return
+  unsigned long long* phase;  // optional: ns spent per phase as seen by CTA 0 (kPhases slots)
+  uint32_t* tc_img;      // operator images of the tensor-core ops (kTcImageBytes each)
 };
+constexpr int kPhases = 10;  // begin, matvec, alpha, reorth coefficients, reorth + norm,
+                             // ||H V_m||, control, combine, sub-steps, launches
 
 // co-resident CTAs for the plain (mixed = 0) or tensor-core (mixed = 1) configuration
 int expm_coop_max_grid(int mixed);
@@ -54,7 +62,7 @@ cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s);
 // whether a contraction can run on the tensor cores
 inline bool tc_eligible(int kind, int d, long long na, long long nb) {
   if (kind == MV_MODE) return d == 64 && nb % 64 == 0;
-  if (kind == MV_MF) return d == 64 && na % 128 == 0;
+  if (kind == MV_MF) return d == 64 && na % 64 == 0;
   return false;
 }
 

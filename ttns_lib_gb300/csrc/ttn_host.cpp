@@ -407,6 +407,8 @@ struct Integrator {
   int num_sms = 0, qr_max_grid = 1, expm_max_grid = 1, expm_max_grid_tc = 1;
   bool mixed = false;                      // tensor-core contractions in the matvec programs
   std::vector<char> heff_tc, kbond_tc;     // program contains tensor-core contractions
+  int max_tc_images = 0;                   // most tensor-core ops in one program
+  DevBuf tc_img_buf;                       // their operator images (kTcImageBytes each)
   // compiled matrix-vector programs for the persistent Krylov kernel
   DevBuf prog_buf, expm_part_buf;
   std::vector<int> heff_off, heff_n, kbond_off, kbond_n;
@@ -424,6 +426,7 @@ struct Integrator {
   // optional breakdown (TTN_PROFILE=1): synchronising wall time per operation kind and
   // node-size class; slows the sweep down, for analysis only
   bool profiling = std::getenv("TTN_PROFILE") != nullptr;
+  unsigned long long* phase_dev = nullptr;  // Krylov kernel phase timers (TTN_PROFILE)
   double prof_t[8][4] = {};
   long long prof_n[8][4] = {};
   struct Prof {
@@ -565,9 +568,10 @@ struct Integrator {
       qtau = take(kQrMaxCols * sizeof(double2));
       scal = take(64 * sizeof(double2));
     }
-    ctl_buf.alloc(align256(sizeof(KrylovCtl)) + 256);
+    ctl_buf.alloc(align256(sizeof(KrylovCtl)) + 512);
     ctl = ctl_buf.as<KrylovCtl>();
     status = (int*)(ctl_buf.as<char>() + align256(sizeof(KrylovCtl)));
+    if (profiling) phase_dev = (unsigned long long*)(ctl_buf.as<char>() + align256(sizeof(KrylovCtl)) + 256);
     CK(cudaMemsetAsync(ctl_buf.p, 0, ctl_buf.bytes, stream));
     CK(cudaMallocHost((void**)&hctl, sizeof(HostCtl)));
     CK(cudaEventCreate(&ev0));
@@ -594,6 +598,7 @@ struct Integrator {
       flops_dev = (double*)(expm_part_buf.as<char>() + expm_partial_bytes(expm_max_grid) + 256);
       CK(cudaMemset(expm_part_buf.p, 0, expm_part_buf.bytes));
       compile_programs();
+      if (max_tc_images > 0) tc_img_buf.alloc((size_t)max_tc_images * kTcImageBytes);
     }
 
     CK(cudaStreamSynchronize(stream));
@@ -900,8 +905,10 @@ struct Integrator {
     bool mixed = false;
     std::vector<MvOp> ops;
     unsigned dirty = 0, read = 0, dirty_tc = 0;
+    int n_img = 0;
     void emit(MvOp op) {
       op.tc = (mixed && tc_eligible(op.kind, op.d, op.na, op.nb)) ? 1 : 0;
+      op.img = op.tc ? n_img++ : -1;
       const unsigned in_bit = (op.kind == MV_ZERO) ? 0u : (1u << op.in);
       const unsigned out_bit = 1u << op.out;
       const bool waw = (out_bit & dirty) && (op.tc || (out_bit & dirty_tc));
@@ -1002,10 +1009,12 @@ struct Integrator {
     std::vector<MvOp> all;
     heff_off.assign(T.n, 0); heff_n.assign(T.n, 0); kbond_off.assign(T.n, 0); kbond_n.assign(T.n, 0);
     heff_tc.assign(T.n, 0); kbond_tc.assign(T.n, 0);
+    max_tc_images = 0;
     auto mark = [&](const std::vector<MvOp>& ops) {
-      bool any = false;
-      for (const auto& o : ops) any = any || o.tc;
-      return any;
+      int n = 0;
+      for (const auto& o : ops) n += o.tc ? 1 : 0;
+      max_tc_images = std::max(max_tc_images, n);
+      return n > 0;
     };
     for (int i = 0; i < T.n; ++i) {
       auto h = heff_program(i);
@@ -1043,6 +1052,8 @@ struct Integrator {
     a.m = cfg.krylov_dim; a.tau = tau; a.cf_re = cf.real(); a.cf_im = cf.imag(); a.tol = cfg.krylov_tol;
     a.mixed = (kind == 0 ? heff_tc[nd] : kbond_tc[nd]) ? 1 : 0;
     a.apply_only = apply_only ? 1 : 0;
+    a.phase = phase_dev;
+    a.tc_img = tc_img_buf.as<uint32_t>();
     CK(expm_coop(a, expm_grid(n, a.mixed), stream));
     // Lanczos vector passes of one sub-step (the matvec flops are tallied on the device)
     if (tally) flops += lanczos_vec_flops(n);
@@ -1812,6 +1823,20 @@ int ttn_debug_expm_node(ttn_integrator* it, int node, double tau, double cre, do
   CK(cudaMemset(I.status, 0, sizeof(int)));
   TTN_REQUIRE(h == 0, TTN_ENUMERIC, "Krylov exponential failed on the device");
   if (napps) *napps = (tau == 0.0) ? 0 : k;
+  TTN_API_END
+}
+int ttn_integrator_kernel_phases(ttn_integrator* it, double* out) {
+  TTN_API_BEGIN
+  auto& I = it->I;
+  TTN_REQUIRE(out, TTN_EINVAL, "null output");
+  for (int k = 0; k < ttn::kPhases; ++k) out[k] = 0.0;
+  if (!I.phase_dev) return TTN_OK;
+  CK(cudaSetDevice(I.device));
+  CK(cudaStreamSynchronize(I.stream));
+  unsigned long long h[ttn::kPhases];
+  CK(cudaMemcpy(h, I.phase_dev, sizeof(h), cudaMemcpyDeviceToHost));
+  CK(cudaMemset(I.phase_dev, 0, sizeof(h)));
+  for (int k = 0; k < ttn::kPhases; ++k) out[k] = k < 8 ? 1e-6 * (double)h[k] : (double)h[k];
   TTN_API_END
 }
 int ttn_debug_program_apply(ttn_integrator* it, int node, int kind, const double* v, double* out) {

@@ -101,6 +101,48 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
   return false;
 }
 
+// ---- bulk copies global -> shared (TMA, 1-D), completing on an mbarrier
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+// dst and src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+               : "memory");
+}
+// order this thread's generic-proxy writes (global or shared) before later async-proxy accesses
+__device__ __forceinline__ void fence_proxy_async_all() { asm volatile("fence.proxy.async;" ::: "memory"); }
+
+// ---- conversions on the integer pipe (FP64 is slow on this part): f64 -> f32 truncating
+// the mantissa, f32 -> f64 exact; magnitudes below the f32 normal range become zero
+__device__ __forceinline__ float f64_to_f32_int(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+  uint32_t r;
+  if (e <= 0) r = sign;
+  else if (e >= 255) r = sign | 0x7F800000u;
+  else r = sign | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7FFFFFu);
+  return __uint_as_float(r);
+}
+__device__ __forceinline__ double f32_to_f64_int(float x) {
+  const uint32_t b = __float_as_uint(x);
+  const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+  const uint32_t e = (b >> 23) & 0xFF;
+  unsigned long long r;
+  if (e == 0) r = sign;
+  else if (e == 255) r = sign | 0x7FF0000000000000ull | ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  else r = sign | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)r);
+}
+// f32 -> tf32 hi + tf32 lo, hi + lo ~ x to about 22 bits
+__device__ __forceinline__ void split_tf32_f(float x, uint32_t& hi, uint32_t& lo) {
+  hi = to_tf32(x);
+  lo = to_tf32(x - __uint_as_float(hi));
+}
+
 // ---- TMEM -> registers: 16 consecutive fp32 columns of this warp's 32 lanes
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];

@@ -331,6 +331,8 @@ def run_ours(args):
     clk = clocks.stop()
     launches = api.launch_count() - l0
     flops_step = (tdvp.flops() - f0) / args.steps
+    sz_trace.append(tdvp.mel()(sb.SZ, 0, A).real)   # after the timed block (outside it)
+    n_compared = len(sz_trace)
     dist.barrier()
     ms_max = dist.max(ms)
     value = world * args.steps / (ms_max / 1e3)
@@ -353,11 +355,36 @@ def run_ours(args):
     h2d = host.nbytes + (io1[0] - io0[0]) // args.steps
     d2h = host.nbytes + (io1[1] - io0[1]) // args.steps
 
+    # The FP64 path on the same start state over the same warm-up and timed steps: its
+    # step rate and the largest |<sz>(mixed) - <sz>(FP64)| over the compared points.
+    fp64 = None
+    if prec_name == "mixed" and not args.no_fp64_compare:
+        del host
+        A64, t64 = make(api.PREC_FP64)
+        sz64 = []
+        for _ in range(args.warmup):
+            t64(A64, m.sop, -1j)
+            sz64.append(t64.mel()(sb.SZ, 0, A64).real)
+        t64.synchronize()
+        dist.barrier()
+        t64.timer_start()
+        for _ in range(args.steps):
+            t64(A64, m.sop, -1j)
+        ms64 = dist.max(t64.timer_stop())
+        sz64.append(t64.mel()(sb.SZ, 0, A64).real)
+        dsz = max(abs(a - b) for a, b in zip(sz_trace[:n_compared], sz64))
+        v64 = world * args.steps / (ms64 / 1e3)
+        fp64 = {"value": v64, "unit": "steps/s", "ms_per_step": ms64 / args.steps,
+                "mixed_over_fp64": value / v64, "max_abs_dsz": dsz, "dsz_bound": 1e-6,
+                "within_bound": bool(dsz <= 1e-6), "compared_points": n_compared,
+                "compared": "<sz> after each warm-up step and after the timed steps, same start state"}
+        del A64, t64
+
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "c128" if prec_name == "fp64" else "c128 state, split bf16/tf32 contractions",
+        "dtype": "c128" if prec_name == "fp64" else "c128 state and Krylov, split-TF32 tensor-core contractions",
         "data": "synthetic (formula-generated spin-boson bath; std::mt19937 unoccupied SPFs)",
         "config": workload_config(args.config, cfg, prec_name, over),
         "roofline": roof,
@@ -371,6 +398,8 @@ def run_ours(args):
     }
     if prec_name == "fp64" and args.precision == "auto":
         line["mixed"] = {"available": False, "reason": mixed_unavailable}
+    if fp64 is not None:
+        line["fp64"] = fp64
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, desc, _ = cpu_sample(args.config, threads)

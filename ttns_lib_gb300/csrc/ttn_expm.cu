@@ -72,8 +72,17 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
       const long long b = rem % nb;
       const double2* S = op.mat + (long long)i * d;
       const double2* v = in + aa * d * nb + b;
-      double2 s = make_double2(0.0, 0.0);
-      for (int j = 0; j < d; ++j) s = cfma(S[j], v[(long long)j * nb], s);
+      // four independent chains: FP64 latency, not throughput, bounds small contractions
+      double2 s0 = make_double2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
+      int j = 0;
+      for (; j + 4 <= d; j += 4) {
+        s0 = cfma(S[j], v[(long long)j * nb], s0);
+        s1 = cfma(S[j + 1], v[(long long)(j + 1) * nb], s1);
+        s2 = cfma(S[j + 2], v[(long long)(j + 2) * nb], s2);
+        s3 = cfma(S[j + 3], v[(long long)(j + 3) * nb], s3);
+      }
+      for (; j < d; ++j) s0 = cfma(S[j], v[(long long)j * nb], s0);
+      const double2 s = cadd(cadd(s0, s1), cadd(s2, s3));
       double2 r = cmul(op.alpha, s);
       if (acc) r = cadd(r, out[e]);
       out[e] = r;
@@ -86,8 +95,16 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
       const int k = (int)(e % r);
       const double2* v = in + xx * r;
       const double2* M = op.mat + (long long)k * r;
-      double2 s = make_double2(0.0, 0.0);
-      for (int l = 0; l < r; ++l) s = cfma(v[l], M[l], s);
+      double2 s0 = make_double2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
+      int l = 0;
+      for (; l + 4 <= r; l += 4) {
+        s0 = cfma(v[l], M[l], s0);
+        s1 = cfma(v[l + 1], M[l + 1], s1);
+        s2 = cfma(v[l + 2], M[l + 2], s2);
+        s3 = cfma(v[l + 3], M[l + 3], s3);
+      }
+      for (; l < r; ++l) s0 = cfma(v[l], M[l], s0);
+      const double2 s = cadd(cadd(s0, s1), cadd(s2, s3));
       double2 o = cmul(op.alpha, s);
       if (acc) o = cadd(o, out[e]);
       out[e] = o;
@@ -510,7 +527,7 @@ __device__ void control(const ExpmArgs& a, CtlSmem& S) {
 __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
   __shared__ Red sm;
   __shared__ double2 red[EQ];
-  __shared__ int s_done;
+  __shared__ int s_done, s_mb;
   __shared__ __align__(8) uint64_t s_mbar;
   __shared__ __align__(8) uint64_t s_lbar;
   __shared__ uint32_t s_tmem;
@@ -612,6 +629,10 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
     for (int j = 0; j < m; ++j) {
       const double2* Vj = a.V + (long long)j * a.ldv;
       grid_barrier(a.bar, a.err);
+      // after an exact breakdown the basis is complete: no further vectors
+      if (threadIdx.x == 0) s_mb = *(volatile int*)&ctl->mb;
+      __syncthreads();
+      if (s_mb < m) break;
       run_program(a, Vj, tcp);
       pc.mark(1);
       // partial <V_j, p> over my elements (same element ownership as the last writes of p)
@@ -640,13 +661,31 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
         a.p[i] = x;
       }
       pc.mark(2);
-      for (int q = 0; q <= j; ++q) {
-        const double2* Vq = a.V + (long long)q * a.ldv;
-        double2 s = make_double2(0.0, 0.0);
-        for (long long i = tid; i < n; i += nthreads) s = cadd(s, cmulc(Vq[i], a.p[i]));
-        s.x = wsum(s.x);
-        s.y = wsum(s.y);
-        if (lane == 0) sm.w[warp][q] = s;
+      // <V_q, p> for q <= j, four at a time so that the loads and the warp sums of the
+      // four overlap
+      for (int q0 = 0; q0 <= j; q0 += 4) {
+        double2 s[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) s[u] = make_double2(0.0, 0.0);
+        for (long long i = tid; i < n; i += nthreads) {
+          const double2 pi = a.p[i];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (q0 + u <= j) s[u] = cadd(s[u], cmulc(a.V[(long long)(q0 + u) * a.ldv + i], pi));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            s[u].x += __shfl_xor_sync(0xffffffffu, s[u].x, o);
+            s[u].y += __shfl_xor_sync(0xffffffffu, s[u].y, o);
+          }
+        }
+        if (lane == 0) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (q0 + u <= j) sm.w[warp][q0 + u] = s[u];
+        }
       }
       store_partials(sm, j + 1, pb);
       if (blockIdx.x == 0 && threadIdx.x == 0) ctl->alpha[j] = alpha;
@@ -656,8 +695,15 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
       {
         double s = 0.0;
         for (long long i = tid; i < n; i += nthreads) {
-          double2 x = a.p[i];
-          for (int q = 0; q <= j; ++q) x = csub(x, cmul(red[q], a.V[(long long)q * a.ldv + i]));
+          // p -= sum_q c_q V_q in two chains (even and odd q)
+          double2 x0 = a.p[i], x1 = make_double2(0.0, 0.0);
+          int q = 0;
+          for (; q + 2 <= j + 1; q += 2) {
+            x0 = csub(x0, cmul(red[q], a.V[(long long)q * a.ldv + i]));
+            x1 = csub(x1, cmul(red[q + 1], a.V[(long long)(q + 1) * a.ldv + i]));
+          }
+          if (q <= j) x0 = csub(x0, cmul(red[q], a.V[(long long)q * a.ldv + i]));
+          const double2 x = cadd(x0, x1);
           a.p[i] = x;
           s += x.x * x.x + x.y * x.y;
         }
@@ -693,13 +739,17 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
     }
     // ---- ||H V_m|| for the error estimate
     grid_barrier(a.bar, a.err);
-    run_program(a, a.V + (long long)m * a.ldv, tcp);
+    if (threadIdx.x == 0) s_mb = *(volatile int*)&ctl->mb;
+    __syncthreads();
+    const bool breakdown = s_mb < m;  // no error estimate after an exact breakdown
+    if (!breakdown) run_program(a, a.V + (long long)m * a.ldv, tcp);
     {
       double s = 0.0;
-      for (long long i = tid; i < n; i += nthreads) {
-        double2 v = a.p[i];
-        s += v.x * v.x + v.y * v.y;
-      }
+      if (!breakdown)
+        for (long long i = tid; i < n; i += nthreads) {
+          double2 v = a.p[i];
+          s += v.x * v.x + v.y * v.y;
+        }
       s = wsum(s);
       if (lane == 0) sm.w[warp][0] = make_double2(s, 0.0);
       store_partials(sm, 1, pa);

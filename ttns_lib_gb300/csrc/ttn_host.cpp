@@ -585,6 +585,7 @@ struct Integrator {
       bar = coop_buf.as<GridBarrier>();
       qr_scratch = (double*)(coop_buf.as<char>() + align256(sizeof(GridBarrier)));
       mixed = (cfg.precision == TTN_PREC_MIXED);
+      if (const char* e = std::getenv("TTN_EXPM_CTA_FLOPS")) expm_cta_flops = std::atof(e);
       expm_max_grid = std::max(1, expm_coop_max_grid(0));
       expm_max_grid_tc = std::max(1, expm_coop_max_grid(1));
       if (mixed) {
@@ -1029,8 +1030,17 @@ struct Integrator {
     prog_buf.alloc(all.size() * sizeof(MvOp) + 16);
     CK(cudaMemcpy(prog_buf.p, all.data(), all.size() * sizeof(MvOp), cudaMemcpyHostToDevice));
   }
-  int expm_grid(long long n, bool tc) const {
+  // CTAs of a Krylov launch: at most one per 64 vector elements and one per
+  // expm_cta_flops of matvec work.  Small problems run on few CTAs (one CTA synchronises
+  // with __syncthreads alone, several need grid barriers of a few microseconds each),
+  // large ones on the whole device.
+  double expm_cta_flops = 2.0e5;
+  int expm_grid(long long n, bool tc, double flops_per_app) const {
     long long g = (n + 63) / 64;
+    if (expm_cta_flops > 0.0) {
+      const long long gw = (long long)std::ceil(flops_per_app / expm_cta_flops);
+      if (gw < g) g = gw;
+    }
     if (g < 1) g = 1;
     const int mx = tc ? expm_max_grid_tc : expm_max_grid;
     if (g > mx) g = mx;
@@ -1054,7 +1064,7 @@ struct Integrator {
     a.apply_only = apply_only ? 1 : 0;
     a.phase = phase_dev;
     a.tc_img = tc_img_buf.as<uint32_t>();
-    CK(expm_coop(a, expm_grid(n, a.mixed), stream));
+    CK(expm_coop(a, expm_grid(n, a.mixed, a.flops_per_app), stream));
     // Lanczos vector passes of one sub-step (the matvec flops are tallied on the device)
     if (tally) flops += lanczos_vec_flops(n);
   }

@@ -578,8 +578,8 @@ struct Integrator {
     CK(cudaEventCreate(&ev1));
     {
       CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
-      qr_max_grid = std::max(1, std::min(coop_qr_max_grid(), num_sms));
-      size_t qb = align256(sizeof(GridBarrier)) + align256(coop_qr_scratch_bytes(qr_max_grid));
+      qr_max_grid = std::max(1, std::min(qr_blocked_max_grid(), num_sms));
+      size_t qb = align256(sizeof(GridBarrier)) + align256(qr_blocked_scratch_bytes(qr_max_grid));
       coop_buf.alloc(qb);
       CK(cudaMemset(coop_buf.p, 0, coop_buf.bytes));
       bar = coop_buf.as<GridBarrier>();
@@ -1110,7 +1110,7 @@ struct Integrator {
   // Householder QR on as many CTAs as the height allows (one row block per CTA)
   void qr(double2* M, long long m, int n, double2* R, int Rt) {
     int g = std::min(coop_qr_grid(m, num_sms), qr_max_grid);
-    CK(householder_qr_coop(M, m, n, R, Rt, qtau, qr_scratch, bar, status, g, stream));
+    CK(householder_qr_blocked(M, m, n, R, Rt, qtau, qr_scratch, bar, status, g, stream));
   }
   static double qr_flops(double m, double n) { return 2.0 * 8.0 * (m * n * n - n * n * n / 3.0); }
   void l2r(int nd, double2* A) {
@@ -1920,14 +1920,14 @@ int ttn_debug_qr(int m, int n, double* a, double* r, int device) {
   CK(cudaMemcpy(dA, a, (size_t)m * n * sizeof(double2), cudaMemcpyHostToDevice));
   int sms = 0;
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-  int g = std::min(ttn::coop_qr_grid(m, sms), std::max(1, std::min(ttn::coop_qr_max_grid(), sms)));
+  int g = std::min(ttn::coop_qr_grid(m, sms), std::max(1, std::min(ttn::qr_blocked_max_grid(), sms)));
   ttn::DevBuf cb;
-  cb.alloc(ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(ttn::coop_qr_scratch_bytes(g)) + 256);
+  cb.alloc(ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(ttn::qr_blocked_scratch_bytes(g)) + 256);
   CK(cudaMemset(cb.p, 0, cb.bytes));
   auto* bar = cb.as<ttn::GridBarrier>();
   double* scr = (double*)(cb.as<char>() + ttn::align256(sizeof(ttn::GridBarrier)));
-  int* err = (int*)(cb.as<char>() + ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(ttn::coop_qr_scratch_bytes(g)));
-  CK(ttn::householder_qr_coop(dA, m, n, dR, 0, dt, scr, bar, err, g, 0));
+  int* err = (int*)(cb.as<char>() + ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(ttn::qr_blocked_scratch_bytes(g)));
+  CK(ttn::householder_qr_blocked(dA, m, n, dR, 0, dt, scr, bar, err, g, 0));
   CK(cudaDeviceSynchronize());
   CK(cudaGetLastError());
   int herr = 0;

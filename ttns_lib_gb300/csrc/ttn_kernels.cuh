@@ -86,6 +86,12 @@ int coop_qr_grid(long long m, int num_sms);
 int coop_qr_max_grid();
 cudaError_t householder_qr_coop(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, double* scratch,
                                 GridBarrier* bar, int* err, int grid, cudaStream_t s);
+// Panel-blocked cooperative Householder QR (ttn_qr.cu), same conventions and arguments
+// as householder_qr_coop; scratch of qr_blocked_scratch_bytes(grid) bytes.
+size_t qr_blocked_scratch_bytes(int max_grid);
+int qr_blocked_max_grid();
+cudaError_t householder_qr_blocked(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws,
+                                   double* scratch, GridBarrier* bar, int* err, int grid, cudaStream_t s);
 // r2l matricisation: M(y*pre + x, i) = A((x*dm + i)*post + y) and its inverse.
 void permute_mode_last(const double2* A, double2* M, long long pre, int dm, long long post, cudaStream_t s);
 void unpermute_mode_last(const double2* M, double2* A, long long pre, int dm, long long post, cudaStream_t s);

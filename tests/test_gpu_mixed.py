@@ -1,11 +1,14 @@
-"""Mixed precision (split-TF32 tcgen05 contractions) against the oracle and the FP64 path.
+"""Mixed precision (tcgen05 tensor-core contractions on exact integer slices) against the
+oracle and the FP64 path.
 
-The mixed form runs the rank-64 mode and mean-field contractions of the Krylov matvec
-on the tensor cores with operands split into two TF32 parts and FP32 accumulation
-(relative error per contraction about 1e-7); everything else stays FP64.  Tolerances:
-one H_eff application within 5e-6 relative of the oracle, one node exponential within
-2e-5, and <sigma_z> after several sweeps within 1e-6 absolute of the FP64 device path,
-the accuracy bar the mixed form is measured at.
+The mixed form runs the rank-64 mode and mean-field contractions of the Krylov matvec and
+of the environment updates on the tensor cores: every FP64 operand row is scaled by a
+power of two and cut into six 7-bit integer slices, the slice products are accumulated
+exactly in FP32 level by level, and the levels are combined in integers, so a contraction
+is accurate to about 1e-13 relative to sum |a||b|.  Tolerances: one H_eff application
+within 1e-10 relative of the oracle, one node exponential within 1e-9, and <sigma_z> after
+several sweeps within 1e-8 of the FP64 device path (the mixed form is measured against
+max |d<sigma_z>| <= 1e-6).
 """
 import numpy as np
 import pytest
@@ -58,10 +61,11 @@ def test_mixed_program_apply_matches_oracle():
         ymx = its["mixed"][1].program_apply(node, v)
         assert rel(y64, ref) < 1e-12, node
         e = rel(ymx, ref)
-        assert e < 5e-6, (node, e)
-        if e > 1e-11:
+        assert e < 1e-10, (node, e)
+        if not np.array_equal(ymx, y64):
             n_tc += 1
-    # every interior node of bond dimension 64 ran contractions on the tensor cores
+    # every interior node of bond dimension 64 ran contractions on the tensor cores (its
+    # result differs in the last bits from the FP64 contractions)
     rank64 = sum(1 for i in range(topo.nnodes) if not topo.is_leaf(i) and topo.hrank[i] == 64)
     assert rank64 > 0 and n_tc >= rank64
 
@@ -79,7 +83,7 @@ def test_mixed_expm_node_matches_oracle():
     for node in range(2, topo.nnodes, 3):
         yo, _ = orc.expm_node(node, st[node], cfg["dt"])
         yd, _ = it.expm_node(node, st[node], cfg["dt"])
-        assert rel(yd, yo) < 2e-5, node
+        assert rel(yd, yo) < 1e-9, node
 
 
 def test_mixed_sweeps_track_fp64():
@@ -96,6 +100,6 @@ def test_mixed_sweeps_track_fp64():
             it(A, m.sop, -1j)
             sz[name] = it.mel()(sb.SZ, 0, A).real
         worst = max(worst, abs(sz["mixed"] - sz["fp64"]))
-    assert worst <= 1e-6, worst
+    assert worst <= 1e-8, worst
     A, it = its["mixed"]
-    assert abs(it.mel()(A) - 1.0) < 1e-6
+    assert abs(it.mel()(A) - 1.0) < 1e-10

@@ -121,86 +121,184 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
   }
 }
 
-// ---- tensor-core contractions (mixed precision)
+// ---- tensor-core contractions (mixed precision) at FP64 accuracy
 //
-// Both kinds are D(128 x 64) = A B^T per tile on split TF32 operands with FP32
-// accumulation in TMEM (columns 0-63: hi*hi, 64-127: hi*lo + lo*hi; Ootomo-Yokota):
-//   A (128 x 128) = real block form [[Re, -Im], [Im, Re]] of alpha * mat (64 x 64, row =
-//     output index, column = input index), the same for every tile of the op; built once
-//     per launch into a global image in the shared-memory operand layout and brought in
-//     by one bulk copy per op and CTA;
-//   B (64 x 128) = 64 input columns (real parts in k < 64, imaginary in k >= 64):
-//     MODE tile (aa, b0): in(aa, j, b0 + n) for n < 64;  MF tile x0: in(x0 + n, l).
-// Rows of D are (re/im, output index), columns the 64 tile positions n; the epilogue adds
-// the two accumulators in FP32, stages the tile in shared memory and writes coalesced
-// complex doubles (MODE: out(aa, i, b0 + n), MF: out(x0 + n, i)).
+// Both kinds are D(128 x 64) = A B^T per tile, A the real block form of alpha * mat
+// (64 x 64, row = output index, column = input index) and B 64 input columns n:
+//   MODE tile (aa, b0): in(aa, j, b0 + n);   MF tile x0: in(x0 + n, j)   (j < 64)
+// with K = 128 ordered k = 2 j + c (c = 0 real, 1 imaginary part of input j):
+//   A[(0,i)][(j,0)] = Re S, A[(0,i)][(j,1)] = -Im S, A[(1,i)][(j,0)] = Im S, A[(1,i)][(j,1)] = Re S.
+// Exact integer slices (the Ozaki splitting): every row of A and of B is scaled by a power
+// of two 2^E (E the smallest with all |x| < 2^E) and cut into six 7-bit integer slices,
+// x = 2^E sum_t s_t 2^(-7t) + O(2^(E-42)), each slice exact in TF32.  The products s_t s_u
+// (< 2^14) summed over K = 128 and over the at most 7 pairs of one level L = t + u stay
+// below 2^24, so each level is accumulated EXACTLY in FP32 TMEM (levels 2..8, 7 x 64
+// columns); the epilogue combines the levels in integers and scales by 2^(E_i + E_n - 56).
+// Error: the 42-bit truncation of the operands and the dropped levels >= 9, about 1e-13
+// relative to sum_k |A||B| (FP64 contractions: about 1e-16).  Operands arrive in 4 chunks
+// of 32 k (A: 6 slices x 16 KB by one bulk copy from the per-launch operator image; B:
+// sliced from the FP64 vector on the integer pipe), 104 MMAs per chunk.
 struct TcState {
-  uint32_t tmem;      // TMEM base (128 columns)
+  uint32_t tmem;      // TMEM base (512 columns)
   uint32_t phase;     // MMA mbarrier parity
   uint32_t lphase;    // bulk-load mbarrier parity
   uint64_t* mbar;
   uint64_t* lbar;
-  uint32_t* a;        // 128 x 128 tf32, hi then lo (kTcImageBytes)
-  uint32_t* b;        // 64 x 128 tf32, hi then lo; also the epilogue stage
+  uint32_t* a;        // A chunk: 6 slices x 128 x 32 tf32; also the epilogue stage
+  uint32_t* b;        // B chunk: 6 slices x 64 x 32 tf32
+  int* e_n;           // row exponents of the B tile
 };
-constexpr int TC_A_WORDS = 128 * 128, TC_B_WORDS = 64 * 128;
-constexpr int TC_STAGE_LD = 65;   // floats per staged row (padding against bank conflicts)
-constexpr size_t TC_SMEM = (size_t)(2 * TC_A_WORDS + 2 * TC_B_WORDS) * 4;
-static_assert(128 * TC_STAGE_LD * 4 <= 2 * TC_B_WORDS * 4, "epilogue stage must fit in the B buffer");
-static_assert(kTcImageBytes == 2 * TC_A_WORDS * 4, "image size");
+constexpr int TC_SLICES = 6;
+constexpr int TC_LEVELS = 7;                              // t + u = 2 .. 8
+constexpr int TC_CHUNK_K = 32;
+constexpr int TC_CHUNKS = 4;
+constexpr int TC_A_SLICE_WORDS = 128 * TC_CHUNK_K;        // 16 KB
+constexpr int TC_B_SLICE_WORDS = 64 * TC_CHUNK_K;         // 8 KB
+constexpr int TC_A_CHUNK_BYTES = TC_SLICES * TC_A_SLICE_WORDS * 4;
+constexpr int TC_B_CHUNK_BYTES = TC_SLICES * TC_B_SLICE_WORDS * 4;
+constexpr int TC_IMG_HDR = 1024;                          // int E_i[64], padded
+constexpr int TC_STAGE_LD = 65;                           // doubles per staged row
+constexpr size_t TC_SMEM = (size_t)TC_A_CHUNK_BYTES + TC_B_CHUNK_BYTES + 256;
+constexpr uint32_t TC_TMEM_COLS = 512;
+static_assert(kTcImageBytes == (size_t)TC_IMG_HDR + (size_t)TC_CHUNKS * TC_A_CHUNK_BYTES, "image size");
+static_assert(128 * TC_STAGE_LD * 8 <= TC_A_CHUNK_BYTES, "epilogue stage must fit in the A buffer");
+static_assert(TC_LEVELS * 64 <= (int)TC_TMEM_COLS, "TMEM columns");
 
-// operator images of every tensor-core op of the program (all CTAs, grid-stride)
+// smallest E with |x| < 2^E from the bits of |x| (x != 0)
+__device__ __forceinline__ int exp_bound_bits(unsigned long long absbits) {
+  const int e = (int)(absbits >> 52);
+  if (e != 0) return e - 1022;
+  return -1074 + (64 - __clzll((long long)absbits));
+}
+// six 7-bit slices of x relative to 2^Er (|x| < 2^Er), sign of x, as TF32 words
+__device__ __forceinline__ void slice6(double x, int Er, uint32_t* w) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  const unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
+  unsigned long long q = 0;
+  if (e != 0 || frac != 0) {
+    const unsigned long long m = e ? (frac | (1ull << 52)) : frac;
+    const int p = e ? e - 1075 : -1074;          // |x| = m 2^p
+    const int sh = Er - 42 - p;                  // q = floor(|x| 2^(42 - Er)) < 2^42
+    q = sh >= 64 ? 0ull : (sh >= 0 ? (m >> sh) : (m << (-sh)));
+  }
+  const bool neg = (b >> 63) != 0;
+#pragma unroll
+  for (int t = 0; t < TC_SLICES; ++t) {
+    const int v = (int)((q >> (35 - 7 * t)) & 127ull);
+    w[t] = __float_as_uint(__int2float_rn(neg ? -v : v));
+  }
+}
+// v * 2^e2 as a double from the bits (truncating below 53 bits; 0 below the normal range)
+__device__ __forceinline__ double i64_scaled(long long v, int e2) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+  const int msb = 63 - __clzll((long long)a);
+  const unsigned long long mant = msb > 52 ? (a >> (msb - 52)) : (a << (52 - msb));
+  const int ex = msb + e2 + 1023;
+  if (ex <= 0) return 0.0;
+  if (ex >= 2047) return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ull));
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+// operator images of every tensor-core op of the program (all CTAs, one warp per row i)
 __device__ void build_tc_images(const ExpmArgs& a) {
-  const long long nthreads = (long long)gridDim.x * blockDim.x;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  for (int k = 0; k < a.nops; ++k) {
-    const MvOp& op = a.prog[k];
-    if (!op.tc) continue;
-    uint32_t* img = a.tc_img + (size_t)op.img * (2 * TC_A_WORDS);
-    for (long long e = tid; e < 64 * 64; e += nthreads) {
-      const int i = (int)(e / 64), j = (int)(e % 64);
-      const double2 sv = cmul(op.alpha, op.mat[e]);
-      const float re = tc::f64_to_f32_int(sv.x), im = tc::f64_to_f32_int(sv.y);
-      uint32_t h, l;
-      tc::split_tf32_f(re, h, l);
-      img[tc::tf32_offset(i, j, 128) / 4] = h;
-      img[TC_A_WORDS + tc::tf32_offset(i, j, 128) / 4] = l;
-      img[tc::tf32_offset(64 + i, 64 + j, 128) / 4] = h;
-      img[TC_A_WORDS + tc::tf32_offset(64 + i, 64 + j, 128) / 4] = l;
-      tc::split_tf32_f(im, h, l);
-      img[tc::tf32_offset(64 + i, j, 128) / 4] = h;
-      img[TC_A_WORDS + tc::tf32_offset(64 + i, j, 128) / 4] = l;
-      tc::split_tf32_f(-im, h, l);
-      img[tc::tf32_offset(i, 64 + j, 128) / 4] = h;
-      img[TC_A_WORDS + tc::tf32_offset(i, 64 + j, 128) / 4] = l;
+  const int lane = threadIdx.x & 31;
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int ntc = 0;
+  for (int k = 0; k < a.nops; ++k) ntc += a.prog[k].tc ? 1 : 0;
+  for (long long task = gw; task < (long long)ntc * 64; task += nwarps) {
+    int which = (int)(task / 64);
+    const int i = (int)(task % 64);
+    const MvOp* opp = nullptr;
+    for (int k = 0; k < a.nops; ++k)
+      if (a.prog[k].tc && which-- == 0) {
+        opp = &a.prog[k];
+        break;
+      }
+    const MvOp& op = *opp;
+    unsigned char* img = reinterpret_cast<unsigned char*>(a.tc_img) + (size_t)op.img * kTcImageBytes;
+    double2 sv[2];
+    unsigned long long mx = 0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      sv[h] = cmul(op.alpha, op.mat[i * 64 + lane + 32 * h]);
+      const unsigned long long ar = (unsigned long long)__double_as_longlong(sv[h].x) & 0x7FFFFFFFFFFFFFFFull;
+      const unsigned long long ai = (unsigned long long)__double_as_longlong(sv[h].y) & 0x7FFFFFFFFFFFFFFFull;
+      mx = ar > mx ? ar : mx;
+      mx = ai > mx ? ai : mx;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
+      mx = t > mx ? t : mx;
+    }
+    const int Er = mx ? exp_bound_bits(mx) : 0;
+    if (lane == 0) reinterpret_cast<int*>(img)[i] = Er;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int j = lane + 32 * h;
+      const int q = j / 16, kc = 2 * (j % 16);
+      uint32_t* chunk = reinterpret_cast<uint32_t*>(img + TC_IMG_HDR + (size_t)q * TC_A_CHUNK_BYTES);
+      uint32_t wr[TC_SLICES], wi[TC_SLICES], wn[TC_SLICES];
+      slice6(sv[h].x, Er, wr);
+      slice6(sv[h].y, Er, wi);
+      slice6(-sv[h].y, Er, wn);
+#pragma unroll
+      for (int t = 0; t < TC_SLICES; ++t) {
+        uint32_t* sl = chunk + t * TC_A_SLICE_WORDS;
+        sl[tc::tf32_offset(i, kc, 128) / 4] = wr[t];           // (re out, re in)
+        sl[tc::tf32_offset(i, kc + 1, 128) / 4] = wn[t];       // (re out, im in)
+        sl[tc::tf32_offset(64 + i, kc, 128) / 4] = wi[t];      // (im out, re in)
+        sl[tc::tf32_offset(64 + i, kc + 1, 128) / 4] = wr[t];  // (im out, im in)
+      }
     }
   }
   // the images are read by bulk copies (async proxy) after the next grid barrier
   tc::fence_proxy_async_all();
 }
 
-// stage the B tile: thread task (n, j4) converts in[n-th column, k = 4 j4 .. 4 j4 + 3]
-// (element offset src(n, j) = base + n * sn + j * sj) into 16-byte core-matrix rows
-__device__ __forceinline__ void tc_stage_b(const TcState& t, const double2* base, long long sn, long long sj) {
-  for (int task = threadIdx.x; task < 64 * 16; task += blockDim.x) {
-    const int n = task & 63, j4 = task >> 6;
-    uint32_t rh[4], rl[4], ih[4], il[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const double2 v = base[(long long)n * sn + (long long)(4 * j4 + q) * sj];
-      tc::split_tf32_f(tc::f64_to_f32_int(v.x), rh[q], rl[q]);
-      tc::split_tf32_f(tc::f64_to_f32_int(v.y), ih[q], il[q]);
+// row exponents of the B tile: 4 threads per row n, 16 inputs each
+__device__ __forceinline__ void tc_b_exponents(const TcState& t, const double2* base, long long sn, long long sj) {
+  const int n = threadIdx.x >> 2, part = threadIdx.x & 3;
+  unsigned long long mx = 0;
+  if (n < 64) {
+    for (int j = 16 * part; j < 16 * part + 16; ++j) {
+      const double2 v = base[(long long)n * sn + (long long)j * sj];
+      const unsigned long long ar = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+      const unsigned long long ai = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+      mx = ar > mx ? ar : mx;
+      mx = ai > mx ? ai : mx;
     }
-    const uint32_t ore = tc::tf32_offset(n, 4 * j4, 64) / 4, oim = tc::tf32_offset(n, 64 + 4 * j4, 64) / 4;
-    *reinterpret_cast<uint4*>(t.b + ore) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
-    *reinterpret_cast<uint4*>(t.b + TC_B_WORDS + ore) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
-    *reinterpret_cast<uint4*>(t.b + oim) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
-    *reinterpret_cast<uint4*>(t.b + TC_B_WORDS + oim) = make_uint4(il[0], il[1], il[2], il[3]);
+  }
+#pragma unroll
+  for (int o = 1; o < 4; o <<= 1) {
+    const unsigned long long u = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = u > mx ? u : mx;
+  }
+  if (n < 64 && part == 0) t.e_n[n] = mx ? exp_bound_bits(mx) : 0;
+  __syncthreads();
+}
+
+// slices of chunk q of the B tile (inputs j = 16 q .. 16 q + 15) into shared memory
+__device__ __forceinline__ void tc_stage_b(const TcState& t, const double2* base, long long sn, long long sj, int q) {
+  for (int task = threadIdx.x; task < 64 * 16; task += blockDim.x) {
+    const int n = task & 63, jj = task >> 6;
+    const double2 v = base[(long long)n * sn + (long long)(16 * q + jj) * sj];
+    const int Er = t.e_n[n];
+    uint32_t wr[TC_SLICES], wi[TC_SLICES];
+    slice6(v.x, Er, wr);
+    slice6(v.y, Er, wi);
+    const uint32_t o = tc::tf32_offset(n, 2 * jj, 64) / 4;  // k = 2 jj and 2 jj + 1 are adjacent words
+#pragma unroll
+    for (int s = 0; s < TC_SLICES; ++s) *reinterpret_cast<uint2*>(t.b + s * TC_B_SLICE_WORDS + o) = make_uint2(wr[s], wi[s]);
   }
 }
 
-// issue the 48 MMAs of one tile and wait for them; false on a timed-out wait
-__device__ bool tc_tile_mma(TcState& t) {
+// MMAs of one chunk (26 slice pairs x 4 k-steps) and wait for them; false on a timed-out wait
+__device__ bool tc_chunk_mma(TcState& t, int q) {
   tc::fence_proxy_async();
   tc::fence_before();
   __syncthreads();
@@ -208,17 +306,19 @@ __device__ bool tc_tile_mma(TcState& t) {
   if (threadIdx.x == 0) {
     const uint32_t idesc = tc::idesc_tf32(128, 64);
     const uint32_t lboA = 16 * 128, lboB = 8 * 128, sbo = 128;
-    const uint32_t a_hi = tc::smem_u32(t.a), a_lo = a_hi + TC_A_WORDS * 4;
-    const uint32_t b_hi = tc::smem_u32(t.b), b_lo = b_hi + TC_B_WORDS * 4;
-    for (int kk = 0; kk < 16; ++kk) {
+    const uint32_t a0 = tc::smem_u32(t.a), b0 = tc::smem_u32(t.b);
+    for (int kk = 0; kk < TC_CHUNK_K / 8; ++kk) {
       const uint32_t offA = (uint32_t)kk * 2 * 16 * 128, offB = (uint32_t)kk * 2 * 8 * 128;
-      const uint64_t ah = tc::smem_desc(a_hi + offA, lboA, sbo);
-      const uint64_t al = tc::smem_desc(a_lo + offA, lboA, sbo);
-      const uint64_t bh = tc::smem_desc(b_hi + offB, lboB, sbo);
-      const uint64_t bl = tc::smem_desc(b_lo + offB, lboB, sbo);
-      tc::mma_tf32(t.tmem, ah, bh, idesc, kk > 0);
-      tc::mma_tf32(t.tmem + 64, ah, bl, idesc, kk > 0);
-      tc::mma_tf32(t.tmem + 64, al, bh, idesc, 1);
+      for (int s = 0; s < TC_SLICES; ++s)
+        for (int u = 0; u < TC_SLICES; ++u) {
+          const int L = s + u;  // level - 2
+          if (L >= TC_LEVELS) continue;
+          const uint64_t ad = tc::smem_desc(a0 + (uint32_t)s * TC_A_SLICE_WORDS * 4 + offA, lboA, sbo);
+          const uint64_t bd = tc::smem_desc(b0 + (uint32_t)u * TC_B_SLICE_WORDS * 4 + offB, lboB, sbo);
+          // the first product into a level starts it: chunk 0, k-step 0, and s = 0 or u = L
+          const bool first = (q == 0 && kk == 0 && (s == (L < TC_SLICES ? 0 : L - TC_SLICES + 1)));
+          tc::mma_tf32(t.tmem + 64u * (uint32_t)L, ad, bd, idesc, first ? 0u : 1u);
+        }
     }
     tc::mma_commit(t.mbar);
   }
@@ -229,17 +329,28 @@ __device__ bool tc_tile_mma(TcState& t) {
   return ok;
 }
 
-// TMEM -> stage (float [128][TC_STAGE_LD], in the B buffer) by warps 0-3, one row each
-__device__ __forceinline__ void tc_drain_to_stage(const TcState& t) {
+// TMEM -> stage (double [128][TC_STAGE_LD], in the A buffer) by warps 0-3, one row each:
+// exact integer combination of the 7 levels, scaled by 2^(E_i + E_n - 56)
+__device__ __forceinline__ void tc_drain_to_stage(const TcState& t, int Ei) {
   const int warp = threadIdx.x >> 5;
   if (warp < 4) {
-    float* row = reinterpret_cast<float*>(t.b) + threadIdx.x * TC_STAGE_LD;
-    for (int c0 = 0; c0 < 64; c0 += 16) {
-      float mv[16], cv[16];
-      tc::tmem_ld16(t.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, mv);
-      tc::tmem_ld16(t.tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(64 + c0), cv);
+    double* row = reinterpret_cast<double*>(t.a) + threadIdx.x * TC_STAGE_LD;
+    const uint32_t lane_base = t.tmem + ((uint32_t)(32 * warp) << 16);
+    for (int c0 = 0; c0 < 64; c0 += 8) {
+      float f[TC_LEVELS][8];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) row[c0 + q] = mv[q] + cv[q];
+      for (int L = 0; L < TC_LEVELS; ++L) tc::tmem_ld8_nowait(lane_base + 64u * L + (uint32_t)c0, f[L]);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        // levels 2,3 -> hi (scale 2^35 relative to lo); levels 4..8 -> lo
+        const long long hi = (long long)__float2int_rn(f[0][c]) * 128 + (long long)__float2int_rn(f[1][c]);
+        long long lo = 0;
+#pragma unroll
+        for (int L = 2; L < TC_LEVELS; ++L) lo += (long long)__float2int_rn(f[L][c]) << (7 * (TC_LEVELS - 1 - L));
+        const int e2 = Ei + t.e_n[c0 + c] - 56;
+        row[c0 + c] = i64_scaled(hi, e2 + 35) + i64_scaled(lo, e2);
+      }
     }
   }
   tc::fence_before();
@@ -254,31 +365,37 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
   const long long nb = op.nb;
   const long long tiles = mode ? op.na * (nb / 64) : op.na / 64;
   if ((long long)blockIdx.x >= tiles) return;
-  // operator image -> shared memory (one bulk copy), overlapped with the first B tile
-  if (threadIdx.x == 0) {
-    tc::fence_proxy_async_all();
-    tc::mbar_expect_tx(t.lbar, (uint32_t)kTcImageBytes);
-    tc::bulk_g2s(t.a, a.tc_img + (size_t)op.img * (2 * TC_A_WORDS), (uint32_t)kTcImageBytes, t.lbar);
-  }
-  bool loaded = false;
-  const float* stage = reinterpret_cast<const float*>(t.b);
+  const unsigned char* img = reinterpret_cast<const unsigned char*>(a.tc_img) + (size_t)op.img * kTcImageBytes;
+  const int Ei = (threadIdx.x < 128) ? reinterpret_cast<const int*>(img)[threadIdx.x & 63] : 0;
+  const double* stage = reinterpret_cast<const double*>(t.a);
   for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    long long aa = 0, b0 = 0;
+    long long aa = 0, b0 = 0, sn, sj;
+    const double2* base;
     if (mode) {
       aa = tile / (nb / 64);
       b0 = (tile % (nb / 64)) * 64;
-      tc_stage_b(t, in + aa * 64 * nb + b0, 1, nb);
+      base = in + aa * 64 * nb + b0;
+      sn = 1;
+      sj = nb;
     } else {
       b0 = tile * 64;
-      tc_stage_b(t, in + b0 * 64, 64, 1);
+      base = in + b0 * 64;
+      sn = 64;
+      sj = 1;
     }
-    if (!loaded) {
+    tc_b_exponents(t, base, sn, sj);
+    for (int q = 0; q < TC_CHUNKS; ++q) {
+      if (threadIdx.x == 0) {
+        tc::fence_proxy_async_all();
+        tc::mbar_expect_tx(t.lbar, (uint32_t)TC_A_CHUNK_BYTES);
+        tc::bulk_g2s(t.a, img + TC_IMG_HDR + (size_t)q * TC_A_CHUNK_BYTES, (uint32_t)TC_A_CHUNK_BYTES, t.lbar);
+      }
+      tc_stage_b(t, base, sn, sj, q);
       if (!tc::mbar_wait(t.lbar, t.lphase) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
       t.lphase ^= 1u;
-      loaded = true;
+      if (!tc_chunk_mma(t, q) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
     }
-    if (!tc_tile_mma(t) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
-    tc_drain_to_stage(t);
+    tc_drain_to_stage(t, Ei);
     // stage -> out: element (i, n) = (stage[i][n], stage[64 + i][n])
     for (int task = threadIdx.x; task < 64 * 64; task += blockDim.x) {
       int i, n;
@@ -292,11 +409,12 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
         n = task >> 6;
         dst = out + (b0 + n) * 64 + i;
       }
-      double2 v = make_double2(tc::f32_to_f64_int(stage[i * TC_STAGE_LD + n]),
-                               tc::f32_to_f64_int(stage[(64 + i) * TC_STAGE_LD + n]));
+      double2 v = make_double2(stage[i * TC_STAGE_LD + n], stage[(64 + i) * TC_STAGE_LD + n]);
       if (acc) v = cadd(v, *dst);
       *dst = v;
     }
+    // the next tile's bulk copy (async proxy) overwrites the stage just read
+    tc::fence_proxy_async_all();
     __syncthreads();
   }
 }
@@ -308,6 +426,7 @@ __device__ void run_program(const ExpmArgs& a, const double2* x, TcState* t) {
     if (op.tc && t) run_op_tc(a, op, x, *t);
     else run_op(a, op, x);
   }
+  if (a.tail_barrier) grid_barrier(a.bar, a.err);
 }
 
 // ---- reductions: partials [gridDim][nq] (complex), reduced by every CTA in block order
@@ -524,7 +643,7 @@ __device__ void control(const ExpmArgs& a, CtlSmem& S) {
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
+__global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
   __shared__ Red sm;
   __shared__ double2 red[EQ];
   __shared__ int s_done, s_mb;
@@ -532,9 +651,17 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
   __shared__ __align__(8) uint64_t s_lbar;
   __shared__ uint32_t s_tmem;
   extern __shared__ __align__(1024) unsigned char dsm[];
+  __shared__ MvOp s_op1;
   // the controller's scratch and the tensor-core operands share the dynamic buffer: they
   // are used in different phases
   CtlSmem& cs = *reinterpret_cast<CtlSmem*>(dsm);
+  // a single contraction passed by value runs from a shared-memory copy
+  ExpmArgs a = a_in;
+  if (a.prog == nullptr) {
+    if (threadIdx.x == 0) s_op1 = a_in.op1;
+    __syncthreads();
+    a.prog = &s_op1;
+  }
   TcState tcs;
   TcState* tcp = nullptr;
   if (a.mixed) {
@@ -543,7 +670,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
       tc::mbar_init(&s_lbar, 1);
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&s_tmem, 128);
+    if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&s_tmem, TC_TMEM_COLS);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
@@ -553,7 +680,8 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
     tcs.mbar = &s_mbar;
     tcs.lbar = &s_lbar;
     tcs.a = reinterpret_cast<uint32_t*>(dsm);
-    tcs.b = tcs.a + 2 * TC_A_WORDS;
+    tcs.b = reinterpret_cast<uint32_t*>(dsm + TC_A_CHUNK_BYTES);
+    tcs.e_n = reinterpret_cast<int*>(dsm + TC_A_CHUNK_BYTES + TC_B_CHUNK_BYTES);
     tcp = &tcs;
     build_tc_images(a);
   }
@@ -783,7 +911,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a) {
     __syncthreads();
     if ((threadIdx.x >> 5) == 0) {
       tc::fence_after();
-      tc::tmem_dealloc(tcs.tmem, 128);
+      tc::tmem_dealloc(tcs.tmem, TC_TMEM_COLS);
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0 && !a.apply_only) {

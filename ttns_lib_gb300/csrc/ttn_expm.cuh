@@ -27,8 +27,9 @@ struct MvOp {
   int img;   // tensor-core ops: slot of the operator image (split TF32 block form of alpha mat)
   double2 alpha;
 };
-// bytes of one operator image: a 128 x 128 TF32 operand, high and low parts
-constexpr size_t kTcImageBytes = (size_t)2 * 128 * 128 * 4;
+// bytes of one operator image: row exponents (1 KB) and the 128 x 128 block operand as
+// six TF32 integer slices in four K-chunks of 96 KB
+constexpr size_t kTcImageBytes = (size_t)1024 + (size_t)4 * 6 * 128 * 32 * 4;
 
 struct ExpmArgs {
   double2* y;            // vector evolved in place
@@ -51,6 +52,10 @@ struct ExpmArgs {
   int apply_only;        // 1: apply the program once to y (result in p) and return
   unsigned long long* phase;  // optional: ns spent per phase as seen by CTA 0 (kPhases slots)
   uint32_t* tc_img;      // operator images of the tensor-core ops (kTcImageBytes each)
+  MvOp op1;              // the program when prog is null (one contraction, apply_only)
+  int tail_barrier;      // 1: a grid barrier after the program (tensor-core writes to p
+                         // are distributed by tiles, not by the element-wise ownership the
+                         // Lanczos passes assume)
 };
 constexpr int kPhases = 10;  // begin, matvec, alpha, reorth coefficients, reorth + norm,
                              // ||H V_m||, control, combine, sub-steps, launches

@@ -407,6 +407,7 @@ struct Integrator {
   int num_sms = 0, qr_max_grid = 1, expm_max_grid = 1, expm_max_grid_tc = 1;
   bool mixed = false;                      // tensor-core contractions in the matvec programs
   std::vector<char> heff_tc, kbond_tc;     // program contains tensor-core contractions
+  std::vector<char> heff_tail, kbond_tail; // program needs a barrier after it
   int max_tc_images = 0;                   // most tensor-core ops in one program
   DevBuf tc_img_buf;                       // their operator images (kTcImageBytes each)
   // compiled matrix-vector programs for the persistent Krylov kernel
@@ -599,7 +600,7 @@ struct Integrator {
       flops_dev = (double*)(expm_part_buf.as<char>() + expm_partial_bytes(expm_max_grid) + 256);
       CK(cudaMemset(expm_part_buf.p, 0, expm_part_buf.bytes));
       compile_programs();
-      if (max_tc_images > 0) tc_img_buf.alloc((size_t)max_tc_images * kTcImageBytes);
+      if (mixed) tc_img_buf.alloc((size_t)std::max(1, max_tc_images) * kTcImageBytes);
     }
 
     CK(cudaStreamSynchronize(stream));
@@ -613,11 +614,35 @@ struct Integrator {
     d = T.dims[nd][mu];
     for (int i = mu + 1; i < T.nmodes[nd]; ++i) nb *= T.dims[nd][i];
   }
+  // One mode or mean-field product on the tensor cores (mixed precision, eligible
+  // shapes): the persistent kernel's apply-only path with a one-contraction program.
+  bool tc_apply(int kind, const double2* mat, const double2* in, double2* out, long long na, int d, long long nb,
+                cd alpha, bool acc) {
+    if (!mixed || !tc_eligible(kind, d, na, nb)) return false;
+    ExpmArgs a{};
+    a.y = const_cast<double2*>(in); a.p = out; a.n = 0;
+    a.V = V; a.ldv = ldv; a.t1 = w1; a.t2 = w2; a.t3 = w3;
+    a.prog = nullptr; a.nops = 1;
+    MvOp& o = a.op1;
+    o.kind = kind; o.in = 0; o.out = 1; o.mat = mat; o.na = na; o.d = d; o.nb = nb;
+    o.alpha = d2(alpha); o.beta = acc ? 1 : 0; o.tc = 1; o.img = 0; o.barrier_before = 0;
+    a.part = expm_part_buf.as<double2>();
+    a.ctl = ctl; a.bar = bar; a.err = status;
+    a.m = cfg.krylov_dim; a.tau = 0.0; a.cf_re = 0.0; a.cf_im = -1.0; a.tol = cfg.krylov_tol;
+    a.mixed = 1; a.apply_only = 1; a.phase = nullptr;
+    a.tc_img = tc_img_buf.as<uint32_t>();
+    const long long tiles = kind == MV_MODE ? na * (nb / 64) : na / 64;
+    const int grid = (int)std::max(1LL, std::min<long long>(tiles, expm_max_grid_tc));
+    CK(expm_coop(a, grid, stream));
+    return true;
+  }
   // out(a,i,b) = alpha sum_j S(i,j) in(a,j,b) (+ out)
+  // (allow_tc = false keeps a product in FP64 in mixed precision: the gauge moves, which
+  // change the state itself, always run in FP64)
   void mode_apply(const double2* S, int d, const double2* in, double2* out, long long na, long long nb, cd alpha,
-                  bool acc) {
+                  bool acc, bool allow_tc = true) {
     flops += 8.0 * na * (double)d * d * nb;
-    if (tc && tc_mode_apply(tc, S, d, in, out, na, nb, d2(alpha), acc, stream)) return;
+    if (allow_tc && tc_apply(MV_MODE, S, in, out, na, d, nb, alpha, acc)) return;
     ZGemm g{};
     g.M = d; g.N = (int)nb; g.K = d;
     g.A = op_rowmajor(S, d);
@@ -632,7 +657,7 @@ struct Integrator {
   // out(x,k) = alpha sum_l in(x,l) M(k,l) (+ out)
   void mf_apply(const double2* in, const double2* M, int r, long long nx, double2* out, cd alpha, bool acc) {
     flops += 8.0 * nx * (double)r * r;
-    if (tc && tc_mf_apply(tc, in, M, r, nx, out, d2(alpha), acc, stream)) return;
+    if (tc_apply(MV_MF, M, in, out, nx, r, 0, alpha, acc)) return;
     ZGemm g{};
     g.M = (int)nx; g.N = r; g.K = r;
     g.A = op_rowmajor(in, r);
@@ -1010,7 +1035,17 @@ struct Integrator {
     std::vector<MvOp> all;
     heff_off.assign(T.n, 0); heff_n.assign(T.n, 0); kbond_off.assign(T.n, 0); kbond_n.assign(T.n, 0);
     heff_tc.assign(T.n, 0); kbond_tc.assign(T.n, 0);
+    heff_tail.assign(T.n, 0); kbond_tail.assign(T.n, 0);
     max_tc_images = 0;
+    // a tensor-core op wrote the result buffer (1) after the program's last barrier
+    auto tail_needed = [](const std::vector<MvOp>& ops) {
+      bool pending = false;
+      for (const auto& o : ops) {
+        if (o.barrier_before) pending = false;
+        if (o.tc && o.out == 1) pending = true;
+      }
+      return pending;
+    };
     auto mark = [&](const std::vector<MvOp>& ops) {
       int n = 0;
       for (const auto& o : ops) n += o.tc ? 1 : 0;
@@ -1020,10 +1055,12 @@ struct Integrator {
     for (int i = 0; i < T.n; ++i) {
       auto h = heff_program(i);
       heff_tc[i] = mark(h);
+      heff_tail[i] = tail_needed(h);
       heff_off[i] = (int)all.size(); heff_n[i] = (int)h.size();
       all.insert(all.end(), h.begin(), h.end());
       auto k = kbond_program(i);
       kbond_tc[i] = mark(k);
+      kbond_tail[i] = tail_needed(k);
       kbond_off[i] = (int)all.size(); kbond_n[i] = (int)k.size();
       all.insert(all.end(), k.begin(), k.end());
     }
@@ -1061,6 +1098,7 @@ struct Integrator {
     a.flops_per_app = (kind == 0) ? heff_flops(nd) : kbond_flops(nd);
     a.m = cfg.krylov_dim; a.tau = tau; a.cf_re = cf.real(); a.cf_im = cf.imag(); a.tol = cfg.krylov_tol;
     a.mixed = (kind == 0 ? heff_tc[nd] : kbond_tc[nd]) ? 1 : 0;
+    a.tail_barrier = (kind == 0 ? heff_tail[nd] : kbond_tail[nd]) ? 1 : 0;
     a.apply_only = apply_only ? 1 : 0;
     a.phase = phase_dev;
     a.tc_img = tc_img_buf.as<uint32_t>();
@@ -1125,7 +1163,7 @@ struct Integrator {
     long long na, nb;
     int d;
     r3(p, T.slot[nd], na, d, nb);
-    mode_apply(rmat[nd], d, Ap, w4, na, nb, 1.0, false);
+    mode_apply(rmat[nd], d, Ap, w4, na, nb, 1.0, false, false);
     zcopy(Ap, w4, T.size(p), stream);
   }
   void r2l(int nd, int mu, double2* A) {
@@ -1267,6 +1305,7 @@ struct Integrator {
   }
 
   // ---------------------------------------------------------------- observables
+  // (always FP64, also in mixed precision)
   cd expect(ttn_state* S, int mode, const double2* op_dev) {
     for (int id = T.n - 1; id >= 0; --id) {
       const int r = T.hrank[id];
@@ -1275,7 +1314,7 @@ struct Integrator {
       const double2* X = A;
       if (T.leaf(id)) {
         if (op_dev && T.leaf_mode[id] == mode) {
-          mode_apply(op_dev, T.dims[id][0], A, w1, 1, r, 1.0, false);
+          mode_apply(op_dev, T.dims[id][0], A, w1, 1, r, 1.0, false, false);
           X = w1;
         }
       } else {
@@ -1285,7 +1324,7 @@ struct Integrator {
           long long na, nb;
           int d;
           r3(id, s, na, d, nb);
-          mode_apply(mel[T.children[id][s]], d, cur, nxt, na, nb, 1.0, false);
+          mode_apply(mel[T.children[id][s]], d, cur, nxt, na, nb, 1.0, false, false);
           cur = nxt;
           nxt = (nxt == w1) ? w2 : w1;
         }

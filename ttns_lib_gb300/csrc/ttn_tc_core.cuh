@@ -143,6 +143,17 @@ __device__ __forceinline__ void split_tf32_f(float x, uint32_t& hi, uint32_t& lo
   lo = to_tf32(x - __uint_as_float(hi));
 }
 
+// ---- TMEM -> registers: 8 consecutive fp32 columns, no wait (pair with tmem_wait_ld)
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 // ---- TMEM -> registers: 16 consecutive fp32 columns of this warp's 32 lanes
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];

@@ -139,29 +139,29 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
 // of 32 k (A: 6 slices x 16 KB by one bulk copy from the per-launch operator image; B:
 // sliced from the FP64 vector on the integer pipe), 104 MMAs per chunk.
 struct TcState {
-  uint32_t tmem;      // TMEM base (512 columns)
-  uint32_t phase;     // MMA mbarrier parity
-  uint32_t lphase;    // bulk-load mbarrier parity
-  uint64_t* mbar;
-  uint64_t* lbar;
-  uint32_t* a;        // A chunk: 6 slices x 128 x 32 tf32; also the epilogue stage
-  uint32_t* b;        // B chunk: 6 slices x 64 x 32 tf32
-  int* e_n;           // row exponents of the B tile
+  uint32_t tmem;          // TMEM base (512 columns)
+  uint32_t mph[2];        // MMA mbarrier parities
+  uint32_t lph[2];        // bulk-load mbarrier parities
+  uint64_t* mbar;         // [2] MMA completion, one per operand buffer
+  uint64_t* lbar;         // [2] bulk-load completion
+  unsigned char* a[2];    // A chunk buffers: 6 slices x 128 x 32 bf16; both together the epilogue stage
+  unsigned char* b[2];    // B chunk buffers: 6 slices x 64 x 32 bf16
+  int* e_n;               // row exponents of the B tile
 };
 constexpr int TC_SLICES = 6;
 constexpr int TC_LEVELS = 7;                              // t + u = 2 .. 8
 constexpr int TC_CHUNK_K = 32;
 constexpr int TC_CHUNKS = 4;
-constexpr int TC_A_SLICE_WORDS = 128 * TC_CHUNK_K;        // 16 KB
-constexpr int TC_B_SLICE_WORDS = 64 * TC_CHUNK_K;         // 8 KB
-constexpr int TC_A_CHUNK_BYTES = TC_SLICES * TC_A_SLICE_WORDS * 4;
-constexpr int TC_B_CHUNK_BYTES = TC_SLICES * TC_B_SLICE_WORDS * 4;
+constexpr int TC_A_SLICE_BYTES = 128 * TC_CHUNK_K * 2;    // 8 KB
+constexpr int TC_B_SLICE_BYTES = 64 * TC_CHUNK_K * 2;     // 4 KB
+constexpr int TC_A_CHUNK_BYTES = TC_SLICES * TC_A_SLICE_BYTES;
+constexpr int TC_B_CHUNK_BYTES = TC_SLICES * TC_B_SLICE_BYTES;
 constexpr int TC_IMG_HDR = 1024;                          // int E_i[64], padded
 constexpr int TC_STAGE_LD = 65;                           // doubles per staged row
-constexpr size_t TC_SMEM = (size_t)TC_A_CHUNK_BYTES + TC_B_CHUNK_BYTES + 256;
+constexpr size_t TC_SMEM = (size_t)2 * (TC_A_CHUNK_BYTES + TC_B_CHUNK_BYTES) + 256;
 constexpr uint32_t TC_TMEM_COLS = 512;
 static_assert(kTcImageBytes == (size_t)TC_IMG_HDR + (size_t)TC_CHUNKS * TC_A_CHUNK_BYTES, "image size");
-static_assert(128 * TC_STAGE_LD * 8 <= TC_A_CHUNK_BYTES, "epilogue stage must fit in the A buffer");
+static_assert(128 * TC_STAGE_LD * 8 <= 2 * TC_A_CHUNK_BYTES, "epilogue stage must fit in the A buffers");
 static_assert(TC_LEVELS * 64 <= (int)TC_TMEM_COLS, "TMEM columns");
 
 // smallest E with |x| < 2^E from the bits of |x| (x != 0)
@@ -170,7 +170,8 @@ __device__ __forceinline__ int exp_bound_bits(unsigned long long absbits) {
   if (e != 0) return e - 1022;
   return -1074 + (64 - __clzll((long long)absbits));
 }
-// six 7-bit slices of x relative to 2^Er (|x| < 2^Er), sign of x, as TF32 words
+// the six 7-bit slices of x relative to 2^Er (|x| < 2^Er), with the sign of x, as bf16
+// (integers of at most 7 bits are exact in bf16)
 __device__ __forceinline__ void slice6(double x, int Er, uint32_t* w) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const int e = (int)((b >> 52) & 0x7FF);
@@ -186,7 +187,7 @@ __device__ __forceinline__ void slice6(double x, int Er, uint32_t* w) {
 #pragma unroll
   for (int t = 0; t < TC_SLICES; ++t) {
     const int v = (int)((q >> (35 - 7 * t)) & 127ull);
-    w[t] = __float_as_uint(__int2float_rn(neg ? -v : v));
+    w[t] = __float_as_uint(__int2float_rn(neg ? -v : v)) >> 16;
   }
 }
 // v * 2^e2 as a double from the bits (truncating below 53 bits; 0 below the normal range)
@@ -202,7 +203,9 @@ __device__ __forceinline__ double i64_scaled(long long v, int e2) {
   return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
-// operator images of every tensor-core op of the program (all CTAs, one warp per row i)
+// operator images of every tensor-core op of the program (all CTAs, one warp per row i):
+// [int E_i[64]] then 4 chunks x 6 slices of the 128 x 32 bf16 operand, k = 2 j + c packed
+// in pairs (real, imaginary input part) per 32-bit word
 __device__ void build_tc_images(const ExpmArgs& a) {
   const int lane = threadIdx.x & 31;
   const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
@@ -241,18 +244,16 @@ __device__ void build_tc_images(const ExpmArgs& a) {
     for (int h = 0; h < 2; ++h) {
       const int j = lane + 32 * h;
       const int q = j / 16, kc = 2 * (j % 16);
-      uint32_t* chunk = reinterpret_cast<uint32_t*>(img + TC_IMG_HDR + (size_t)q * TC_A_CHUNK_BYTES);
+      unsigned char* chunk = img + TC_IMG_HDR + (size_t)q * TC_A_CHUNK_BYTES;
       uint32_t wr[TC_SLICES], wi[TC_SLICES], wn[TC_SLICES];
       slice6(sv[h].x, Er, wr);
       slice6(sv[h].y, Er, wi);
       slice6(-sv[h].y, Er, wn);
 #pragma unroll
       for (int t = 0; t < TC_SLICES; ++t) {
-        uint32_t* sl = chunk + t * TC_A_SLICE_WORDS;
-        sl[tc::tf32_offset(i, kc, 128) / 4] = wr[t];           // (re out, re in)
-        sl[tc::tf32_offset(i, kc + 1, 128) / 4] = wn[t];       // (re out, im in)
-        sl[tc::tf32_offset(64 + i, kc, 128) / 4] = wi[t];      // (im out, re in)
-        sl[tc::tf32_offset(64 + i, kc + 1, 128) / 4] = wr[t];  // (im out, im in)
+        unsigned char* sl = chunk + t * TC_A_SLICE_BYTES;
+        *reinterpret_cast<uint32_t*>(sl + tc::b16_offset(i, kc, 128)) = wr[t] | (wn[t] << 16);       // re out
+        *reinterpret_cast<uint32_t*>(sl + tc::b16_offset(64 + i, kc, 128)) = wi[t] | (wr[t] << 16);  // im out
       }
     }
   }
@@ -282,8 +283,9 @@ __device__ __forceinline__ void tc_b_exponents(const TcState& t, const double2* 
   __syncthreads();
 }
 
-// slices of chunk q of the B tile (inputs j = 16 q .. 16 q + 15) into shared memory
-__device__ __forceinline__ void tc_stage_b(const TcState& t, const double2* base, long long sn, long long sj, int q) {
+// slices of chunk q of the B tile (inputs j = 16 q .. 16 q + 15) into buffer bi
+__device__ __forceinline__ void tc_stage_b(const TcState& t, int bi, const double2* base, long long sn, long long sj,
+                                           int q) {
   for (int task = threadIdx.x; task < 64 * 16; task += blockDim.x) {
     const int n = task & 63, jj = task >> 6;
     const double2 v = base[(long long)n * sn + (long long)(16 * q + jj) * sj];
@@ -291,50 +293,47 @@ __device__ __forceinline__ void tc_stage_b(const TcState& t, const double2* base
     uint32_t wr[TC_SLICES], wi[TC_SLICES];
     slice6(v.x, Er, wr);
     slice6(v.y, Er, wi);
-    const uint32_t o = tc::tf32_offset(n, 2 * jj, 64) / 4;  // k = 2 jj and 2 jj + 1 are adjacent words
+    const uint32_t o = tc::b16_offset(n, 2 * jj, 64);
 #pragma unroll
-    for (int s = 0; s < TC_SLICES; ++s) *reinterpret_cast<uint2*>(t.b + s * TC_B_SLICE_WORDS + o) = make_uint2(wr[s], wi[s]);
+    for (int s = 0; s < TC_SLICES; ++s)
+      *reinterpret_cast<uint32_t*>(t.b[bi] + s * TC_B_SLICE_BYTES + o) = wr[s] | (wi[s] << 16);
   }
 }
 
-// MMAs of one chunk (26 slice pairs x 4 k-steps) and wait for them; false on a timed-out wait
-__device__ bool tc_chunk_mma(TcState& t, int q) {
-  tc::fence_proxy_async();
-  tc::fence_before();
-  __syncthreads();
-  tc::fence_after();
-  if (threadIdx.x == 0) {
-    const uint32_t idesc = tc::idesc_tf32(128, 64);
-    const uint32_t lboA = 16 * 128, lboB = 8 * 128, sbo = 128;
-    const uint32_t a0 = tc::smem_u32(t.a), b0 = tc::smem_u32(t.b);
-    for (int kk = 0; kk < TC_CHUNK_K / 8; ++kk) {
-      const uint32_t offA = (uint32_t)kk * 2 * 16 * 128, offB = (uint32_t)kk * 2 * 8 * 128;
-      for (int s = 0; s < TC_SLICES; ++s)
-        for (int u = 0; u < TC_SLICES; ++u) {
-          const int L = s + u;  // level - 2
-          if (L >= TC_LEVELS) continue;
-          const uint64_t ad = tc::smem_desc(a0 + (uint32_t)s * TC_A_SLICE_WORDS * 4 + offA, lboA, sbo);
-          const uint64_t bd = tc::smem_desc(b0 + (uint32_t)u * TC_B_SLICE_WORDS * 4 + offB, lboB, sbo);
-          // the first product into a level starts it: chunk 0, k-step 0, and s = 0 or u = L
-          const bool first = (q == 0 && kk == 0 && (s == (L < TC_SLICES ? 0 : L - TC_SLICES + 1)));
-          tc::mma_tf32(t.tmem + 64u * (uint32_t)L, ad, bd, idesc, first ? 0u : 1u);
-        }
-    }
-    tc::mma_commit(t.mbar);
+// issue the MMAs of chunk q from buffer bi (26 slice pairs x 2 k-steps) and commit them
+// to mbar[bi]; one thread
+__device__ __forceinline__ void tc_issue_chunk(const TcState& t, int q, int bi) {
+  const uint32_t idesc = tc::idesc_bf16(128, 64);
+  const uint32_t lboA = 16 * 128, lboB = 8 * 128, sbo = 128;
+  const uint32_t a0 = tc::smem_u32(t.a[bi]), b0 = tc::smem_u32(t.b[bi]);
+  for (int kk = 0; kk < TC_CHUNK_K / 16; ++kk) {
+    const uint32_t offA = (uint32_t)kk * 2 * 16 * 128, offB = (uint32_t)kk * 2 * 8 * 128;
+    for (int s = 0; s < TC_SLICES; ++s)
+      for (int u = 0; u < TC_SLICES; ++u) {
+        const int L = s + u;  // level - 2
+        if (L >= TC_LEVELS) continue;
+        const uint64_t ad = tc::smem_desc(a0 + (uint32_t)s * TC_A_SLICE_BYTES + offA, lboA, sbo);
+        const uint64_t bd = tc::smem_desc(b0 + (uint32_t)u * TC_B_SLICE_BYTES + offB, lboB, sbo);
+        // the first product into a level starts it: chunk 0, k-step 0, smallest s of the level
+        const bool first = (q == 0 && kk == 0 && (s == (L < TC_SLICES ? 0 : L - TC_SLICES + 1)));
+        tc::mma_bf16(t.tmem + 64u * (uint32_t)L, ad, bd, idesc, first ? 0u : 1u);
+      }
   }
-  __syncwarp();
-  const bool ok = tc::mbar_wait(t.mbar, t.phase);
-  t.phase ^= 1u;
-  tc::fence_after();
+  tc::mma_commit(&t.mbar[bi]);
+}
+
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t& ph) {
+  const bool ok = tc::mbar_wait(bar, ph);
+  ph ^= 1u;
   return ok;
 }
 
-// TMEM -> stage (double [128][TC_STAGE_LD], in the A buffer) by warps 0-3, one row each:
+// TMEM -> stage (double [128][TC_STAGE_LD] over the A buffers) by warps 0-3, one row each:
 // exact integer combination of the 7 levels, scaled by 2^(E_i + E_n - 56)
 __device__ __forceinline__ void tc_drain_to_stage(const TcState& t, int Ei) {
   const int warp = threadIdx.x >> 5;
   if (warp < 4) {
-    double* row = reinterpret_cast<double*>(t.a) + threadIdx.x * TC_STAGE_LD;
+    double* row = reinterpret_cast<double*>(t.a[0]) + threadIdx.x * TC_STAGE_LD;
     const uint32_t lane_base = t.tmem + ((uint32_t)(32 * warp) << 16);
     for (int c0 = 0; c0 < 64; c0 += 8) {
       float f[TC_LEVELS][8];
@@ -367,7 +366,7 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
   if ((long long)blockIdx.x >= tiles) return;
   const unsigned char* img = reinterpret_cast<const unsigned char*>(a.tc_img) + (size_t)op.img * kTcImageBytes;
   const int Ei = (threadIdx.x < 128) ? reinterpret_cast<const int*>(img)[threadIdx.x & 63] : 0;
-  const double* stage = reinterpret_cast<const double*>(t.a);
+  const double* stage = reinterpret_cast<const double*>(t.a[0]);
   for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     long long aa = 0, b0 = 0, sn, sj;
     const double2* base;
@@ -384,17 +383,41 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
       sj = 1;
     }
     tc_b_exponents(t, base, sn, sj);
-    for (int q = 0; q < TC_CHUNKS; ++q) {
-      if (threadIdx.x == 0) {
-        tc::fence_proxy_async_all();
-        tc::mbar_expect_tx(t.lbar, (uint32_t)TC_A_CHUNK_BYTES);
-        tc::bulk_g2s(t.a, img + TC_IMG_HDR + (size_t)q * TC_A_CHUNK_BYTES, (uint32_t)TC_A_CHUNK_BYTES, t.lbar);
-      }
-      tc_stage_b(t, base, sn, sj, q);
-      if (!tc::mbar_wait(t.lbar, t.lphase) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
-      t.lphase ^= 1u;
-      if (!tc_chunk_mma(t, q) && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
+    // double-buffered chunks: the bulk copy and the slicing of chunk q + 1 overlap the
+    // MMAs of chunk q
+    if (threadIdx.x == 0) {
+      tc::fence_proxy_async_all();
+      tc::mbar_expect_tx(&t.lbar[0], (uint32_t)TC_A_CHUNK_BYTES);
+      tc::bulk_g2s(t.a[0], img + TC_IMG_HDR, (uint32_t)TC_A_CHUNK_BYTES, &t.lbar[0]);
     }
+    tc_stage_b(t, 0, base, sn, sj, 0);
+    bool ok = true;
+    for (int q = 0; q < TC_CHUNKS; ++q) {
+      const int bi = q & 1, nbi = bi ^ 1;
+      ok = tc_wait(&t.lbar[bi], t.lph[bi]) && ok;
+      tc::fence_proxy_async();
+      tc::fence_before();
+      __syncthreads();
+      tc::fence_after();
+      if (threadIdx.x == 0) tc_issue_chunk(t, q, bi);
+      __syncwarp();
+      if (q + 1 < TC_CHUNKS) {
+        if (q >= 1) ok = tc_wait(&t.mbar[nbi], t.mph[nbi]) && ok;  // chunk q - 1 has released buffer nbi
+        tc::fence_after();
+        if (threadIdx.x == 0) {
+          tc::fence_proxy_async_all();
+          tc::mbar_expect_tx(&t.lbar[nbi], (uint32_t)TC_A_CHUNK_BYTES);
+          tc::bulk_g2s(t.a[nbi], img + TC_IMG_HDR + (size_t)(q + 1) * TC_A_CHUNK_BYTES, (uint32_t)TC_A_CHUNK_BYTES,
+                       &t.lbar[nbi]);
+        }
+        tc_stage_b(t, nbi, base, sn, sj, q + 1);
+      }
+    }
+    // chunks 2 and 3 (buffers 0 and 1) complete
+    ok = tc_wait(&t.mbar[0], t.mph[0]) && ok;
+    ok = tc_wait(&t.mbar[1], t.mph[1]) && ok;
+    tc::fence_after();
+    if (!ok && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
     tc_drain_to_stage(t, Ei);
     // stage -> out: element (i, n) = (stage[i][n], stage[64 + i][n])
     for (int task = threadIdx.x; task < 64 * 64; task += blockDim.x) {
@@ -413,7 +436,7 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
       if (acc) v = cadd(v, *dst);
       *dst = v;
     }
-    // the next tile's bulk copy (async proxy) overwrites the stage just read
+    // the next tile's bulk copies (async proxy) overwrite the stage just read
     tc::fence_proxy_async_all();
     __syncthreads();
   }
@@ -647,8 +670,8 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
   __shared__ Red sm;
   __shared__ double2 red[EQ];
   __shared__ int s_done, s_mb;
-  __shared__ __align__(8) uint64_t s_mbar;
-  __shared__ __align__(8) uint64_t s_lbar;
+  __shared__ __align__(8) uint64_t s_mbar[2];
+  __shared__ __align__(8) uint64_t s_lbar[2];
   __shared__ uint32_t s_tmem;
   extern __shared__ __align__(1024) unsigned char dsm[];
   __shared__ MvOp s_op1;
@@ -666,8 +689,10 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
   TcState* tcp = nullptr;
   if (a.mixed) {
     if (threadIdx.x == 0) {
-      tc::mbar_init(&s_mbar, 1);
-      tc::mbar_init(&s_lbar, 1);
+      tc::mbar_init(&s_mbar[0], 1);
+      tc::mbar_init(&s_mbar[1], 1);
+      tc::mbar_init(&s_lbar[0], 1);
+      tc::mbar_init(&s_lbar[1], 1);
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(&s_tmem, TC_TMEM_COLS);
@@ -675,13 +700,15 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
     __syncthreads();
     tc::fence_after();
     tcs.tmem = s_tmem;
-    tcs.phase = 0;
-    tcs.lphase = 0;
-    tcs.mbar = &s_mbar;
-    tcs.lbar = &s_lbar;
-    tcs.a = reinterpret_cast<uint32_t*>(dsm);
-    tcs.b = reinterpret_cast<uint32_t*>(dsm + TC_A_CHUNK_BYTES);
-    tcs.e_n = reinterpret_cast<int*>(dsm + TC_A_CHUNK_BYTES + TC_B_CHUNK_BYTES);
+    tcs.mph[0] = tcs.mph[1] = 0;
+    tcs.lph[0] = tcs.lph[1] = 0;
+    tcs.mbar = s_mbar;
+    tcs.lbar = s_lbar;
+    tcs.a[0] = dsm;
+    tcs.a[1] = dsm + TC_A_CHUNK_BYTES;
+    tcs.b[0] = dsm + 2 * TC_A_CHUNK_BYTES;
+    tcs.b[1] = dsm + 2 * TC_A_CHUNK_BYTES + TC_B_CHUNK_BYTES;
+    tcs.e_n = reinterpret_cast<int*>(dsm + 2 * (TC_A_CHUNK_BYTES + TC_B_CHUNK_BYTES));
     tcp = &tcs;
     build_tc_images(a);
   }

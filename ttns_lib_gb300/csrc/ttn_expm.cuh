@@ -28,8 +28,8 @@ struct MvOp {
   double2 alpha;
 };
 // bytes of one operator image: row exponents (1 KB) and the 128 x 128 block operand as
-// six TF32 integer slices in four K-chunks of 96 KB
-constexpr size_t kTcImageBytes = (size_t)1024 + (size_t)4 * 6 * 128 * 32 * 4;
+// six bf16 integer slices in four K-chunks of 48 KB
+constexpr size_t kTcImageBytes = (size_t)1024 + (size_t)4 * 6 * 128 * 32 * 2;
 
 struct ExpmArgs {
   double2* y;            // vector evolved in place
@@ -65,9 +65,12 @@ int expm_coop_max_grid(int mixed);
 size_t expm_partial_bytes(int max_grid);
 cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s);
 // whether a contraction can run on the tensor cores
+// Tensor-core contractions need rank-64 operands and enough 64-column tiles to occupy the
+// device; smaller ones run faster as element-wise FP64 contractions.
+constexpr long long kTcMinTiles = 32;
 inline bool tc_eligible(int kind, int d, long long na, long long nb) {
-  if (kind == MV_MODE) return d == 64 && nb % 64 == 0;
-  if (kind == MV_MF) return d == 64 && na % 64 == 0;
+  if (kind == MV_MODE) return d == 64 && nb % 64 == 0 && na * (nb / 64) >= kTcMinTiles;
+  if (kind == MV_MF) return d == 64 && na % 64 == 0 && na / 64 >= kTcMinTiles;
   return false;
 }
 

@@ -252,7 +252,8 @@ def workload_config(name, cfg, precision, over=None):
         "config": name, "modes": modes, "chi": cfg["chi"], "local_dim": cfg["d"], "dt": cfg["dt"],
         "krylov_dim": cfg["krylov_dim"], "nodes": m.topology.nnodes, "precision": precision,
         "state_bytes": m.topology.state_size() * 16,
-        "l2": "inputs larger than L2: the node tensors (state) exceed the 129 MB L2 many times over",
+        "l2": ("inputs larger than L2: the node tensors (state) exceed the 129 MB L2"
+               if m.topology.state_size() * 16 > 129e6 else "state smaller than L2 (profiling-size tree)"),
     }
 
 
@@ -293,7 +294,10 @@ def run_ours(args):
     # roofline of the dominant kernel: the persistent Krylov exponential on the largest
     # node (it runs every H_eff contraction of the node update)
     node = upper_node(topo)
+    nv = Nvtx()
+    nv.push("ttn_roofline")
     k_ms, k_fl = tdvp.bench_node_op(A, node, 1, 5)
+    nv.pop()
     achieved = k_fl / (k_ms * 1e-3) / 1e12
     peaks, src = measured_peaks()
     if prec_name == "fp64":
@@ -306,7 +310,7 @@ def run_ours(args):
     else:
         peak = peaks["bf16_tflops"]
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": traffic_from_profiles("heff_mixed"),
+                "traffic": traffic_from_profiles("expm_mixed"),
                 "kernel": f"Krylov exponential of a {topo.node_shape(node)[0]}x{topo.node_shape(node)[1]} node",
                 "peak_source": f"bf16 dense, {src} (MEASURED_PEAKS.json)",
                 "ms_per_launch": k_ms, "flops_per_launch": k_fl}
@@ -384,7 +388,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "c128" if prec_name == "fp64" else "c128 state and Krylov, split-TF32 tensor-core contractions",
+        "dtype": "c128" if prec_name == "fp64" else
+                 "c128 state and Krylov; rank-64 contractions on tensor cores from exact bf16 integer slices",
         "data": "synthetic (formula-generated spin-boson bath; std::mt19937 unoccupied SPFs)",
         "config": workload_config(args.config, cfg, prec_name, over),
         "roofline": roof,

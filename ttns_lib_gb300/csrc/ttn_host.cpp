@@ -587,6 +587,7 @@ struct Integrator {
       qr_scratch = (double*)(coop_buf.as<char>() + align256(sizeof(GridBarrier)));
       mixed = (cfg.precision == TTN_PREC_MIXED);
       if (const char* e = std::getenv("TTN_EXPM_CTA_FLOPS")) expm_cta_flops = std::atof(e);
+      if (const char* e = std::getenv("TTN_QR_ROWS_PER_CTA")) qr_rows_per_cta = std::max(1, std::atoi(e));
       expm_max_grid = std::max(1, expm_coop_max_grid(0));
       expm_max_grid_tc = std::max(1, expm_coop_max_grid(1));
       if (mixed) {
@@ -1146,8 +1147,9 @@ struct Integrator {
 
   // ---------------------------------------------------------------- gauge moves
   // Householder QR on as many CTAs as the height allows (one row block per CTA)
+  int qr_rows_per_cta = 32;  // rows of the matrix per CTA of the cooperative QR
   void qr(double2* M, long long m, int n, double2* R, int Rt) {
-    int g = std::min(coop_qr_grid(m, num_sms), qr_max_grid);
+    int g = (int)std::max(1LL, std::min<long long>(m / qr_rows_per_cta, qr_max_grid));
     CK(householder_qr_blocked(M, m, n, R, Rt, qtau, qr_scratch, bar, status, g, stream));
   }
   static double qr_flops(double m, double n) { return 2.0 * 8.0 * (m * n * n - n * n * n / 3.0); }

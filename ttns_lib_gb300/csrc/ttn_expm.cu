@@ -18,6 +18,7 @@ namespace ttn {
 namespace {
 constexpr int ET = 256;   // threads per CTA
 constexpr int EQ = 72;    // max Krylov vectors
+constexpr int kSliceReduceGrid = 64;  // from this many CTAs on, coefficient sums are split over CTAs
 
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
@@ -190,13 +191,14 @@ __device__ __forceinline__ void slice6(double x, int Er, uint32_t* w) {
     w[t] = __float_as_uint(__int2float_rn(neg ? -v : v)) >> 16;
   }
 }
-// v * 2^e2 as a double from the bits (truncating below 53 bits; 0 below the normal range)
-__device__ __forceinline__ double i64_scaled(long long v, int e2) {
+// v * 2^e2 as a double (truncating below 53 bits; 0 below the normal range), |v| < 2^126
+__device__ __forceinline__ double i128_scaled(__int128 v, int e2) {
   if (v == 0) return 0.0;
   const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
-  const unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
-  const int msb = 63 - __clzll((long long)a);
-  const unsigned long long mant = msb > 52 ? (a >> (msb - 52)) : (a << (52 - msb));
+  const unsigned __int128 a = v < 0 ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  const unsigned long long hi = (unsigned long long)(a >> 64), lo = (unsigned long long)a;
+  const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+  const unsigned long long mant = (unsigned long long)(msb > 52 ? (a >> (msb - 52)) : (a << (52 - msb)));
   const int ex = msb + e2 + 1023;
   if (ex <= 0) return 0.0;
   if (ex >= 2047) return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ull));
@@ -348,7 +350,7 @@ __device__ __forceinline__ void tc_drain_to_stage(const TcState& t, int Ei) {
 #pragma unroll
         for (int L = 2; L < TC_LEVELS; ++L) lo += (long long)__float2int_rn(f[L][c]) << (7 * (TC_LEVELS - 1 - L));
         const int e2 = Ei + t.e_n[c0 + c] - 56;
-        row[c0 + c] = i64_scaled(hi, e2 + 35) + i64_scaled(lo, e2);
+        row[c0 + c] = i128_scaled(((__int128)hi << 35) + (__int128)lo, e2);
       }
     }
   }
@@ -678,6 +680,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
   // the controller's scratch and the tensor-core operands share the dynamic buffer: they
   // are used in different phases
   CtlSmem& cs = *reinterpret_cast<CtlSmem*>(dsm);
+  grid_barrier_begin(a_in.bar);
   // a single contraction passed by value runs from a shared-memory copy
   ExpmArgs a = a_in;
   if (a.prog == nullptr) {
@@ -845,7 +848,24 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
       store_partials(sm, j + 1, pb);
       if (blockIdx.x == 0 && threadIdx.x == 0) ctl->alpha[j] = alpha;
       grid_barrier(a.bar, a.err);
-      reduce_partials(pb, j + 1, red, sm);
+      if (gridDim.x >= kSliceReduceGrid) {
+        // CTA q < j + 1 reduces coefficient q over all partials (same order as
+        // reduce_partials), then everyone reads the j + 1 results: one more barrier instead
+        // of every CTA summing (j + 1) x grid partials in FP64
+        double2* rq = a.part + (size_t)2 * gridDim.x * EQ;
+        if ((int)blockIdx.x <= j && warp == 0) {
+          double2 t = make_double2(0.0, 0.0);
+          for (int b = lane; b < (int)gridDim.x; b += 32) t = cadd(t, pb[(long long)b * (j + 1) + blockIdx.x]);
+          t.x = wsum(t.x);
+          t.y = wsum(t.y);
+          if (lane == 0) rq[blockIdx.x] = t;
+        }
+        grid_barrier(a.bar, a.err);
+        for (int q = threadIdx.x; q <= j; q += blockDim.x) red[q] = rq[q];
+        __syncthreads();
+      } else {
+        reduce_partials(pb, j + 1, red, sm);
+      }
       pc.mark(3);
       {
         double s = 0.0;
@@ -941,6 +961,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
       tc::tmem_dealloc(tcs.tmem, TC_TMEM_COLS);
     }
   }
+  grid_barrier_end(a.bar);
   if (blockIdx.x == 0 && threadIdx.x == 0 && !a.apply_only) {
     if (a.napps_total) atomicAdd((unsigned long long*)a.napps_total, (unsigned long long)ctl->napps);
     if (a.flops_total) atomicAdd(a.flops_total, a.flops_per_app * (double)ctl->napps);
@@ -962,7 +983,8 @@ int expm_coop_max_grid(int mixed) {
   return sms * (per < 1 ? 1 : per);
 }
 
-size_t expm_partial_bytes(int max_grid) { return (size_t)2 * max_grid * EQ * sizeof(double2); }
+// partials of two reductions ([grid][EQ] complex each) and the reduced coefficients
+size_t expm_partial_bytes(int max_grid) { return (size_t)(2 * max_grid + 1) * EQ * sizeof(double2); }
 
 cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s) {
   ExpmArgs b = a;

@@ -1052,6 +1052,7 @@ __global__ void __launch_bounds__(CQT) k_qr_coop(CoopQrArgs a) {
   const int n = a.n;
   const long long r0 = b * m / G, r1 = (b + 1) * m / G;
   const double safmin = 2.2250738585072014e-308 / 1.1102230246251565e-16;
+  grid_barrier_begin(a.bar);
   // scratch layout (doubles): norm partials 2x[G][2], alpha slots 2x[2], w partials 2x[G][2*CQN];
   // the norm / alpha slots alternate with the column parity so that a CTA running ahead
   // never overwrites values a slower CTA still has to read
@@ -1268,6 +1269,7 @@ __global__ void __launch_bounds__(CQT) k_qr_coop(CoopQrArgs a) {
     }
     __syncthreads();
   }
+  grid_barrier_end(a.bar);
 }
 }  // namespace
 

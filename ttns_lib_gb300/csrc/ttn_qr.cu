@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(BT) k_qr_blocked(BqrArgs a) {
   const long long r0 = b * m / G, r1 = (b + 1) * m / G;
   const double safmin = 2.2250738585072014e-308 / 1.1102230246251565e-16;
   const int npan = (n + NB - 1) / NB;
+  grid_barrier_begin(a.bar);
 
   column_partials(a, 0, n < NB ? n : NB, r0, r1, S);
   // ------------------------------------------------------------------ factorisation
@@ -545,6 +546,7 @@ __global__ void __launch_bounds__(BT) k_qr_blocked(BqrArgs a) {
       __syncthreads();
     }
   }
+  grid_barrier_end(a.bar);
 }
 
 }  // namespace

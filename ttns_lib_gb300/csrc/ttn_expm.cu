@@ -459,7 +459,7 @@ __device__ void store_partials(Red& sm, int nq, double2* part) {
   __syncthreads();
   for (int q = threadIdx.x; q < nq; q += blockDim.x) {
     double2 s = make_double2(0.0, 0.0);
-    for (int w = 0; w < ET / 32; ++w) s = cadd(s, sm.w[w][q]);
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = cadd(s, sm.w[w][q]);
     part[(long long)blockIdx.x * nq + q] = s;
   }
   __syncthreads();
@@ -469,7 +469,7 @@ __device__ void reduce_partials(const double2* part, int nq, double2* out, Red& 
   const int G = gridDim.x;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   // warp w handles q = w, w+8, ...; lanes stride over b
-  for (int q = w; q < nq; q += ET / 32) {
+  for (int q = w; q < nq; q += (int)(blockDim.x >> 5)) {
     double2 s = make_double2(0.0, 0.0);
     for (int b = lane; b < G; b += 32) s = cadd(s, part[(long long)b * nq + q]);
     s.x = wsum(s.x);
@@ -986,11 +986,12 @@ int expm_coop_max_grid(int mixed) {
 // partials of two reductions ([grid][EQ] complex each) and the reduced coefficients
 size_t expm_partial_bytes(int max_grid) { return (size_t)(2 * max_grid + 1) * EQ * sizeof(double2); }
 
-cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s) {
+cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s, int threads) {
+  if (threads <= 0 || threads > ET || (threads & 31) || a.mixed) threads = ET;  // tensor-core ops need ET
   ExpmArgs b = a;
   void* args[] = {&b};
   ++g_launches;
-  return cudaLaunchCooperativeKernel((const void*)k_expm_coop, dim3(grid), dim3(ET), args, dyn_smem(a.mixed), s);
+  return cudaLaunchCooperativeKernel((const void*)k_expm_coop, dim3(grid), dim3(threads), args, dyn_smem(a.mixed), s);
 }
 
 }  // namespace ttn

@@ -63,7 +63,8 @@ constexpr int kPhases = 10;  // begin, matvec, alpha, reorth coefficients, reort
 // co-resident CTAs for the plain (mixed = 0) or tensor-core (mixed = 1) configuration
 int expm_coop_max_grid(int mixed);
 size_t expm_partial_bytes(int max_grid);
-cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s);
+// threads per CTA: a multiple of 32 up to 256 (tensor-core programs always use 256)
+cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s, int threads = 256);
 // whether a contraction can run on the tensor cores
 // Tensor-core contractions need rank-64 operands and enough 64-column tiles to occupy the
 // device; smaller ones run faster as element-wise FP64 contractions.

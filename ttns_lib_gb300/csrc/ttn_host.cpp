@@ -588,6 +588,7 @@ struct Integrator {
       mixed = (cfg.precision == TTN_PREC_MIXED);
       if (const char* e = std::getenv("TTN_EXPM_CTA_FLOPS")) expm_cta_flops = std::atof(e);
       if (const char* e = std::getenv("TTN_QR_ROWS_PER_CTA")) qr_rows_per_cta = std::max(1, std::atoi(e));
+      if (const char* e = std::getenv("TTN_EXPM_ELEMS_PER_THREAD")) expm_elems_per_thread = std::max(0.1, std::atof(e));
       expm_max_grid = std::max(1, expm_coop_max_grid(0));
       expm_max_grid_tc = std::max(1, expm_coop_max_grid(1));
       if (mixed) {
@@ -1073,6 +1074,15 @@ struct Integrator {
   // with __syncthreads alone, several need grid barriers of a few microseconds each),
   // large ones on the whole device.
   double expm_cta_flops = 2.0e5;
+  // threads per CTA: about expm_elems_per_thread vector elements per thread, 64..256 (the
+  // FP64 warp reductions cost the same per warp whatever the data, so tiny problems run on
+  // fewer warps)
+  double expm_elems_per_thread = 1.0;
+  int expm_threads(long long n, int grid) const {
+    long long t = (long long)std::ceil((double)n / ((double)grid * expm_elems_per_thread));
+    t = (t + 31) / 32 * 32;
+    return (int)std::max(64LL, std::min(256LL, t));
+  }
   int expm_grid(long long n, bool tc, double flops_per_app) const {
     long long g = (n + 63) / 64;
     if (expm_cta_flops > 0.0) {
@@ -1103,7 +1113,8 @@ struct Integrator {
     a.apply_only = apply_only ? 1 : 0;
     a.phase = phase_dev;
     a.tc_img = tc_img_buf.as<uint32_t>();
-    CK(expm_coop(a, expm_grid(n, a.mixed, a.flops_per_app), stream));
+    const int grid = expm_grid(n, a.mixed, a.flops_per_app);
+    CK(expm_coop(a, grid, stream, expm_threads(n, grid)));
     // Lanczos vector passes of one sub-step (the matvec flops are tallied on the device)
     if (tally) flops += lanczos_vec_flops(n);
   }

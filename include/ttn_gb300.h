@@ -138,8 +138,10 @@ int ttn_debug_refresh_env(ttn_integrator* it, ttn_state* psi);
 /* out = H_eff(node) v with the current environments; v, out are host buffers */
 int ttn_debug_heff(ttn_integrator* it, int node, const double* v, double* out);
 /* Krylov kernel phase times accumulated since the last call (TTN_PROFILE set at creation,
- * else zeros): out[0..7] ms in begin, matvec, alpha, re-orthogonalisation coefficients,
- * re-orthogonalisation + norm, ||H V_m||, control, combine; out[8] sub-steps, out[9] launches */
+ * else zeros), out[16]: out[0..7] ms in begin, matvec, alpha, re-orthogonalisation
+ * coefficients, re-orthogonalisation + norm, ||H V_m||, control, combine; out[8] sub-steps,
+ * out[9] launches; out[10..13] ms inside the tensor-core contractions (row exponents,
+ * chunk pipeline, TMEM drain, output), out[14] tensor-core tiles (as seen by CTA 0) */
 int ttn_integrator_kernel_phases(ttn_integrator* it, double* out);
 /* out = the compiled matrix-vector program of a node (kind 0: H_eff, kind 1: bond
  * Hamiltonian on the node's R matrix) applied once by the persistent kernel, in the

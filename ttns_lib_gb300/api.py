@@ -335,11 +335,15 @@ class fixed_step_projector_splitting_integrator:
 
     def kernel_phases(self):
         """ms per phase of the Krylov kernel since the last call (needs TTN_PROFILE)."""
-        out = np.zeros(10)
+        out = np.zeros(16)
         _check(lib().ttn_integrator_kernel_phases(self.h, _dp(out)))
         d = {k: float(out[i]) for i, k in enumerate(self.KERNEL_PHASES)}
         d["substeps"] = int(out[8])
         d["launches"] = int(out[9])
+        for i, k in enumerate(["tc_exponents", "tc_chunks", "tc_drain", "tc_output"]):
+            d[k] = float(out[10 + i])
+        d["tc_tiles"] = int(out[14])
+        d["tc_drain_tmem_ld"] = float(out[15])
         return d
 
     def io_bytes(self):

@@ -122,6 +122,24 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
   }
 }
 
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// wall time per phase as seen by one thread of CTA 0 (barrier waits included)
+struct PhaseClock {
+  unsigned long long* acc;
+  unsigned long long t;
+  __device__ void mark(int k) {
+    if (acc) {
+      const unsigned long long now = gtimer();
+      acc[k] += now - t;
+      t = now;
+    }
+  }
+};
+
 // ---- tensor-core contractions (mixed precision) at FP64 accuracy
 //
 // Both kinds are D(128 x 64) = A B^T per tile, A the real block form of alpha * mat
@@ -184,21 +202,32 @@ __device__ __forceinline__ void slice6(double x, int Er, uint32_t* w) {
     const int sh = Er - 42 - p;                  // q = floor(|x| 2^(42 - Er)) < 2^42
     q = sh >= 64 ? 0ull : (sh >= 0 ? (m >> sh) : (m << (-sh)));
   }
-  const bool neg = (b >> 63) != 0;
+  const uint32_t sgn = (uint32_t)(b >> 63) << 15;
 #pragma unroll
   for (int t = 0; t < TC_SLICES; ++t) {
-    const int v = (int)((q >> (35 - 7 * t)) & 127ull);
-    w[t] = __float_as_uint(__int2float_rn(neg ? -v : v)) >> 16;
+    const uint32_t v = (uint32_t)((q >> (35 - 7 * t)) & 127ull);
+    // (float)v exactly: 2^23 + v has v in its low mantissa bits; subtracting 2^23 is exact
+    const float f = __uint_as_float(0x4B000000u | v) - 8388608.0f;
+    w[t] = (__float_as_uint(f) >> 16) | (v ? sgn : 0u);
   }
 }
-// v * 2^e2 as a double (truncating below 53 bits; 0 below the normal range), |v| < 2^126
-__device__ __forceinline__ double i128_scaled(__int128 v, int e2) {
+// the integer held exactly by an FP32 accumulator (|x| < 2^24), from its bits
+__device__ __forceinline__ long long f32_exact_int(float x) {
+  const uint32_t b = __float_as_uint(x);
+  const int e = (int)((b >> 23) & 0xFF);
+  if (e < 127) return 0;  // |x| < 1 is 0 for an integer
+  const uint32_t m = (b & 0x7FFFFFu) | 0x800000u;
+  const long long v = (long long)(m >> (150 - e));  // e <= 150 since |x| < 2^24
+  return (b >> 31) ? -v : v;
+}
+// v * 2^e2 as a double from integer operations (truncating below 53 bits; 0 below the
+// normal range)
+__device__ __forceinline__ double i64_to_scaled_double(long long v, int e2) {
   if (v == 0) return 0.0;
   const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
-  const unsigned __int128 a = v < 0 ? (unsigned __int128)(-v) : (unsigned __int128)v;
-  const unsigned long long hi = (unsigned long long)(a >> 64), lo = (unsigned long long)a;
-  const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
-  const unsigned long long mant = (unsigned long long)(msb > 52 ? (a >> (msb - 52)) : (a << (52 - msb)));
+  const unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+  const int msb = 63 - __clzll((long long)a);
+  const unsigned long long mant = msb > 52 ? (a >> (msb - 52)) : (a << (52 - msb));
   const int ex = msb + e2 + 1023;
   if (ex <= 0) return 0.0;
   if (ex >= 2047) return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ull));
@@ -268,6 +297,7 @@ __device__ __forceinline__ void tc_b_exponents(const TcState& t, const double2* 
   const int n = threadIdx.x >> 2, part = threadIdx.x & 3;
   unsigned long long mx = 0;
   if (n < 64) {
+#pragma unroll
     for (int j = 16 * part; j < 16 * part + 16; ++j) {
       const double2 v = base[(long long)n * sn + (long long)j * sj];
       const unsigned long long ar = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
@@ -286,10 +316,16 @@ __device__ __forceinline__ void tc_b_exponents(const TcState& t, const double2* 
 }
 
 // slices of chunk q of the B tile (inputs j = 16 q .. 16 q + 15) into buffer bi
+// (tensor-core programs run with 256 threads: four rounds of 256 (n, jj) tasks; the lanes
+// of a warp cover one 8-row x 4-word block of core matrices, 128 contiguous bytes per
+// slice store, so the stores are free of bank conflicts)
 __device__ __forceinline__ void tc_stage_b(const TcState& t, int bi, const double2* base, long long sn, long long sj,
                                            int q) {
-  for (int task = threadIdx.x; task < 64 * 16; task += blockDim.x) {
-    const int n = task & 63, jj = task >> 6;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int task = threadIdx.x + 256 * r;
+    const int blk = task >> 5, ln = task & 31;
+    const int n = (blk & 7) * 8 + (ln >> 2), jj = (blk >> 3) * 4 + (ln & 3);
     const double2 v = base[(long long)n * sn + (long long)(16 * q + jj) * sj];
     const int Er = t.e_n[n];
     uint32_t wr[TC_SLICES], wi[TC_SLICES];
@@ -303,19 +339,22 @@ __device__ __forceinline__ void tc_stage_b(const TcState& t, int bi, const doubl
 }
 
 // issue the MMAs of chunk q from buffer bi (26 slice pairs x 2 k-steps) and commit them
-// to mbar[bi]; one thread
+// to mbar[bi]; one thread.  A descriptor's start address is its low 14 bits in 16-byte
+// units, so every operand slice's descriptor is the buffer's plus a constant.
 __device__ __forceinline__ void tc_issue_chunk(const TcState& t, int q, int bi) {
   const uint32_t idesc = tc::idesc_bf16(128, 64);
-  const uint32_t lboA = 16 * 128, lboB = 8 * 128, sbo = 128;
-  const uint32_t a0 = tc::smem_u32(t.a[bi]), b0 = tc::smem_u32(t.b[bi]);
+  const uint64_t ad0 = tc::smem_desc(tc::smem_u32(t.a[bi]), 16 * 128, 128);
+  const uint64_t bd0 = tc::smem_desc(tc::smem_u32(t.b[bi]), 8 * 128, 128);
+#pragma unroll
   for (int kk = 0; kk < TC_CHUNK_K / 16; ++kk) {
-    const uint32_t offA = (uint32_t)kk * 2 * 16 * 128, offB = (uint32_t)kk * 2 * 8 * 128;
+#pragma unroll
     for (int s = 0; s < TC_SLICES; ++s)
+#pragma unroll
       for (int u = 0; u < TC_SLICES; ++u) {
         const int L = s + u;  // level - 2
         if (L >= TC_LEVELS) continue;
-        const uint64_t ad = tc::smem_desc(a0 + (uint32_t)s * TC_A_SLICE_BYTES + offA, lboA, sbo);
-        const uint64_t bd = tc::smem_desc(b0 + (uint32_t)u * TC_B_SLICE_BYTES + offB, lboB, sbo);
+        const uint64_t ad = ad0 + (uint64_t)((s * TC_A_SLICE_BYTES + kk * 2 * 16 * 128) >> 4);
+        const uint64_t bd = bd0 + (uint64_t)((u * TC_B_SLICE_BYTES + kk * 2 * 8 * 128) >> 4);
         // the first product into a level starts it: chunk 0, k-step 0, smallest s of the level
         const bool first = (q == 0 && kk == 0 && (s == (L < TC_SLICES ? 0 : L - TC_SLICES + 1)));
         tc::mma_bf16(t.tmem + 64u * (uint32_t)L, ad, bd, idesc, first ? 0u : 1u);
@@ -330,28 +369,30 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t& ph) {
   return ok;
 }
 
-// TMEM -> stage (double [128][TC_STAGE_LD] over the A buffers) by warps 0-3, one row each:
-// exact integer combination of the 7 levels, scaled by 2^(E_i + E_n - 56)
-__device__ __forceinline__ void tc_drain_to_stage(const TcState& t, int Ei) {
-  const int warp = threadIdx.x >> 5;
-  if (warp < 4) {
-    double* row = reinterpret_cast<double*>(t.a[0]) + threadIdx.x * TC_STAGE_LD;
-    const uint32_t lane_base = t.tmem + ((uint32_t)(32 * warp) << 16);
-    for (int c0 = 0; c0 < 64; c0 += 8) {
-      float f[TC_LEVELS][8];
+// TMEM -> stage (double [128][TC_STAGE_LD] over the A buffers): warp w drains TMEM lanes
+// 32 (w % 4) .. + 31 (one row each), columns 32 (w / 4) .. + 31; exact integer combination
+// of the 7 levels, scaled by 2^(E_i + E_n - 56)
+__device__ __forceinline__ void tc_drain_to_stage(const TcState& t, int Ei, PhaseClock& pc) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row_i = 32 * (warp & 3) + lane;
+  double* row = reinterpret_cast<double*>(t.a[0]) + row_i * TC_STAGE_LD;
+  const uint32_t lane_base = t.tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+  for (int c0 = 32 * (warp >> 2); c0 < 32 * (warp >> 2) + 32; c0 += 8) {
+    float f[TC_LEVELS][8];
 #pragma unroll
-      for (int L = 0; L < TC_LEVELS; ++L) tc::tmem_ld8_nowait(lane_base + 64u * L + (uint32_t)c0, f[L]);
-      tc::tmem_wait_ld();
+    for (int L = 0; L < TC_LEVELS; ++L) tc::tmem_ld8_nowait(lane_base + 64u * L + (uint32_t)c0, f[L]);
+    tc::tmem_wait_ld();
+    pc.mark(15);
 #pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        // levels 2,3 -> hi (scale 2^35 relative to lo); levels 4..8 -> lo
-        const long long hi = (long long)__float2int_rn(f[0][c]) * 128 + (long long)__float2int_rn(f[1][c]);
-        long long lo = 0;
+    for (int c = 0; c < 8; ++c) {
+      // sum_L acc_L 2^(7 (6 - L)) / 2: levels 2,3 shifted by 34, the rest below; the bit
+      // dropped is 2^-57 of the scale
+      const long long hi = f32_exact_int(f[0][c]) * 128 + f32_exact_int(f[1][c]);
+      long long lo = 0;
 #pragma unroll
-        for (int L = 2; L < TC_LEVELS; ++L) lo += (long long)__float2int_rn(f[L][c]) << (7 * (TC_LEVELS - 1 - L));
-        const int e2 = Ei + t.e_n[c0 + c] - 56;
-        row[c0 + c] = i128_scaled(((__int128)hi << 35) + (__int128)lo, e2);
-      }
+      for (int L = 2; L < TC_LEVELS; ++L) lo += f32_exact_int(f[L][c]) << (7 * (TC_LEVELS - 1 - L));
+      const int e2 = Ei + t.e_n[c0 + c] - 56;
+      row[c0 + c] = i64_to_scaled_double((hi << 34) + (lo >> 1), e2 + 1);
     }
   }
   tc::fence_before();
@@ -367,9 +408,12 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
   const long long tiles = mode ? op.na * (nb / 64) : op.na / 64;
   if ((long long)blockIdx.x >= tiles) return;
   const unsigned char* img = reinterpret_cast<const unsigned char*>(a.tc_img) + (size_t)op.img * kTcImageBytes;
-  const int Ei = (threadIdx.x < 128) ? reinterpret_cast<const int*>(img)[threadIdx.x & 63] : 0;
+  const int Ei = reinterpret_cast<const int*>(img)[(32 * ((threadIdx.x >> 5) & 3) + (threadIdx.x & 31)) & 63];
   const double* stage = reinterpret_cast<const double*>(t.a[0]);
+  PhaseClock pc{(a.phase && blockIdx.x == 0 && threadIdx.x == 0) ? a.phase : nullptr, 0ull};
+  if (pc.acc) pc.t = gtimer();
   for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    if (pc.acc) pc.acc[14] += 1;
     long long aa = 0, b0 = 0, sn, sj;
     const double2* base;
     if (mode) {
@@ -385,6 +429,7 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
       sj = 1;
     }
     tc_b_exponents(t, base, sn, sj);
+    pc.mark(10);
     // double-buffered chunks: the bulk copy and the slicing of chunk q + 1 overlap the
     // MMAs of chunk q
     if (threadIdx.x == 0) {
@@ -420,27 +465,43 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
     ok = tc_wait(&t.mbar[1], t.mph[1]) && ok;
     tc::fence_after();
     if (!ok && threadIdx.x == 0) atomicOr(a.err, tc::kErrMmaTimeout);
-    tc_drain_to_stage(t, Ei);
-    // stage -> out: element (i, n) = (stage[i][n], stage[64 + i][n])
-    for (int task = threadIdx.x; task < 64 * 64; task += blockDim.x) {
-      int i, n;
-      double2* dst;
-      if (mode) {
-        n = task & 63;
-        i = task >> 6;
-        dst = out + aa * 64 * nb + (long long)i * nb + b0 + n;
-      } else {
-        i = task & 63;
-        n = task >> 6;
-        dst = out + (b0 + n) * 64 + i;
+    pc.mark(11);
+    tc_drain_to_stage(t, Ei, pc);
+    pc.mark(12);
+    // stage -> out: element (i, n) = (stage[i][n], stage[64 + i][n]); 16 elements per
+    // thread in batches of 4 so that the loads of the accumulated outputs overlap
+    for (int r0 = 0; r0 < 16; r0 += 4) {
+      double2* dst[4];
+      double2 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int task = threadIdx.x + 256 * (r0 + u);
+        int i, n;
+        if (mode) {
+          n = task & 63;
+          i = task >> 6;
+          dst[u] = out + aa * 64 * nb + (long long)i * nb + b0 + n;
+        } else {
+          i = task & 63;
+          n = task >> 6;
+          dst[u] = out + (b0 + n) * 64 + i;
+        }
+        v[u] = make_double2(stage[i * TC_STAGE_LD + n], stage[(64 + i) * TC_STAGE_LD + n]);
       }
-      double2 v = make_double2(stage[i * TC_STAGE_LD + n], stage[(64 + i) * TC_STAGE_LD + n]);
-      if (acc) v = cadd(v, *dst);
-      *dst = v;
+      if (acc) {
+        double2 o[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) o[u] = *dst[u];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = cadd(v[u], o[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) *dst[u] = v[u];
     }
     // the next tile's bulk copies (async proxy) overwrite the stage just read
     tc::fence_proxy_async_all();
     __syncthreads();
+    pc.mark(13);
   }
 }
 
@@ -478,24 +539,6 @@ __device__ void reduce_partials(const double2* part, int nq, double2* out, Red& 
   }
   __syncthreads();
 }
-
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-// wall time per phase as seen by one thread of CTA 0 (barrier waits included)
-struct PhaseClock {
-  unsigned long long* acc;
-  unsigned long long t;
-  __device__ void mark(int k) {
-    if (acc) {
-      const unsigned long long now = gtimer();
-      acc[k] += now - t;
-      t = now;
-    }
-  }
-};
 
 // The small exponential of the step control, F = exp(zc * Haug) e1, by one warp.
 // Haug is the Lanczos tridiagonal (d on the diagonal, e[i] coupling rows i-1 and i) of

@@ -57,8 +57,10 @@ struct ExpmArgs {
                          // are distributed by tiles, not by the element-wise ownership the
                          // Lanczos passes assume)
 };
-constexpr int kPhases = 10;  // begin, matvec, alpha, reorth coefficients, reorth + norm,
-                             // ||H V_m||, control, combine, sub-steps, launches
+constexpr int kPhases = 16;  // begin, matvec, alpha, reorth coefficients, reorth + norm,
+                             // ||H V_m||, control, combine, sub-steps, launches; then inside
+                             // the tensor-core contractions: row exponents, chunk pipeline,
+                             // TMEM drain, output, tiles
 
 // co-resident CTAs for the plain (mixed = 0) or tensor-core (mixed = 1) configuration
 int expm_coop_max_grid(int mixed);

@@ -1073,7 +1073,7 @@ struct Integrator {
   // expm_cta_flops of matvec work.  Small problems run on few CTAs (one CTA synchronises
   // with __syncthreads alone, several need grid barriers of a few microseconds each),
   // large ones on the whole device.
-  double expm_cta_flops = 2.0e5;
+  double expm_cta_flops = 5.0e4;
   // threads per CTA: about expm_elems_per_thread vector elements per thread, 64..256 (the
   // FP64 warp reductions cost the same per warp whatever the data, so tiny problems run on
   // fewer warps)
@@ -1898,7 +1898,7 @@ int ttn_integrator_kernel_phases(ttn_integrator* it, double* out) {
   unsigned long long h[ttn::kPhases];
   CK(cudaMemcpy(h, I.phase_dev, sizeof(h), cudaMemcpyDeviceToHost));
   CK(cudaMemset(I.phase_dev, 0, sizeof(h)));
-  for (int k = 0; k < ttn::kPhases; ++k) out[k] = k < 8 ? 1e-6 * (double)h[k] : (double)h[k];
+  for (int k = 0; k < ttn::kPhases; ++k) out[k] = (k < 8 || (k >= 10 && k < 14) || k == 15) ? 1e-6 * (double)h[k] : (double)h[k];
   TTN_API_END
 }
 int ttn_debug_program_apply(ttn_integrator* it, int node, int kind, const double* v, double* out) {

@@ -839,7 +839,14 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
       // partial <V_j, p> over my elements (same element ownership as the last writes of p)
       {
         double2 s = make_double2(0.0, 0.0);
-        for (long long i = tid; i < n; i += nthreads) s = cadd(s, cmulc(Vj[i], a.p[i]));
+        // two elements per iteration (same summation order): twice the loads in flight
+        long long i = tid;
+        for (; i + nthreads < n; i += 2 * nthreads) {
+          const double2 v0 = Vj[i], p0 = a.p[i], v1 = Vj[i + nthreads], p1 = a.p[i + nthreads];
+          s = cadd(s, cmulc(v0, p0));
+          s = cadd(s, cmulc(v1, p1));
+        }
+        if (i < n) s = cadd(s, cmulc(Vj[i], a.p[i]));
         s.x = wsum(s.x);
         s.y = wsum(s.y);
         if (lane == 0) sm.w[warp][0] = s;
@@ -942,7 +949,15 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
         const int brk = (beta <= 1e-14 * (1.0 + anorm)) ? 1 : 0;
         const double inv = brk ? 0.0 : 1.0 / beta;
         double2* Vn = a.V + (long long)(j + 1) * a.ldv;
-        for (long long i = tid; i < n; i += nthreads) Vn[i] = cscale(inv, a.p[i]);
+        {
+          long long i = tid;
+          for (; i + nthreads < n; i += 2 * nthreads) {
+            const double2 p0 = a.p[i], p1 = a.p[i + nthreads];
+            Vn[i] = cscale(inv, p0);
+            Vn[i + nthreads] = cscale(inv, p1);
+          }
+          if (i < n) Vn[i] = cscale(inv, a.p[i]);
+        }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
           ctl->bet[j + 1] = brk ? 0.0 : beta;
           if (brk && ctl->mb == m) {

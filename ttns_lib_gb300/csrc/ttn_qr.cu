@@ -384,7 +384,12 @@ __global__ void __launch_bounds__(BT) k_qr_blocked(BqrArgs a) {
           S.beta = make_double2(ar, ai);
           S.scal = make_double2(0.0, 0.0);
         } else {
-          double bb = -copysign(dlapy3_b(ar, ai, xnorm), ar >= 0.0 ? 1.0 : -1.0);
+          // |(alpha, xnorm)| by one square root when no square can over- or underflow,
+          // else by the scaled dlapy3 form
+          const double w = fmax(fmax(fabs(ar), fabs(ai)), xnorm);
+          const bool safe = w > 1e-150 && w < 1e150;
+          double bb = -copysign(safe ? sqrt(fma(ar, ar, fma(ai, ai, xnorm * xnorm))) : dlapy3_b(ar, ai, xnorm),
+                                ar >= 0.0 ? 1.0 : -1.0);
           if (fabs(bb) < safmin) {
             const double rs = 1.0 / safmin;
             do {
@@ -397,7 +402,15 @@ __global__ void __launch_bounds__(BT) k_qr_blocked(BqrArgs a) {
             bb = -copysign(dlapy3_b(ar, ai, xnorm), ar >= 0.0 ? 1.0 : -1.0);
           }
           S.tau[j] = make_double2((bb - ar) / bb, -ai / bb);
-          S.scal = cdiv_b(make_double2(1.0, 0.0), make_double2(ar - bb, ai));
+          // 1 / (alpha - beta): |alpha - beta| >= |beta|, so in the safe range the squared
+          // magnitude is a normal number and one division suffices; else Smith's division
+          const double dr = ar - bb, di = ai;
+          if (fabs(bb) > 1e-150 && fabs(bb) < 1e150) {
+            const double inv = 1.0 / fma(dr, dr, di * di);
+            S.scal = make_double2(dr * inv, -di * inv);
+          } else {
+            S.scal = cdiv_b(make_double2(1.0, 0.0), make_double2(dr, di));
+          }
           for (int q = 0; q < knt; ++q) bb *= safmin;
           S.beta = make_double2(bb, 0.0);
           S.active = 1;

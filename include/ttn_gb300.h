@@ -106,6 +106,17 @@ int ttn_integrator_destroy(ttn_integrator* it);
 int ttn_integrator_set_dt(ttn_integrator* it, double dt);
 int ttn_integrator_dt(const ttn_integrator* it, double* out);
 int ttn_integrator_t(const ttn_integrator* it, double* out);
+/* Batched form: advance n independent instances by one step each (instance k = its[k]
+ * with states[k]; distinct integrators and states, any mix of trees, operators and
+ * devices).  Instances are stepped from `threads` host threads (0: the hardware
+ * concurrency), each integrator on its own stream, so small instances overlap on the GPU.
+ * Equivalent to calling ttn_integrator_step on each instance in turn (same results); on
+ * failure returns the first failing instance's status and message and its index in
+ * *failed (-1 when all succeed).  The reference steps one instance per
+ * projector_splitting_integrator::operator() (projector_splitting_integrator.hpp:136-169)
+ * from its driver loop (src/spin_boson.cpp:81-105); it has no batched call. */
+int ttn_batch_step(ttn_integrator* const* its, ttn_state* const* states, int n, double coeff_re, double coeff_im,
+                   int threads, int* failed);
 /* One call = one step of dt of exp(coeff * H t) (coeff = -i for Schroedinger
  * dynamics); the first call prepares the environments and sub-steps dt as
  * dt*1e-5, dt*1e-4, ... exactly as the reference integrator does. */
@@ -127,6 +138,12 @@ int ttn_integrator_flops(const ttn_integrator* it, double* out);
 int ttn_integrator_timer(ttn_integrator* it, int start, double* ms);
 
 /* ---- observables ----------------------------------------------------------------- */
+/* Schmidt values ("pops") across the bond above `node` (1 <= node < nodes), descending,
+ * hrank[node] values into out (count in *n); the state must be in the orthogonalised form
+ * the sweep leaves.  Replaces the bond singular values of decomposition_engine
+ * (include/ttns_lib/tdvp_core/decomposition_engine.hpp:111-205,
+ * the S() read after a step) as reported by the reference driver. */
+int ttn_bond_singular_values(ttn_integrator* it, ttn_state* psi, int node, double* out, int* n);
 /* <psi| O_mode |psi> with a dense d x d operator on one leaf mode */
 int ttn_expect_leaf(ttn_integrator* it, ttn_state* psi, int mode, const double* op, double* re,
                     double* im);

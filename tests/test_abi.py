@@ -75,3 +75,17 @@ def test_operator_validation_on_host():
     assert api.lib().ttn_sop_set_coeff(h, 0, float("nan"), 0.0) == api.TTN_EINVAL
     api.lib().ttn_sop_destroy(h)
     del op
+
+
+def test_batch_step_validates_on_host():
+    L = api.lib()
+    failed = C.c_int(5)
+    assert L.ttn_batch_step(None, None, 1, 0.0, -1.0, 0, C.byref(failed)) == api.TTN_EINVAL
+    empty = (C.c_void_p * 1)()
+    assert L.ttn_batch_step(empty, empty, 0, 0.0, -1.0, 0, C.byref(failed)) == api.TTN_OK
+    assert failed.value == -1
+    assert L.ttn_batch_step(empty, empty, 1, 0.0, -1.0, 0, C.byref(failed)) == api.TTN_EINVAL
+    assert b"null instance" in L.ttn_last_error()
+    with pytest.raises(ValueError):
+        api.batch_step([object()], [], -1j)
+

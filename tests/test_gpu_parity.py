@@ -143,6 +143,25 @@ def test_full_rank_random_tree_matches_dense_expm(seed):
         assert np.linalg.norm(full_state(topo, A.get()) - ex) < 1e-10
 
 
+def test_bond_singular_values_match_oracle():
+    m, cfg = spin_boson_small()
+    topo = m.topology
+    st = generic_state(topo, np.random.default_rng(8))
+    orc, A, dev = make_pair(topo, m.sop, st, m=cfg["krylov_dim"])
+    dev.dt = cfg["dt"]
+    for k in range(3):
+        for node in range(1, topo.nnodes):
+            so = orc.bond_sv(node)
+            sd = dev.bond_sv(A, node)
+            assert sd.shape == so.shape
+            assert np.abs(sd - so).max() < 1e-12 * max(1.0, so.max()), (k, node)
+        orc.step(cfg["dt"])
+        dev(A, m.sop, -1j)
+    # a normalised state: the squared Schmidt values of every bond sum to 1
+    for node in range(1, topo.nnodes):
+        assert abs(np.sum(dev.bond_sv(A, node) ** 2) - 1.0) < 1e-12
+
+
 def test_init_product_state_structure():
     m, cfg = spin_boson_small()
     topo = m.topology

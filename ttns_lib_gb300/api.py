@@ -100,6 +100,8 @@ SIGNATURES = {
     "ttn_debug_get_env": (_I, [_P, _I, _I, _I, _DP]),
     "ttn_debug_qr": (_I, [_I, _I, _DP, _DP, _I]),
     "ttn_qr_noalloc": (_I, [_I, _I, _P, _P, _P, _I]),
+    "ttn_bond_singular_values": (_I, [_P, _P, _I, _DP, C.POINTER(C.c_int)]),
+    "ttn_batch_step": (_I, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _I, _D, _D, _I, C.POINTER(C.c_int)]),
     "ttn_debug_tc_gemm": (_I, [_DP, _DP, _DP, _I, _I, _I]),
 }
 
@@ -356,6 +358,13 @@ class fixed_step_projector_splitting_integrator:
         _check(lib().ttn_bench_node_op(self.h, A.h, node, kind, reps, C.byref(ms), C.byref(fl)))
         return ms.value, fl.value
 
+    def bond_sv(self, A: httensor, node: int) -> np.ndarray:
+        """Schmidt values across the bond above ``node`` (descending)."""
+        out = np.zeros(int(self.topo.hrank[node]))
+        n = C.c_int()
+        _check(lib().ttn_bond_singular_values(self.h, A.h, node, _dp(out), C.byref(n)))
+        return out[:n.value]
+
     def mel(self) -> matrix_element:
         return self._mel
 
@@ -426,3 +435,16 @@ def device_qr(a: np.ndarray, device: int = 0):
     r = np.zeros((n, n), dtype=np.complex128)
     _check(lib().ttn_debug_qr(m, n, _dp(a.view(np.float64)), _dp(r.view(np.float64)), device))
     return a, r
+
+
+def batch_step(integrators, states, coeff: complex = -1j, threads: int = 0):
+    """Advance independent instances (integrator k with state k) by one step each,
+    concurrently from ``threads`` host threads (0: all hardware threads)."""
+    n = len(integrators)
+    if len(states) != n:
+        raise ValueError("one state per integrator")
+    its = (C.c_void_p * max(n, 1))(*[it.h for it in integrators])
+    sts = (C.c_void_p * max(n, 1))(*[st.h for st in states])
+    failed = C.c_int(-1)
+    _check(lib().ttn_batch_step(its, sts, n, coeff.real, coeff.imag, int(threads), C.byref(failed)))
+

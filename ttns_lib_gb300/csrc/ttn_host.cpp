@@ -20,6 +20,8 @@
 #include <chrono>
 #include <cstdlib>
 #include <cmath>
+#include <atomic>
+#include <thread>
 #include <complex>
 #include <cstring>
 #include <map>
@@ -657,9 +659,10 @@ struct Integrator {
     zgemm(g, gws, gws_bytes, stream);
   }
   // out(x,k) = alpha sum_l in(x,l) M(k,l) (+ out)
-  void mf_apply(const double2* in, const double2* M, int r, long long nx, double2* out, cd alpha, bool acc) {
+  void mf_apply(const double2* in, const double2* M, int r, long long nx, double2* out, cd alpha, bool acc,
+                bool allow_tc = true) {
     flops += 8.0 * nx * (double)r * r;
-    if (tc_apply(MV_MF, M, in, out, nx, r, 0, alpha, acc)) return;
+    if (allow_tc && tc_apply(MV_MF, M, in, out, nx, r, 0, alpha, acc)) return;
     ZGemm g{};
     g.M = (int)nx; g.N = r; g.K = r;
     g.A = op_rowmajor(in, r);
@@ -1319,6 +1322,67 @@ struct Integrator {
 
   // ---------------------------------------------------------------- observables
   // (always FP64, also in mixed precision)
+
+  // Schmidt values across the bond above node nd, for the orthogonalised form the sweep
+  // leaves (every non-root node an isometry): the bond's density matrix from the root down
+  // the path (mean-field product and mode contraction per node, FP64 on the device), then a
+  // cyclic Hermitian Jacobi eigen-solve on the host; sqrt of the eigenvalues, descending
+  // (matrix_element / decomposition_engine singular values of the reference, S() = "pops").
+  std::vector<double> bond_sv(ttn_state* S, int nd) {
+    std::vector<int> path;
+    for (int x = nd; x != 0; x = T.parent[x]) path.push_back(x);
+    std::reverse(path.begin(), path.end());
+    const int r0 = T.hrank[0];
+    std::vector<double2> eye((size_t)r0 * r0, make_double2(0.0, 0.0));
+    for (int k = 0; k < r0; ++k) eye[(size_t)k * r0 + k] = make_double2(1.0, 0.0);
+    CK(cudaMemcpyAsync(w2, eye.data(), eye.size() * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    h2d_bytes += (long long)eye.size() * sizeof(double2);
+    for (int c : path) {
+      const int p = T.parent[c];
+      long long na, nb;
+      int d;
+      r3(p, T.slot[c], na, d, nb);
+      const long long sz = T.size(p);
+      mf_apply(S->node(p), w2, T.hrank[p], sz / T.hrank[p], w1, 1.0, false, false);
+      mode_contract(S->node(p), w1, na, d, nb, w2, 1.0, false);
+    }
+    const int d = T.hrank[nd];
+    std::vector<cd> a((size_t)d * d);
+    CK(cudaMemcpyAsync(a.data(), w2, a.size() * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+    d2h_bytes += (long long)a.size() * sizeof(double2);
+    CK(cudaStreamSynchronize(stream));
+    for (int sweepi = 0; sweepi < 100; ++sweepi) {
+      double off = 0.0;
+      for (int i = 0; i < d; ++i)
+        for (int j = i + 1; j < d; ++j) off += std::norm(a[(size_t)i * d + j]);
+      if (off < 1e-30) break;
+      for (int pp = 0; pp < d; ++pp)
+        for (int q = pp + 1; q < d; ++q) {
+          const cd apq = a[(size_t)pp * d + q];
+          const double ab = std::abs(apq);
+          if (ab < 1e-300) continue;
+          const double app = a[(size_t)pp * d + pp].real(), aqq = a[(size_t)q * d + q].real();
+          const double th = 0.5 * std::atan2(2.0 * ab, aqq - app);
+          const double c = std::cos(th), sn = std::sin(th);
+          const cd ph = apq / ab;
+          // a <- J^H a J with J_pp = J_qq = c, J_pq = sn ph, J_qp = -sn conj(ph)
+          for (int k = 0; k < d; ++k) {
+            const cd akp = a[(size_t)k * d + pp], akq = a[(size_t)k * d + q];
+            a[(size_t)k * d + pp] = c * akp - sn * std::conj(ph) * akq;
+            a[(size_t)k * d + q] = sn * ph * akp + c * akq;
+          }
+          for (int k = 0; k < d; ++k) {
+            const cd apk = a[(size_t)pp * d + k], aqk = a[(size_t)q * d + k];
+            a[(size_t)pp * d + k] = c * apk - sn * ph * aqk;
+            a[(size_t)q * d + k] = sn * std::conj(ph) * apk + c * aqk;
+          }
+        }
+    }
+    std::vector<double> sv(d);
+    for (int i = 0; i < d; ++i) sv[i] = std::sqrt(std::max(0.0, a[(size_t)i * d + i].real()));
+    std::sort(sv.begin(), sv.end(), std::greater<double>());
+    return sv;
+  }
   cd expect(ttn_state* S, int mode, const double2* op_dev) {
     for (int id = T.n - 1; id >= 0; --id) {
       const int r = T.hrank[id];
@@ -1664,6 +1728,42 @@ int ttn_integrator_step(ttn_integrator* it, ttn_state* psi, double cre, double c
   if (dt_out) *dt_out = dt;
   TTN_API_END
 }
+int ttn_batch_step(ttn_integrator* const* its, ttn_state* const* states, int n, double cre, double cim, int threads,
+                   int* failed) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(its && states && n >= 0, TTN_EINVAL, "null argument");
+  if (failed) *failed = -1;
+  if (n == 0) return TTN_OK;
+  for (int k = 0; k < n; ++k) {
+    TTN_REQUIRE(its[k] && states[k], TTN_EINVAL, "null instance");
+    for (int q = 0; q < k; ++q)
+      TTN_REQUIRE(its[q] != its[k] && states[q] != states[k], TTN_EINVAL,
+                  "instances must use distinct integrators and states");
+  }
+  int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+  nt = std::max(1, std::min(nt, n));
+  std::atomic<int> next{0};
+  std::vector<int> rc(n, TTN_OK);
+  std::vector<std::string> msg(n);
+  // every worker steps whole instances (each integrator has its own stream, so instances
+  // run concurrently on the device and their kernel launches are issued in parallel)
+  auto work = [&]() {
+    for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1)) {
+      rc[k] = ttn_integrator_step(its[k], states[k], cre, cim, nullptr);
+      if (rc[k] != TTN_OK) msg[k] = ttn::g_err;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int w = 1; w < nt; ++w) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+  for (int k = 0; k < n; ++k)
+    if (rc[k] != TTN_OK) {
+      if (failed) *failed = k;
+      throw ttn::Err(rc[k], "instance " + std::to_string(k) + ": " + msg[k]);
+    }
+  TTN_API_END
+}
 int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out) {
   TTN_API_BEGIN
   TTN_REQUIRE(it && out, TTN_EINVAL, "null argument");
@@ -1702,6 +1802,17 @@ int ttn_expect_leaf(ttn_integrator* it, ttn_state* psi, int mode, const double* 
   ttn::cd v = it->I.expect(psi, mode, dop);
   if (re) *re = v.real();
   if (im) *im = v.imag();
+  TTN_API_END
+}
+int ttn_bond_singular_values(ttn_integrator* it, ttn_state* psi, int node, double* out, int* n) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi && out, TTN_EINVAL, "null argument");
+  ttn::check_same_tree(it->I.T, psi->T);
+  TTN_REQUIRE(node >= 1 && node < it->I.T.n, TTN_EINVAL, "node must name a bond (1 <= node < nodes)");
+  CK(cudaSetDevice(it->I.device));
+  const auto sv = it->I.bond_sv(psi, node);
+  for (size_t k = 0; k < sv.size(); ++k) out[k] = sv[k];
+  if (n) *n = (int)sv.size();
   TTN_API_END
 }
 int ttn_norm2(ttn_integrator* it, ttn_state* psi, double* out) {

@@ -1942,7 +1942,7 @@ int ttn_host_free(void* p) {
 int ttn_launch_count(unsigned long long* out) {
   TTN_API_BEGIN
   TTN_REQUIRE(out, TTN_EINVAL, "null argument");
-  *out = ttn::g_launches;
+  *out = ttn::g_launches.load();
   TTN_API_END
 }
 int ttn_device_fp64_peak(int device, double* tflops) {

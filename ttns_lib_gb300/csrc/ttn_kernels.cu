@@ -21,7 +21,7 @@
 namespace ttn {
 
 // kernel launches issued by this library (host-side counter)
-unsigned long long g_launches = 0;
+std::atomic<unsigned long long> g_launches{0};
 
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }

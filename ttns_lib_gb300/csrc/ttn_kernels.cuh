@@ -2,11 +2,14 @@
 // device code (ttn_kernels.cu, ttn_tc.cu).  Not part of the public C-ABI.
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 
 namespace ttn {
 
-extern unsigned long long g_launches;  // kernel launches issued by this library
+// kernel launches issued by this library (atomic: ttn_batch_step launches from several
+// host threads)
+extern std::atomic<unsigned long long> g_launches;
 
 // Element addressing of a GEMM operand.
 //   A(i,k) = p[i*s0 + (k/kdiv)*k1 + (k%kdiv)*k2]        (conj if cj)

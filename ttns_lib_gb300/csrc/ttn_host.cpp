@@ -396,7 +396,7 @@ struct Integrator {
   DevBuf ops_buf, env_buf, r_buf, work_buf, ctl_buf, mel_buf;
   std::vector<std::vector<double2*>> leaf_ops;  // [mode][k]
   std::vector<double2*> rmat, mel;
-  double2 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w4 = nullptr, *V = nullptr, *p = nullptr, *part = nullptr,
+  double2 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w4 = nullptr, *V = nullptr, *p = nullptr,
           *gws = nullptr, *qtau = nullptr, *scal = nullptr;
   size_t gws_bytes = 0;
   long long maxsize = 0, ldv = 0;
@@ -418,8 +418,6 @@ struct Integrator {
   long long* nh_dev = nullptr;
   double* flops_dev = nullptr;   // matvec flops executed by the persistent kernels
   // host mirrors
-  struct HostCtl { int done, err; long long napps; };
-  HostCtl* hctl = nullptr;  // pinned
   double dt = 0.0, t_engine = 0.0;
   cd coeff = cd(0.0, -1.0);
   long long nsteps = 0, nh = 0;
@@ -449,13 +447,10 @@ struct Integrator {
     }
   };
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  TcEngine* tc = nullptr;  // tensor-core contraction engine (mixed precision)
 
   ~Integrator() {
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
-    if (tc) tc_destroy(tc);
-    if (hctl) cudaFreeHost(hctl);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -551,7 +546,6 @@ struct Integrator {
     wb += 4 * align256(ldv * sizeof(double2));                   // w1..w4
     wb += (size_t)(m + 1) * ldv * sizeof(double2);               // V
     wb += align256(ldv * sizeof(double2));                        // p
-    wb += align256(lanczos_partial_bytes());                      // partials
     wb += gws_bytes;                                              // zgemm split-K
     wb += align256(kQrMaxCols * sizeof(double2));                 // QR tau
     wb += align256(64 * sizeof(double2));                         // scalars
@@ -566,7 +560,6 @@ struct Integrator {
       w4 = take(ldv * sizeof(double2));
       V = take((size_t)(m + 1) * ldv * sizeof(double2));
       p = take(ldv * sizeof(double2));
-      part = take(lanczos_partial_bytes());
       gws = take(gws_bytes);
       qtau = take(kQrMaxCols * sizeof(double2));
       scal = take(64 * sizeof(double2));
@@ -576,7 +569,6 @@ struct Integrator {
     status = (int*)(ctl_buf.as<char>() + align256(sizeof(KrylovCtl)));
     if (profiling) phase_dev = (unsigned long long*)(ctl_buf.as<char>() + align256(sizeof(KrylovCtl)) + 256);
     CK(cudaMemsetAsync(ctl_buf.p, 0, ctl_buf.bytes, stream));
-    CK(cudaMallocHost((void**)&hctl, sizeof(HostCtl)));
     CK(cudaEventCreate(&ev0));
     CK(cudaEventCreate(&ev1));
     {
@@ -676,7 +668,6 @@ struct Integrator {
   // out(i,j) = alpha sum_x conj(A(x,i)) X(x,j) (+ out)
   void adj_mul(const double2* A, const double2* X, long long nx, int r, double2* out, cd alpha, bool acc) {
     flops += 8.0 * nx * (double)r * r;
-    if (tc && tc_adj_mul(tc, A, X, nx, r, out, d2(alpha), acc, stream)) return;
     ZGemm g{};
     g.M = r; g.N = r; g.K = (int)nx;
     g.A = op_colk(A, r, 1);
@@ -692,7 +683,6 @@ struct Integrator {
   void mode_contract(const double2* A, const double2* Tt, long long na, int d, long long nb, double2* out, cd alpha,
                      bool acc) {
     flops += 8.0 * na * nb * (double)d * d;
-    if (tc && tc_mode_contract(tc, A, Tt, na, d, nb, out, d2(alpha), acc, stream)) return;
     ZGemm g{};
     g.M = d; g.N = d; g.K = (int)(na * nb);
     ZOperand o{A, nb, (long long)d * nb, 1, nb, 1, 1};
@@ -900,32 +890,6 @@ struct Integrator {
     }
     return f;
   }
-  // out = K_bond(nd) R (full_hamiltonian_action)
-  void kbond(int nd, const double2* R, double2* out) {
-    const int r = T.hrank[nd];
-    bool first = true;
-    for (auto& g : G[nd]) {
-      const double2* X = R;
-      if (!g.id_spf) {
-        flops += 8.0 * (double)r * r * r;
-        ZGemm gg{};
-        gg.M = r; gg.N = r; gg.K = r;
-        gg.A = op_rowmajor(g.spf_dev, r);
-        gg.B = op_colk(R, r, 1);
-        gg.C = w1; gg.ci = r; gg.cj = 1;
-        gg.batch = 1;
-        gg.alpha = make_double2(1.0, 0.0);
-        gg.beta = make_double2(0.0, 0.0);
-        zgemm(gg, gws, gws_bytes, stream);
-        X = w1;
-      }
-      if (g.id_mf) mode_identity_axpy(X, out, (long long)r * r, g.s, !first);
-      else mf_apply(X, g.mf_dev, r, r, out, g.s, !first);
-      first = false;
-    }
-    if (first) zfill(out, make_double2(0.0, 0.0), (long long)r * r, stream);
-  }
-
   // ---------------------------------------------------------------- matvec programs
   // Barriers go where one contraction reads a buffer another wrote (or overwrites one
   // another read) since the last barrier.  The element-wise FP64 contractions give output
@@ -1127,36 +1091,6 @@ struct Integrator {
     for (int j = 0; j < m; ++j) vec += (8.0 + 8.0 + 16.0 * (j + 1) + 4.0 + 2.0) * n;
     vec += (4.0 + 8.0 * (m + 1)) * n;
     return vec;
-  }
-
-  // ---------------------------------------------------------------- Krylov exponential
-  template <typename Op>
-  void expm(Op&& hop, double2* y, long long n, double tau, cd cf, bool count) {
-    if (tau == 0.0) return;
-    const int m = cfg.krylov_dim;
-    krylov_init_ctl(ctl, m, tau, cf.real(), cf.imag(), cfg.krylov_tol, stream);
-    for (int sub = 0;; ++sub) {
-      TTN_REQUIRE(sub < 100000, TTN_ENUMERIC, "Krylov exponential did not finish");
-      krylov_begin(ctl, y, V, n, part, stream);
-      for (int j = 0; j < m; ++j) {
-        hop(V + (long long)j * ldv, p);
-        lanczos_orth(ctl, j, V, ldv, p, n, part, stream);
-      }
-      hop(V + (long long)m * ldv, p);
-      lanczos_avnorm(ctl, p, n, part, stream);
-      // vector passes: per iteration j: <V_j,p>, two real axpys, (j+1) dots and axpys, a norm
-      for (int j = 0; j < m; ++j) flops += (8.0 + 8.0 + 16.0 * (j + 1) + 4.0 + 2.0) * n;
-      flops += (4.0 + 8.0 * (m + 1)) * n;
-      krylov_control(ctl, stream);
-      krylov_combine(ctl, V, ldv, y, n, m + 1, stream);
-      CK(cudaMemcpyAsync(&hctl->done, &ctl->done, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream));
-      CK(cudaMemcpyAsync(&hctl->napps, &ctl->napps, sizeof(long long), cudaMemcpyDeviceToHost, stream));
-      d2h_bytes += sizeof(int) * 2 + sizeof(long long);
-      CK(cudaStreamSynchronize(stream));
-      TTN_REQUIRE(hctl->err == 0, TTN_ENUMERIC, "Krylov exponential failed (tolerance unreachable or non-finite values)");
-      if (hctl->done) break;
-    }
-    if (count) nh += hctl->napps;
   }
 
   // ---------------------------------------------------------------- gauge moves

@@ -255,470 +255,9 @@ void zgemm(const ZGemm& g, double2* ws, size_t ws_bytes, cudaStream_t s) {
 }
 
 // =====================================================================================
-// Lanczos vector passes
+// Block reductions and scalar helpers of the cooperative Householder QR; layout kernels
 // =====================================================================================
 namespace {
-constexpr int VT = 256;       // threads per block
-constexpr int VQ = 72;        // max vectors reduced in one pass
-constexpr int VMAXB = 512;    // max blocks of a pass
-
-// Block-reduce nq complex partials held as (per-warp) shared sums; writes part[block*nq + q].
-struct RedSmem {
-  double2 w[VT / 32][VQ];
-};
-
-__device__ void block_store_partials(RedSmem& sm, int nq, double2* part) {
-  __syncthreads();
-  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-    double2 s = make_double2(0.0, 0.0);
-    for (int w = 0; w < VT / 32; ++w) s = cadd(s, sm.w[w][q]);
-    part[(long long)blockIdx.x * nq + q] = s;
-  }
-}
-
-// Every block sums the partials of the previous pass in the same order (deterministic).
-__device__ double2 sum_partials(const double2* part, int nblocks, int nq, int q) {
-  double2 s = make_double2(0.0, 0.0);
-  for (int b = 0; b < nblocks; ++b) s = cadd(s, part[(long long)b * nq + q]);
-  return s;
-}
-
-__global__ void k_norm_partial(const double2* __restrict__ x, long long n, double2* part) {
-  __shared__ RedSmem sm;
-  double s = 0.0;
-  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
-    double2 v = x[i];
-    s += v.x * v.x + v.y * v.y;
-  }
-  s = warp_sum(s);
-  if ((threadIdx.x & 31) == 0) sm.w[threadIdx.x >> 5][0] = make_double2(s, 0.0);
-  block_store_partials(sm, 1, part);
-}
-
-// V0 = y / ||y||; block 0 records beta.
-__global__ void k_begin(KrylovCtl* ctl, const double2* __restrict__ y, double2* __restrict__ V0, long long n,
-                        const double2* part, int nparts) {
-  __shared__ double sbeta;
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < nparts; ++b) s += part[b].x;
-    sbeta = sqrt(s);
-  }
-  __syncthreads();
-  double beta = sbeta;
-  double inv = beta > 0.0 ? 1.0 / beta : 0.0;
-  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
-    V0[i] = cscale(inv, y[i]);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    ctl->beta = beta;
-    ctl->mb = ctl->m;
-    ctl->k1 = 2;
-    ctl->bet[0] = 0.0;
-    if (!(beta > 0.0) || !isfinite(beta)) {
-      ctl->done = 1;
-      if (!isfinite(beta)) ctl->err |= 2;
-    }
-  }
-}
-
-// pass 1: partial <V_j, p>
-__global__ void k_orth1(const double2* __restrict__ Vj, const double2* __restrict__ p, long long n, double2* part) {
-  __shared__ RedSmem sm;
-  double2 s = make_double2(0.0, 0.0);
-  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
-    s = cadd(s, cmulc(Vj[i], p[i]));
-  s = warp_sum2(s);
-  if ((threadIdx.x & 31) == 0) sm.w[threadIdx.x >> 5][0] = s;
-  block_store_partials(sm, 1, part);
-}
-
-// pass 2: alpha = Re<V_j,p>; p -= alpha V_j + bet_j V_{j-1}; partial h_q = <V_q, p>, q <= j
-__global__ void k_orth2(KrylovCtl* ctl, int j, const double2* __restrict__ V, long long ldv, double2* __restrict__ p,
-                        long long n, const double2* part_in, int nparts, double2* part_out) {
-  __shared__ RedSmem sm;
-  __shared__ double salpha;
-  if (threadIdx.x == 0) salpha = sum_partials(part_in, nparts, 1, 0).x;
-  __syncthreads();
-  const double a = salpha;
-  const double bj = (j > 0) ? ctl->bet[j] : 0.0;
-  const double2* Vj = V + (long long)j * ldv;
-  const double2* Vm = V + (long long)(j > 0 ? j - 1 : 0) * ldv;
-  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
-    double2 x = p[i];
-    double2 vj = Vj[i];
-    x.x -= a * vj.x;
-    x.y -= a * vj.y;
-    if (j > 0) {
-      double2 vm = Vm[i];
-      x.x -= bj * vm.x;
-      x.y -= bj * vm.y;
-    }
-    p[i] = x;
-  }
-  // p was only touched element-wise by this thread; dots use the updated values
-  for (int q = 0; q <= j; ++q) {
-    const double2* Vq = V + (long long)q * ldv;
-    double2 s = make_double2(0.0, 0.0);
-    for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
-      s = cadd(s, cmulc(Vq[i], p[i]));
-    s = warp_sum2(s);
-    if ((threadIdx.x & 31) == 0) sm.w[threadIdx.x >> 5][q] = s;
-  }
-  block_store_partials(sm, j + 1, part_out);
-  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->alpha[j] = a;
-}
-
-// pass 3: p -= sum_q h_q V_q; partial ||p||^2
-__global__ void k_orth3(int j, const double2* __restrict__ V, long long ldv, double2* __restrict__ p, long long n,
-                        const double2* part_in, int nparts, double2* part_out) {
-  __shared__ RedSmem sm;
-  __shared__ double2 h[VQ];
-  for (int q = threadIdx.x; q <= j; q += blockDim.x) h[q] = sum_partials(part_in, nparts, j + 1, q);
-  __syncthreads();
-  double s = 0.0;
-  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
-    double2 x = p[i];
-    for (int q = 0; q <= j; ++q) {
-      double2 v = V[(long long)q * ldv + i];
-      double2 hv = cmul(h[q], v);
-      x = csub(x, hv);
-    }
-    p[i] = x;
-    s += x.x * x.x + x.y * x.y;
-  }
-  s = warp_sum(s);
-  if ((threadIdx.x & 31) == 0) sm.w[threadIdx.x >> 5][0] = make_double2(s, 0.0);
-  block_store_partials(sm, 1, part_out);
-}
-
-// pass 4: beta_{j+1} = ||p||; breakdown test; V_{j+1} = p / beta (or 0)
-__global__ void k_orth4(KrylovCtl* ctl, int j, double2* __restrict__ V, long long ldv, const double2* __restrict__ p,
-                        long long n, const double2* part_in, int nparts) {
-  __shared__ double sb;
-  __shared__ int sbreak;
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < nparts; ++b) s += part_in[b].x;
-    double beta = sqrt(s);
-    double anorm = 0.0;
-    for (int q = 0; q <= j; ++q) {
-      double nb = (q < j) ? ctl->bet[q + 1] : beta;
-      double v = fabs(ctl->alpha[q]) + ctl->bet[q] + nb;
-      anorm = v > anorm ? v : anorm;
-    }
-    sb = beta;
-    sbreak = (beta <= 1e-14 * (1.0 + anorm)) ? 1 : 0;
-  }
-  __syncthreads();
-  const double beta = sb;
-  const int brk = sbreak;
-  const double inv = brk ? 0.0 : 1.0 / beta;
-  double2* Vn = V + (long long)(j + 1) * ldv;
-  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT)
-    Vn[i] = cscale(inv, p[i]);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    ctl->bet[j + 1] = brk ? 0.0 : beta;
-    if (brk && ctl->mb == ctl->m) {
-      ctl->mb = j + 1;
-      ctl->k1 = 0;
-    }
-    if (!isfinite(beta)) ctl->err |= 2;
-  }
-}
-
-// ---- small dense math for the controller (single thread) ---------------------------
-// Implicit-QL eigen-decomposition of a symmetric tridiagonal matrix (EISPACK tql2
-// scheme).  z is n x n row-major, columns are eigenvectors.
-__device__ int dev_tql2(int n, double* d, double* e, double* z) {
-  for (int i = 0; i < n; ++i)
-    for (int k = 0; k < n; ++k) z[i * n + k] = (i == k) ? 1.0 : 0.0;
-  for (int l = 0; l < n; ++l) {
-    int iter = 0, m;
-    for (;;) {
-      for (m = l; m < n - 1; ++m) {
-        double dd = fabs(d[m]) + fabs(d[m + 1]);
-        if (fabs(e[m]) <= 1e-300 + 2.220446049250313e-16 * dd) break;
-      }
-      if (m == l) break;
-      if (++iter > 60) return 1;
-      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-      double r = hypot(g, 1.0);
-      g = d[m] - d[l] + e[l] / (g + (g >= 0.0 ? fabs(r) : -fabs(r)));
-      double s = 1.0, c = 1.0, p = 0.0;
-      bool underflow = false;
-      for (int i = m - 1; i >= l; --i) {
-        double f = s * e[i], b = c * e[i];
-        r = hypot(f, g);
-        e[i + 1] = r;
-        if (r == 0.0) {
-          d[i + 1] -= p;
-          e[m] = 0.0;
-          underflow = true;
-          break;
-        }
-        s = f / r;
-        c = g / r;
-        g = d[i + 1] - p;
-        r = (d[i] - g) * s + 2.0 * c * b;
-        p = s * r;
-        d[i + 1] = g + p;
-        g = c * r - b;
-        for (int k = 0; k < n; ++k) {
-          f = z[k * n + i + 1];
-          z[k * n + i + 1] = s * z[k * n + i] + c * f;
-          z[k * n + i] = c * z[k * n + i] - s * f;
-        }
-      }
-      if (underflow) continue;
-      d[l] -= p;
-      e[l] = g;
-      e[m] = 0.0;
-    }
-  }
-  return 0;
-}
-
-__device__ double2 cexp_d(double2 x) {
-  double ex = exp(x.x);
-  double sn, cs;
-  sincos(x.y, &sn, &cs);
-  return make_double2(ex * cs, ex * sn);
-}
-__device__ double cabs_d(double2 x) { return hypot(x.x, x.y); }
-// a / b by Smith's algorithm (CACM 5(8), 1962): no squared magnitudes, so no spurious
-// underflow or overflow for very small or very large b.
-__device__ double2 cdiv_d(double2 a, double2 b) {
-  if (fabs(b.x) >= fabs(b.y)) {
-    double r = b.y / b.x, den = b.x + b.y * r;
-    return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
-  }
-  double r = b.x / b.y, den = b.x * r + b.y;
-  return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
-}
-// phi_1(x) = (e^x - 1)/x, phi_2(x) = (e^x - 1 - x)/x^2
-__device__ double2 dphi1(double2 x) {
-  if (cabs_d(x) < 0.5) {
-    double2 s = make_double2(0.0, 0.0), t = make_double2(1.0, 0.0);
-    for (int k = 1; k <= 18; ++k) {
-      s = cadd(s, t);
-      t = cscale(1.0 / double(k + 1), cmul(t, x));
-    }
-    return s;
-  }
-  double2 ex = cexp_d(x);
-  return cdiv_d(make_double2(ex.x - 1.0, ex.y), x);
-}
-__device__ double2 dphi2(double2 x) {
-  if (cabs_d(x) < 0.5) {
-    double2 s = make_double2(0.0, 0.0), t = make_double2(0.5, 0.0);
-    for (int k = 2; k <= 20; ++k) {
-      s = cadd(s, t);
-      t = cscale(1.0 / double(k + 1), cmul(t, x));
-    }
-    return s;
-  }
-  double2 ex = cexp_d(x);
-  return cdiv_d(make_double2(ex.x - 1.0 - x.x, ex.y - x.y), cmul(x, x));
-}
-
-__global__ void k_avnorm(KrylovCtl* ctl, const double2* part, int nparts) {
-  if (threadIdx.x != 0) return;
-  double s = 0.0;
-  for (int b = 0; b < nparts; ++b) s += part[b].x;
-  ctl->avnorm = sqrt(s);
-}
-
-// Expokit step control on the mb x mb tridiagonal (single thread; m <= 64).
-__global__ void k_control(KrylovCtl* ctl) {
-  __shared__ double z[64 * 64];
-  __shared__ double d[64], e[64];
-  __shared__ double2 F[66];
-  if (threadIdx.x != 0) return;
-  if (ctl->done) {
-    for (int q = 0; q < 2 * 72; ++q) ctl->coef[q] = 0.0;
-    return;
-  }
-  const int m = ctl->m, mb = ctl->mb, k1 = ctl->k1;
-  const double tol = ctl->tol, gamma = 0.9, delta = 1.2;
-  const double beta = ctl->beta, avnorm = ctl->avnorm;
-  double t_step = fmin(ctl->t_out - ctl->t_now, ctl->t_new);
-  if (k1 == 0) t_step = ctl->t_out - ctl->t_now;
-  for (int i = 0; i < mb; ++i) d[i] = ctl->alpha[i];
-  for (int i = 0; i + 1 < mb; ++i) e[i] = ctl->bet[i + 1];
-  e[mb - 1] = 0.0;
-  if (dev_tql2(mb, d, e, z)) {
-    ctl->err |= 4;
-    ctl->done = 1;
-    return;
-  }
-  const double2 cf = make_double2(ctl->cf_re, ctl->cf_im);
-  double err_loc = 0.0, xm = 1.0 / m;
-  int ireject = 0;
-  for (;;) {
-    double2 zc = cscale(ctl->sgn * t_step, cf);
-    for (int i = 0; i < mb; ++i) {
-      double2 s = make_double2(0.0, 0.0);
-      for (int q = 0; q < mb; ++q) {
-        double2 ex = cexp_d(cscale(d[q], zc));
-        s = cadd(s, cscale(z[i * mb + q] * z[q], ex));
-      }
-      F[i] = s;
-    }
-    if (k1 == 0) {
-      err_loc = 1e-14;
-      break;
-    }
-    double2 f1 = make_double2(0.0, 0.0), f2 = make_double2(0.0, 0.0);
-    for (int q = 0; q < mb; ++q) {
-      double2 x = cscale(d[q], zc);
-      double w = z[(mb - 1) * mb + q] * z[q];
-      f1 = cadd(f1, cscale(w, cmul(zc, dphi1(x))));
-      f2 = cadd(f2, cscale(w, cmul(cmul(zc, zc), dphi2(x))));
-    }
-    F[mb] = cscale(ctl->bet[mb], f1);
-    F[mb + 1] = cscale(ctl->bet[mb], f2);
-    double p1 = cabs_d(F[mb]) * beta, p2 = cabs_d(F[mb + 1]) * beta * avnorm;
-    if (p1 > 10.0 * p2) {
-      err_loc = p2;
-      xm = 1.0 / m;
-    } else if (p1 > p2) {
-      err_loc = p1 * p2 / (p1 - p2);
-      xm = 1.0 / m;
-    } else {
-      err_loc = p1;
-      xm = 1.0 / (m - 1);
-    }
-    if (err_loc <= delta * t_step * tol) break;
-    if (ireject == 10) {
-      ctl->err |= 1;
-      ctl->done = 1;
-      return;
-    }
-    t_step = gamma * t_step * pow(t_step * tol / err_loc, xm);
-    double sc = pow(10.0, floor(log10(t_step)) - 1.0);
-    t_step = ceil(t_step / sc) * sc;
-    ++ireject;
-  }
-  if (!isfinite(t_step) || !(t_step > 0.0) || !isfinite(err_loc)) {
-    ctl->err |= 8;
-    ctl->done = 1;
-    return;
-  }
-  const int mx = mb + (k1 > 1 ? k1 - 1 : 0);
-  for (int q = 0; q < 72; ++q) {
-    double2 c = (q < mx) ? cscale(beta, F[q]) : make_double2(0.0, 0.0);
-    ctl->coef[2 * q] = c.x;
-    ctl->coef[2 * q + 1] = c.y;
-  }
-  ctl->t_now += t_step;
-  if (k1 != 0) {
-    double tn = gamma * t_step * pow(t_step * tol / fmax(err_loc, 1e-300), xm);
-    double sc = pow(10.0, floor(log10(tn)) - 1.0);
-    ctl->t_new = ceil(tn / sc) * sc;
-    if (!isfinite(ctl->t_new) || !(ctl->t_new > 0.0)) ctl->t_new = t_step;
-  }
-  ctl->napps += mb + (k1 != 0 ? 1 : 0);
-  ctl->substeps += 1;
-  if (ctl->t_now >= ctl->t_out) ctl->done = 1;
-}
-
-// y = sum_q c_q V_q
-__global__ void k_combine(const KrylovCtl* ctl, const double2* __restrict__ V, long long ldv, double2* __restrict__ y,
-                          long long n, int nq) {
-  __shared__ double2 c[VQ];
-  for (int q = threadIdx.x; q < nq; q += blockDim.x) c[q] = make_double2(ctl->coef[2 * q], ctl->coef[2 * q + 1]);
-  __syncthreads();
-  for (long long i = (long long)blockIdx.x * VT + threadIdx.x; i < n; i += (long long)gridDim.x * VT) {
-    double2 s = make_double2(0.0, 0.0);
-    for (int q = 0; q < nq; ++q) s = cfma(c[q], V[(long long)q * ldv + i], s);
-    y[i] = s;
-  }
-}
-
-__global__ void k_init_ctl(KrylovCtl* ctl, int m, double tau, double cre, double cim, double tol) {
-  if (threadIdx.x != 0) return;
-  ctl->m = m;
-  ctl->t_out = fabs(tau);
-  ctl->sgn = tau >= 0.0 ? 1.0 : -1.0;
-  ctl->t_now = 0.0;
-  ctl->t_new = fabs(tau);
-  ctl->cf_re = cre;
-  ctl->cf_im = cim;
-  ctl->tol = tol;
-  ctl->done = (tau == 0.0) ? 1 : 0;
-  ctl->err = 0;
-  ctl->substeps = 0;
-  ctl->napps = 0;
-  ctl->mb = m;
-  ctl->k1 = 2;
-  for (int q = 0; q < 73; ++q) ctl->bet[q] = 0.0;
-  for (int q = 0; q < 72; ++q) ctl->alpha[q] = 0.0;
-}
-}  // namespace
-
-size_t lanczos_partial_bytes() { return (size_t)2 * VMAXB * VQ * sizeof(double2); }
-
-int vec_blocks(long long n) {
-  long long b = (n + VT * 4 - 1) / (VT * 4);
-  if (b < 1) b = 1;
-  if (b > VMAXB) b = VMAXB;
-  return (int)b;
-}
-
-void krylov_init_ctl(KrylovCtl* ctl, int m, double tau, double cre, double cim, double tol, cudaStream_t s) {
-  ++g_launches;
-  k_init_ctl<<<1, 32, 0, s>>>(ctl, m, tau, cre, cim, tol);
-}
-
-void krylov_begin(KrylovCtl* ctl, const double2* y, double2* V0, long long n, double2* part, cudaStream_t s) {
-  int nb = vec_blocks(n);
-  ++g_launches;
-  k_norm_partial<<<nb, VT, 0, s>>>(y, n, part);
-  ++g_launches;
-  k_begin<<<nb, VT, 0, s>>>(ctl, y, V0, n, part, nb);
-}
-
-void lanczos_orth(KrylovCtl* ctl, int j, double2* V, long long ldv, double2* p, long long n, double2* part,
-                  cudaStream_t s) {
-  int nb = vec_blocks(n);
-  double2* pa = part;
-  double2* pb = part + (size_t)VMAXB * VQ;
-  ++g_launches;
-  k_orth1<<<nb, VT, 0, s>>>(V + (long long)j * ldv, p, n, pa);
-  ++g_launches;
-  k_orth2<<<nb, VT, 0, s>>>(ctl, j, V, ldv, p, n, pa, nb, pb);
-  ++g_launches;
-  k_orth3<<<nb, VT, 0, s>>>(j, V, ldv, p, n, pb, nb, pa);
-  ++g_launches;
-  k_orth4<<<nb, VT, 0, s>>>(ctl, j, V, ldv, p, n, pa, nb);
-}
-
-void lanczos_avnorm(KrylovCtl* ctl, const double2* p, long long n, double2* part, cudaStream_t s) {
-  int nb = vec_blocks(n);
-  ++g_launches;
-  k_norm_partial<<<nb, VT, 0, s>>>(p, n, part);
-  ++g_launches;
-  k_avnorm<<<1, 32, 0, s>>>(ctl, part, nb);
-}
-
-void krylov_control(KrylovCtl* ctl, cudaStream_t s) {
-  ++g_launches;
-  k_control<<<1, 32, 0, s>>>(ctl);
-}
-
-void krylov_combine(KrylovCtl* ctl, const double2* V, long long ldv, double2* y, long long n, int nq,
-                    cudaStream_t s) {
-  int nb = vec_blocks(n);
-  ++g_launches;
-  k_combine<<<nb, VT, 0, s>>>(ctl, V, ldv, y, n, nq);
-}
-
-// =====================================================================================
-// Householder QR (single CTA)
-// =====================================================================================
-namespace {
-constexpr int QT = 1024;
-constexpr int QMAXN = 64;
 
 __device__ double block_sum_qr(double v, double* red) {
   v = warp_sum(v);
@@ -739,46 +278,6 @@ __device__ double block_sum_qr(double v, double* red) {
 // Trailing reflector application: for c in (c0, n): w_c = sum_{r >= r0} conj(v_r) M[r][c]
 // with v_{r0} = 1 and v_r = M[r][col] below; then M[r][c] -= v_r * (f * w_c).
 // conjf: use conj(tau) (factorisation) or tau (forming Q).
-__device__ void apply_reflector(double2* M, long long m, int n, int col, long long r0, int c0, double2 tau,
-                                bool conjt, double2 (*wacc)[QMAXN], double2* wsh) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int nc = n - c0;
-  if (nc <= 0) return;
-  // per-warp partial sums over a strided set of rows; lanes own columns
-  double2 acc[QMAXN / 32];
-#pragma unroll
-  for (int u = 0; u < QMAXN / 32; ++u) acc[u] = make_double2(0.0, 0.0);
-  for (long long r = r0 + w; r < m; r += nw) {
-    double2 v = (r == r0) ? make_double2(1.0, 0.0) : M[r * n + col];
-#pragma unroll
-    for (int u = 0; u < QMAXN / 32; ++u) {
-      int c = c0 + lane + 32 * u;
-      if (c < n) acc[u] = cadd(acc[u], cmulc(v, M[r * n + c]));
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < QMAXN / 32; ++u) {
-    int c = lane + 32 * u;
-    if (c < nc) wacc[w][c] = acc[u];
-  }
-  __syncthreads();
-  double2 t = conjt ? make_double2(tau.x, -tau.y) : tau;
-  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-    double2 s = make_double2(0.0, 0.0);
-    for (int k = 0; k < nw; ++k) s = cadd(s, wacc[k][c]);
-    wsh[c] = cmul(t, s);
-  }
-  __syncthreads();
-  const long long rows = m - r0;
-  for (long long e = threadIdx.x; e < rows * nc; e += blockDim.x) {
-    long long r = r0 + e / nc;
-    int c = c0 + (int)(e % nc);
-    double2 v = (r == r0) ? make_double2(1.0, 0.0) : M[r * n + col];
-    M[r * n + c] = csub(M[r * n + c], cmul(v, wsh[c - c0]));
-  }
-  __syncthreads();
-}
-
 __device__ double block_max_qr(double v, double* red) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -803,112 +302,15 @@ __device__ double dlapy3_d(double x, double y, double z) {
   double a = x / w, b = y / w, c = z / w;
   return w * sqrt(a * a + b * b + c * c);
 }
-
-__global__ void __launch_bounds__(QT) k_householder_qr(double2* M, long long m, int n, double2* R, int Rt,
-                                                       double2* tau) {
-  __shared__ double2 wacc[QT / 32][QMAXN];
-  __shared__ double2 wsh[QMAXN];
-  __shared__ double red[33];
-  __shared__ double2 s_tau, s_scal, s_beta;
-  __shared__ double s_xscale;
-  const double safmin = 2.2250738585072014e-308 / 1.1102230246251565e-16;  // 2^-969
-  for (int j = 0; j < n; ++j) {
-    // scaled norm of the sub-column: max first, then the sum of scaled squares
-    double amax = 0.0;
-    for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
-      double2 x = M[i * n + j];
-      amax = fmax(amax, fmax(fabs(x.x), fabs(x.y)));
-    }
-    amax = block_max_qr(amax, red);
-    double s = 0.0;
-    if (amax > 1e-290) {
-      const double inv = 1.0 / amax;
-      for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
-        double2 x = M[i * n + j];
-        double a = x.x * inv, b = x.y * inv;
-        s += a * a + b * b;
-      }
-    } else if (amax > 0.0) {
-      // 1/amax would overflow for denormal columns: divide instead
-      for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
-        double2 x = M[i * n + j];
-        double a = x.x / amax, b = x.y / amax;
-        s += a * a + b * b;
-      }
-    }
-    s = block_sum_qr(s, red);
-    if (threadIdx.x == 0) {
-      double2 alpha = M[(long long)j * n + j];
-      double xnorm = amax * sqrt(s);
-      double ar = alpha.x, ai = alpha.y;
-      s_xscale = 1.0;
-      if (xnorm == 0.0 && ai == 0.0) {
-        s_tau = make_double2(0.0, 0.0);
-        s_beta = alpha;
-        s_scal = make_double2(0.0, 0.0);
-      } else {
-        double b = -copysign(dlapy3_d(ar, ai, xnorm), ar >= 0.0 ? 1.0 : -1.0);
-        int knt = 0;
-        double xs = 1.0;
-        if (fabs(b) < safmin) {
-          // rescale tiny columns by the exact power of two 1/safmin (zlarfg), at most 20 times
-          const double rs = 1.0 / safmin;
-          do {
-            ++knt;
-            xs *= rs;
-            b *= rs;
-            ar *= rs;
-            ai *= rs;
-            xnorm *= rs;
-          } while (fabs(b) < safmin && knt < 20);
-          b = -copysign(dlapy3_d(ar, ai, xnorm), ar >= 0.0 ? 1.0 : -1.0);
-        }
-        s_tau = make_double2((b - ar) / b, -ai / b);
-        s_scal = cdiv_d(make_double2(1.0, 0.0), make_double2(ar - b, ai));
-        s_xscale = xs;
-        for (int q = 0; q < knt; ++q) b *= safmin;
-        s_beta = make_double2(b, 0.0);
-      }
-      tau[j] = s_tau;
-    }
-    __syncthreads();
-    const double2 tj = s_tau;
-    if (tj.x != 0.0 || tj.y != 0.0) {
-      const double xs = s_xscale;
-      for (long long i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
-        double2 x = M[i * n + j];
-        x.x *= xs;
-        x.y *= xs;
-        M[i * n + j] = cmul(x, s_scal);
-      }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) M[(long long)j * n + j] = s_beta;
-    __syncthreads();
-    if (tj.x != 0.0 || tj.y != 0.0) apply_reflector(M, m, n, j, j, j + 1, tj, true, wacc, wsh);
+// a / b by Smith's algorithm (CACM 5(8), 1962): no squared magnitudes, so no spurious
+// underflow or overflow for very small or very large b.
+__device__ double2 cdiv_d(double2 a, double2 b) {
+  if (fabs(b.x) >= fabs(b.y)) {
+    double r = b.y / b.x, den = b.x + b.y * r;
+    return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
   }
-  // R
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-    int i = e / n, k = e % n;
-    double2 v = (k >= i) ? M[(long long)i * n + k] : make_double2(0.0, 0.0);
-    if (Rt) R[(long long)k * n + i] = v;
-    else R[(long long)i * n + k] = v;
-  }
-  __syncthreads();
-  // Q = H_0 ... H_{n-1} [I; 0]  (zung2r ordering)
-  for (int i = n - 1; i >= 0; --i) {
-    const double2 ti = tau[i];
-    if (i < n - 1) {
-      if (threadIdx.x == 0) M[(long long)i * n + i] = make_double2(1.0, 0.0);
-      __syncthreads();
-      if (ti.x != 0.0 || ti.y != 0.0) apply_reflector(M, m, n, i, i, i + 1, ti, false, wacc, wsh);
-    }
-    for (long long r = i + 1 + threadIdx.x; r < m; r += blockDim.x)
-      M[r * n + i] = cmul(make_double2(-ti.x, -ti.y), M[r * n + i]);
-    if (threadIdx.x == 0) M[(long long)i * n + i] = make_double2(1.0 - ti.x, -ti.y);
-    for (int r = threadIdx.x; r < i; r += blockDim.x) M[(long long)r * n + i] = make_double2(0.0, 0.0);
-    __syncthreads();
-  }
+  double r = b.x / b.y, den = b.x * r + b.y;
+  return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
 }
 
 __global__ void k_permute_mode_last(const double2* __restrict__ A, double2* __restrict__ M, long long pre, int dm,
@@ -1300,10 +702,6 @@ cudaError_t householder_qr_coop(double2* M, long long m, int n, double2* R, int 
   return cudaLaunchCooperativeKernel((const void*)k_qr_coop, dim3(grid), dim3(CQT), args, 0, s);
 }
 
-void householder_qr(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, cudaStream_t s) {
-  ++g_launches;
-  k_householder_qr<<<1, QT, 0, s>>>(M, m, n, R, Rt, tau_ws);
-}
 void permute_mode_last(const double2* A, double2* M, long long pre, int dm, long long post, cudaStream_t s) {
   ++g_launches;
   k_permute_mode_last<<<grid_for(pre * dm * post), 256, 0, s>>>(A, M, pre, dm, post);

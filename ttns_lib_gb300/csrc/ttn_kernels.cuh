@@ -59,27 +59,13 @@ struct KrylovCtl {
   long long napps;       // H applications (including the error-estimate one)
 };
 
-// Reduction partial buffers are laid out [nblocks][nq] complex.
-int vec_blocks(long long n);
-void krylov_begin(KrylovCtl* ctl_dev, const double2* y, double2* V0, long long n, double2* part,
-                  cudaStream_t s);
-// after p = H V_j: alpha, CGS pass, beta, V_{j+1}
-void lanczos_orth(KrylovCtl* ctl, int j, double2* V, long long ldv, double2* p, long long n, double2* part,
-                  cudaStream_t s);
-void lanczos_avnorm(KrylovCtl* ctl, const double2* p, long long n, double2* part, cudaStream_t s);
-void krylov_control(KrylovCtl* ctl, cudaStream_t s);
-void krylov_combine(KrylovCtl* ctl, const double2* V, long long ldv, double2* y, long long n, int nq,
-                    cudaStream_t s);
 constexpr int kQrMaxCols = 64;   // widest matrix the device QR accepts
 constexpr int kKrylovMax = 64;   // largest Krylov dimension
-size_t lanczos_partial_bytes();
-void krylov_init_ctl(KrylovCtl* ctl, int m, double tau, double cre, double cim, double tol, cudaStream_t s);
 
 // ---- Householder QR --------------------------------------------------------------
-// In-place Householder QR of an m x n row-major matrix (m >= n): M <- Q, R (n x n) out.
-// Rt != 0 stores R^T instead of R.
-void householder_qr(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, cudaStream_t s);
-// Cooperative multi-CTA version (grid <= co-resident CTAs); scratch of
+// In-place Householder QR of an m x n row-major matrix (m >= n): M <- Q, R (n x n) out;
+// Rt != 0 stores R^T instead of R.  Column-by-column cooperative multi-CTA version
+// (grid <= co-resident CTAs); scratch of
 // coop_qr_scratch_bytes(grid) bytes, barrier state zero-initialised once, err is a
 // device status word (kErrBarrierTimeout on a barrier that gave up).
 struct GridBarrier;

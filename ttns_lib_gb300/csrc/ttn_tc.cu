@@ -9,7 +9,6 @@
 #include "ttn_tc_core.cuh"
 #include "ttn_kernels.cuh"
 
-#include <stdexcept>
 
 namespace ttn {
 
@@ -92,25 +91,5 @@ cudaError_t tc_gemm_test(const double* A, const double* B, double* D, int K, int
   k_tc_gemm_test<<<1, 256, kTcSmem, s>>>(A, B, D, K, N, err);
   return cudaGetLastError();
 }
-
-// ---- engine used by the integrator (contractions are not routed here yet)
-struct TcEngine {
-  int device;
-};
-
-TcEngine* tc_create(int, long long, cudaStream_t) {
-  throw std::runtime_error("mixed-precision contractions are not available in this build");
-}
-void tc_destroy(TcEngine* e) { delete e; }
-bool tc_mode_apply(TcEngine*, const double2*, int, const double2*, double2*, long long, long long, double2, bool,
-                   cudaStream_t) { return false; }
-bool tc_mf_apply(TcEngine*, const double2*, const double2*, int, long long, double2*, double2, bool, cudaStream_t) {
-  return false;
-}
-bool tc_adj_mul(TcEngine*, const double2*, const double2*, long long, int, double2*, double2, bool, cudaStream_t) {
-  return false;
-}
-bool tc_mode_contract(TcEngine*, const double2*, const double2*, long long, int, long long, double2*, double2, bool,
-                      cudaStream_t) { return false; }
 
 }  // namespace ttn

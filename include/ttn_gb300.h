@@ -200,8 +200,9 @@ int ttn_debug_qr(int m, int n, double* a, double* r, int device);
 /* No counterpart in the reference: it is the one entry point that allocates no device
  * memory, for callers that cannot allocate where they factorise (all their device memory
  * comes from their own pool or arena, or a cudaMalloc/cudaFree device synchronisation
- * is not affordable).  Householder QR (LAPACK zgeqrf/zungqr conventions, the same
- * cooperative kernel as the sweep's gauge moves) of an m x n row-major complex matrix
+ * is not affordable).  Householder QR (LAPACK zgeqrf/zungqr conventions, the
+ * column-by-column cooperative kernel; the sweep's gauge moves use its panel-blocked
+ * variant, equal to rounding) of an m x n row-major complex matrix
  * already on `device`: a <- Q (m x n), r <- R (n x n, upper triangular); a and r are
  * device pointers to interleaved complex doubles, 16-byte aligned; stream is a
  * cudaStream_t (NULL: the legacy default stream).  The workspace (about 0.52 MB) is one

@@ -6,6 +6,9 @@ Runs that start from the rank-1 product state are compared against the oracle's 
 spread under rounding-level perturbations (see test_product_state_within_envelope)."""
 import copy
 
+import json
+import os
+
 import numpy as np
 import pytest
 import scipy.linalg as sla
@@ -212,3 +215,17 @@ def test_product_state_within_envelope():
     diff = np.abs(np.array(sd) - so)
     assert diff[0] < 1e-7
     assert np.all(diff <= 20 * np.maximum(env, 1e-8)), (diff, env)
+
+def test_device_matches_golden_trajectory():
+    """The committed dense-expm trajectory (tests/golden/make_golden.py) on the device:
+    full-rank tree, so the sweep is exact; 40 steps including the first-step sub-steps."""
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "spin_boson_fullrank_N4.json")))
+    m = sb.build(**g["params"])
+    A = api.httensor(m.topology)
+    A.set(sb.initial_state_numpy(m.topology, seed=g["seed"], psi0=np.array([1.0, 0.0])))
+    dev = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=12, krylov_tolerance=1e-12)
+    dev.dt = g["dt"]
+    for k in range(g["steps"]):
+        dev(A, m.sop, -1j)
+        assert abs(dev.mel()(sb.SZ, 0, A).real - g["sz"][k]) < 1e-11, k
+        assert abs(dev.mel()(sb.SX, 0, A).real - g["sx"][k]) < 1e-11, k

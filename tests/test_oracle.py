@@ -1,5 +1,8 @@
 """The oracle pinned by known answers: dense exp(-iHt) on full-rank trees, the
 uncoupled spin, conservation laws and the Householder conventions."""
+import json
+import os
+
 import numpy as np
 import pytest
 import scipy.linalg as sla
@@ -87,3 +90,16 @@ def test_householder_tiny_columns_stay_finite():
     assert np.isfinite(q).all() and np.isfinite(r).all()
     assert np.allclose(q.conj().T @ q, np.eye(6), atol=1e-13)
     assert np.allclose(q @ r, a, rtol=0, atol=1e-13 * np.abs(a).max())
+
+def test_oracle_matches_golden_trajectory():
+    """The committed dense-expm trajectory (tests/golden/make_golden.py): full-rank tree,
+    so the sweep is exact; 40 steps including the first-step sub-steps."""
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "spin_boson_fullrank_N4.json")))
+    m = sb.build(**g["params"])
+    orc = Oracle(m.topology, m.sop, krylov_dim=12, krylov_tol=1e-12)
+    orc.set_state(sb.initial_state_numpy(m.topology, seed=g["seed"], psi0=np.array([1.0, 0.0])))
+    for k in range(g["steps"]):
+        orc.step(g["dt"])
+        assert abs(orc.expect(0, sb.SZ).real - g["sz"][k]) < 1e-11, k
+        assert abs(orc.expect(0, sb.SX).real - g["sx"][k]) < 1e-11, k
+        assert abs(orc.norm2() - g["norm"][k]) < 1e-11, k

@@ -456,7 +456,10 @@ struct Integrator {
 
   void setup() {
     CK(cudaSetDevice(device));
-    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    // A blocking stream: its work waits for work issued earlier to the legacy default
+    // stream, where the state uploads and downloads of ttn_state (cudaMemcpy) run; with a
+    // non-blocking stream a step could start before an upload has landed.
+    CK(cudaStreamCreate(&stream));
     compile_plan(T, H, G, gof);
     // leaf operators
     size_t ob = 0;
@@ -484,7 +487,7 @@ struct Integrator {
       for (auto& g : G[i]) eb += (g.id_spf ? 0 : align256(rr)) + (g.id_mf ? 0 : align256(rr));
     }
     env_buf.alloc(eb);
-    CK(cudaMemset(env_buf.p, 0, env_buf.bytes));
+    CK(cudaMemsetAsync(env_buf.p, 0, env_buf.bytes, stream));
     {
       char* base = env_buf.as<char>();
       size_t o = 0;
@@ -576,7 +579,7 @@ struct Integrator {
       qr_max_grid = std::max(1, std::min(qr_blocked_max_grid(), num_sms));
       size_t qb = align256(sizeof(GridBarrier)) + align256(qr_blocked_scratch_bytes(qr_max_grid));
       coop_buf.alloc(qb);
-      CK(cudaMemset(coop_buf.p, 0, coop_buf.bytes));
+      CK(cudaMemsetAsync(coop_buf.p, 0, coop_buf.bytes, stream));
       bar = coop_buf.as<GridBarrier>();
       qr_scratch = (double*)(coop_buf.as<char>() + align256(sizeof(GridBarrier)));
       mixed = (cfg.precision == TTN_PREC_MIXED);
@@ -594,7 +597,7 @@ struct Integrator {
       expm_part_buf.alloc(expm_partial_bytes(expm_max_grid) + 512);
       nh_dev = (long long*)(expm_part_buf.as<char>() + expm_partial_bytes(expm_max_grid));
       flops_dev = (double*)(expm_part_buf.as<char>() + expm_partial_bytes(expm_max_grid) + 256);
-      CK(cudaMemset(expm_part_buf.p, 0, expm_part_buf.bytes));
+      CK(cudaMemsetAsync(expm_part_buf.p, 0, expm_part_buf.bytes, stream));
       compile_programs();
       if (mixed) tc_img_buf.alloc((size_t)std::max(1, max_tc_images) * kTcImageBytes);
     }
@@ -1034,7 +1037,8 @@ struct Integrator {
       all.insert(all.end(), k.begin(), k.end());
     }
     prog_buf.alloc(all.size() * sizeof(MvOp) + 16);
-    CK(cudaMemcpy(prog_buf.p, all.data(), all.size() * sizeof(MvOp), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(prog_buf.p, all.data(), all.size() * sizeof(MvOp), cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));  // `all` is pageable and goes out of scope
   }
   // CTAs of a Krylov launch: at most one per 64 vector elements and one per
   // expm_cta_flops of matvec work.  Small problems run on few CTAs (one CTA synchronises

@@ -219,6 +219,11 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
+    if args.config == "c4":
+        print(json.dumps({"impl": "reference", "unavailable": "the batched form has no reference implementation "
+                          "(the reference steps one instance per integrator); its baseline is the one-after-another "
+                          "leg of the same bench line"}), flush=True)
+        return 0
     threads = os.cpu_count() or 1
     vals = []
     desc = ""

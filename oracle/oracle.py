@@ -17,8 +17,8 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    src = os.path.join(_HERE, "ttn_oracle.cpp")
-    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("ttn_oracle.cpp", "ttn_adjoint.hpp")]
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < max(os.path.getmtime(s) for s in srcs):
         subprocess.check_call(["make", "-s", "-C", _HERE, "liboracle.so"])
     return _LIB
 
@@ -62,6 +62,8 @@ def lib():
         L.orc_node_times.argtypes = [P, dp]
         L.orc_reset_node_times.argtypes = [P]
         L.orc_tql2.argtypes = [C.c_int, dp, dp, dp]
+        L.orc_adjoint.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_int, dp, C.c_int, dp, C.c_int, C.c_int,
+                                  dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -93,6 +95,9 @@ class Oracle:
             raise ValueError(err.value.decode())
         L.orc_set_threads(self.h, threads)
         self.offsets = topo.offsets()
+        self._nterms = sop.nterms
+        self._opdims = [int(sop.mode_dims[m]) for m in op_mode]
+        self._opsize = sum(d * d for d in self._opdims)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -174,6 +179,28 @@ class Oracle:
         self._check(lib().orc_expm_node(self.h, node, tau, coeff.real, coeff.imag, _dp(x.view(np.float64)),
                                         C.byref(n)))
         return x.reshape(self.topo.node_shape(node)), int(n.value)
+
+    def adjoint(self, dt: float, nsteps: int, weights, mode: int, op, checkpoint_every: int = 20,
+                coeff: complex = -1j, skip_prepare: bool = False, state_cotangent: bool = False):
+        """J = sum_k weights[k] Re <op on mode>(end of step k) over nsteps steps from the
+        current state, and its gradients by the adjoint sweep: (J, dJ/dc_r per term,
+        cotangent of every operator matrix in binding order[, cotangent of the state])."""
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        assert w.size == nsteps
+        o = np.ascontiguousarray(op, dtype=np.complex128)
+        J = np.zeros(1)
+        gc = np.zeros(self._nterms)
+        gops = np.zeros(self._opsize, dtype=np.complex128)
+        gs = np.zeros(int(self.offsets[-1]), dtype=np.complex128) if state_cotangent else None
+        self._check(lib().orc_adjoint(self.h, dt, coeff.real, coeff.imag, nsteps, _dp(w), mode, _dp(o.view(np.float64)),
+                                      checkpoint_every, int(skip_prepare), _dp(J), _dp(gc),
+                                      _dp(gops.view(np.float64)), _dp(gs.view(np.float64)) if gs is not None else None))
+        ops, off = [], 0
+        for d in self._opdims:
+            ops.append(gops[off:off + d * d].reshape(d, d))
+            off += d * d
+        out = (float(J[0]), gc, ops)
+        return out + (gs,) if state_cotangent else out
 
     def groups(self, node: int):
         out = []

@@ -23,6 +23,8 @@
 //                          include/ttns_lib/tdvp_core/operator_compression.hpp:373-489
 //   * first-step schedule  include/ttns_lib/integrators/projector_splitting_integrator.hpp:136-169
 //   * <O> on one mode .... include/ttns_lib/observables/matrix_element.hpp:264-314
+//   * adjoint sweep ...... ttn_adjoint.hpp (no counterpart in the reference: the reverse
+//                          of the sweep above, checked against finite differences)
 //
 // Two definitions are ours because the reference's versions live in the absent
 // submodules:
@@ -42,6 +44,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -59,6 +62,8 @@ struct Error : std::runtime_error {
   Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
 enum { OK = 0, EINVAL_ = 1, ECAP = 2, ENUM = 3 };
+// operations of a sweep, as reported to Engine::on_op
+enum { OP_AFP = 1, OP_R2L, OP_MF, OP_NODE, OP_L2R, OP_SPF, OP_BOND, OP_ATP };
 
 #define ORC_REQUIRE(cond, msg) \
   do { if (!(cond)) throw ::orc::Error(::orc::EINVAL_, msg); } while (0)
@@ -232,6 +237,7 @@ struct SOP {
   std::vector<int> mode_dim;
   std::vector<std::vector<std::vector<cd>>> ops;  // ops[mode][k] dense d x d
   std::vector<std::vector<int>> opidx;            // opidx[mode][r] = k or -1
+  std::vector<std::pair<int, int>> op_order;      // (mode, k) of each operator in creation order
 };
 
 // ---------------------------------------------------------------- compiled operator plan
@@ -243,8 +249,10 @@ struct SOP {
 // singletons apply c_r as a scalar.  Each c_r is applied exactly once.
 enum { G_S = 0, G_M = 1, G_1 = 2 };
 struct Item { int slot; int grp; };
-struct SpfTuple { cd a; std::vector<Item> items; };
-struct MfKey { cd b; int pg; std::vector<Item> sib; };
+// a_mem / b_mem: the terms whose coefficients were summed into a / b (empty when the
+// scalar is the constant 1); the adjoint sweep maps scalar cotangents back through them.
+struct SpfTuple { cd a; std::vector<Item> items; std::vector<int> a_mem; };
+struct MfKey { cd b; int pg; std::vector<Item> sib; std::vector<int> b_mem; };
 struct Group {
   int type = G_1;
   std::vector<int> members;
@@ -342,7 +350,7 @@ static void compile_plan(const Tree& T, const SOP& H, Plan& P) {
                 throw Error(EINVAL_, "operator compression invariant violated (spf carrying group)");
             }
           }
-        if (g.type == G_M && !carrying) { cd a = 0.0; for (int r : mem) a += H.coeff[r]; t.a = a; }
+        if (g.type == G_M && !carrying) { cd a = 0.0; for (int r : mem) a += H.coeff[r]; t.a = a; t.a_mem = mem; }
         else t.a = 1.0;
         g.spf.push_back(t);
       }
@@ -388,7 +396,7 @@ static void compile_plan(const Tree& T, const SOP& H, Plan& P) {
           throw Error(EINVAL_, "operator compression invariant violated (mf carrying component)");
         if (carrying && *carrier != mem)
           throw Error(EINVAL_, "operator compression invariant violated (mf carrier members)");
-        if (g.type == G_S && !carrying) { cd b = 0.0; for (int r : mem) b += H.coeff[r]; k.b = b; }
+        if (g.type == G_S && !carrying) { cd b = 0.0; for (int r : mem) b += H.coeff[r]; k.b = b; k.b_mem = mem; }
         else k.b = 1.0;
         g.mf.push_back(k);
       }
@@ -575,6 +583,9 @@ struct Engine {
   std::vector<cd> w1, w2, w3, w4;                       // work buffers (max node size)
   std::vector<std::vector<cd>> V;                       // Krylov basis
   std::vector<double> node_time;                        // seconds spent per node in sweeps
+  // Called before every operation of a sweep (kind OP_*, node, auxiliary index) while
+  // set; the adjoint sweep uses it to record the operations' inputs.
+  std::function<void(int, int, int)> on_op;
   std::chrono::steady_clock::time_point tmark;
   void tick() { tmark = std::chrono::steady_clock::now(); }
   void tock(int id) {
@@ -657,6 +668,7 @@ struct Engine {
 
   // ---- bottom-up environment (single_particle_operator.hpp:26-103)
   void update_spf(int nd) {
+    if (on_op) on_op(OP_SPF, nd, 0);
     const size_t sz = T.size(nd);
     const int r = T.hrank[nd];
     for (size_t g = 0; g < P.groups[nd].size(); ++g) {
@@ -674,6 +686,7 @@ struct Engine {
   // ---- top-down environment for child nd (mean_field_operator.hpp:37-184)
   void update_mf(int nd) {
     if (nd == 0) return;
+    if (on_op) on_op(OP_MF, nd, 0);
     const int p = T.parent[nd], mu = T.slot[nd];
     size_t na, nb; int d;
     r3(p, mu, na, d, nb);
@@ -848,6 +861,7 @@ struct Engine {
   // ---- gauge moves
   // leaf_to_root_decomposition.hpp:57-101: A = Q R, A <- Q, rmat = R
   void l2r(int nd) {
+    if (on_op) on_op(OP_L2R, nd, 0);
     const size_t m = T.dimen[nd];
     const int r = T.hrank[nd];
     std::vector<cd> tau;
@@ -855,6 +869,7 @@ struct Engine {
   }
   // leaf_to_root_decomposition.hpp:105-138: parent mode <- R . parent
   void apply_to_parent(int nd) {
+    if (on_op) on_op(OP_ATP, nd, 0);
     const int p = T.parent[nd], mu = T.slot[nd];
     size_t na, nb; int d;
     r3(p, mu, na, d, nb);
@@ -864,6 +879,7 @@ struct Engine {
   // root_to_leaf_decomposition.hpp:113-183: permute mode mu to the fastest index, QR,
   // store R^T so that the child applies A_c <- A_c R^T.
   void r2l(int nd, int mu) {
+    if (on_op) on_op(OP_R2L, nd, mu);
     size_t pre = 1, post = (size_t)T.hrank[nd];
     for (int i = 0; i < mu; ++i) pre *= T.dims[nd][i];
     const int dm = T.dims[nd][mu];
@@ -885,6 +901,7 @@ struct Engine {
   }
   // root_to_leaf_decomposition.hpp:208-233: A <- A . R_parent
   void apply_from_parent(int nd) {
+    if (on_op) on_op(OP_AFP, nd, 0);
     const int p = T.parent[nd], r = T.hrank[nd];
     const size_t m = T.dimen[nd];
     matmul(A[nd].data(), rmat[p].data(), (int)m, r, r, w4.data());
@@ -893,9 +910,13 @@ struct Engine {
 
   // ---- node and bond evolution (projector_splitting_engine.hpp:117-165)
   void evolve_node(int nd) {
+    if (on_op) on_op(OP_NODE, nd, 0);
     nh += expm([&](const cd* v, cd* o) { heff(nd, v, o); }, A[nd].data(), T.size(nd), dt / 2.0, coeff);
   }
-  void evolve_bond(int nd, std::vector<cd>& R) {
+  // R: the bond matrix held in rmat[owner] (the node's own after l2r, its parent's after r2l)
+  void evolve_bond(int nd, int owner) {
+    if (on_op) on_op(OP_BOND, nd, owner);
+    std::vector<cd>& R = rmat[owner];
     const size_t rr = (size_t)T.hrank[nd] * T.hrank[nd];
     std::vector<cd> tmp(R.begin(), R.begin() + rr);
     expm([&](const cd* v, cd* o) { kbond(nd, v, o); }, tmp.data(), rr, -dt / 2.0, coeff);
@@ -937,7 +958,7 @@ struct Engine {
         if (id != 0) {
           l2r(id); chk("l2r", id);
           update_spf(id); chk("update_spf", id);
-          if (evolve) { evolve_bond(id, rmat[id]); chk("evolve_bond", id); }
+          if (evolve) { evolve_bond(id, id); chk("evolve_bond", id); }
           apply_to_parent(id); chk("apply_to_parent", id);
         }
       }
@@ -954,7 +975,7 @@ struct Engine {
         int mode = T.nmodes[id] - (t + 1);
         if (t == 0) {
           if (id != 0) {
-            if (evolve) evolve_bond(id, rmat[T.parent[id]]);
+            if (evolve) evolve_bond(id, T.parent[id]);
             apply_from_parent(id);
           }
           if (evolve) evolve_node(id);
@@ -1103,6 +1124,8 @@ struct Engine {
   }
 };
 
+#include "ttn_adjoint.hpp"
+
 }  // namespace orc
 
 // ---------------------------------------------------------------- C API (ctypes)
@@ -1147,6 +1170,7 @@ void* orc_create(int nnodes, const int* parent, const int* hrank, const int* lea
       off += M.size();
       int idx = (int)H.ops[m].size();
       H.ops[m].push_back(M);
+      H.op_order.push_back({m, idx});
       for (int q = bind_ptr[k]; q < bind_ptr[k + 1]; ++q) {
         int r = bind_r[q];
         ORC_REQUIRE(r >= 0 && r < nterms, "bound term index out of range");
@@ -1299,6 +1323,36 @@ int orc_get_env(void* p, int node, int g, int which, double* out) {
   ORC_TRY(h, {
     const auto& M = which == 0 ? h->E.spf[node][g] : h->E.mf[node][g];
     for (size_t i = 0; i < M.size(); ++i) { out[2 * i] = M[i].real(); out[2 * i + 1] = M[i].imag(); }
+  })
+}
+// Adjoint sweep (ttn_adjoint.hpp): J = sum_k w[k] Re <O_mode>(end of step k) over nsteps
+// steps of dt from the current state (prepared first unless skip_prepare), checkpoints
+// every ckpt steps.  Out: J; gcoeff[nterms] = dJ/dc_r; gops = cotangent of every operator
+// (creation order, interleaved d x d); gstate (optional) = cotangent of the state after
+// preparation.  Leaves the oracle at the final state.
+int orc_adjoint(void* p, double dt, double cre, double cim, int nsteps, const double* w, int mode, const double* op,
+                int ckpt, int skip_prepare, double* J, double* gcoeff, double* gops, double* gstate) {
+  OrcHandle* h = (OrcHandle*)p;
+  ORC_TRY(h, {
+    orc::Engine& E = h->E;
+    ORC_REQUIRE(mode >= 0 && mode < E.H.nmodes, "mode out of range");
+    const int d = E.H.mode_dim[mode];
+    std::vector<cd> O((size_t)d * d);
+    for (size_t i = 0; i < O.size(); ++i) O[i] = cd(op[2 * i], op[2 * i + 1]);
+    orc::Adjoint adj(E);
+    *J = adj.run(dt, cd(cre, cim), nsteps, w, mode, O.data(), ckpt, skip_prepare != 0);
+    for (int r = 0; r < E.H.nterms; ++r) gcoeff[r] = adj.gc[r];
+    size_t off = 0;
+    for (auto& mk : E.H.op_order) {
+      const auto& G = adj.gop[mk.first][mk.second];
+      for (size_t i = 0; i < G.size(); ++i) { gops[2 * (off + i)] = G[i].real(); gops[2 * (off + i) + 1] = G[i].imag(); }
+      off += G.size();
+    }
+    if (gstate) {
+      off = 0;
+      for (int i = 0; i < E.T.n; ++i)
+        for (auto& z : adj.Ab[i]) { gstate[2 * off] = z.real(); gstate[2 * off + 1] = z.imag(); ++off; }
+    }
   })
 }
 // Householder QR of an m x n row-major complex matrix (in/out: Q), R out (n x n).

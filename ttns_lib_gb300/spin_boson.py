@@ -70,6 +70,17 @@ def build(N: int, alpha: float, wc: float, d: int, chi: int, eps: float = 0.0, d
     w, c = ohmic_modes(N, alpha, wc)
     if beta is not None:
         w, c = thermofield(w, c, beta)
+    desc = f"spin-boson N={N}{' (thermofield x2)' if beta is not None else ''} alpha={alpha} wc={wc} d={d} chi={chi}"
+    return build_from_modes(w, c, d, chi, eps, delta, desc)
+
+
+def build_from_modes(w, c, d: int, chi: int, eps: float = 0.0, delta: float = 1.0,
+                     description: str = "") -> SpinBosonModel:
+    """The spin-boson operator and tree for explicit bath frequencies ``w`` and couplings
+    ``c`` (one leaf per entry).  Operator binding order: 0 the system operator
+    (eps/2) sz + (Delta/2) sx, 1 sz, then per bath mode i: 2+2i w_i n, 3+2i c_i (b + b^dag)."""
+    w = np.asarray(w, dtype=np.float64)
+    c = np.asarray(c, dtype=np.float64)
     M = len(w)
     topo = spin_bath_topology(2, [d] * M, chi)
     mode_dims = [2] + [d] * M
@@ -80,8 +91,25 @@ def build(N: int, alpha: float, wc: float, d: int, chi: int, eps: float = 0.0, d
     for i in range(M):
         H.bind_diag(w[i] * n, [1 + 2 * i], i + 1)
         H.bind_dense(c[i] * x, [2 + 2 * i], i + 1)
-    desc = f"spin-boson N={N}{' (thermofield x2)' if beta is not None else ''} alpha={alpha} wc={wc} d={d} chi={chi}"
+    desc = description or f"spin-boson with {M} bath modes d={d} chi={chi}"
     return SpinBosonModel(topo, H, w, c, eps, delta, d, chi, desc)
+
+
+def parameter_gradient(model: SpinBosonModel, op_cotangents) -> dict:
+    """dJ/d(eps, Delta, c_k, w_k) from the cotangents of the operator matrices (binding
+    order of ``build_from_modes``) returned by an adjoint sweep: for an operator
+    O = p B, dJ/dp = Re sum conj(O_bar) * B."""
+    G = op_cotangents
+    d = model.local_dim
+    n, x = boson_ops(d)
+    M = len(model.omega)
+
+    def proj(Gk, B):
+        return float(np.real(np.sum(np.conj(Gk) * B)))
+
+    return dict(eps=proj(G[0], 0.5 * SZ), delta=proj(G[0], 0.5 * SX),
+                coupling=np.array([proj(G[3 + 2 * i], x) for i in range(M)]),
+                omega=np.array([proj(G[2 + 2 * i], np.diag(n)) for i in range(M)]))
 
 
 # The five workloads of the benchmark suite (synthetic, formula-generated).

@@ -149,6 +149,26 @@ int ttn_expect_leaf(ttn_integrator* it, ttn_state* psi, int mode, const double* 
                     double* im);
 int ttn_norm2(ttn_integrator* it, ttn_state* psi, double* out);
 
+/* ---- adjoint sweep ----------------------------------------------------------------- */
+/* Gradient of J = sum_k weights[k] Re <psi(t_k)| O_mode |psi(t_k)>, t_k the end of step k,
+ * over nsteps integrator steps of dt from psi (the first step sub-stepped like
+ * ttn_integrator_step; psi prepared first unless skip_prepare).  No counterpart in the
+ * reference: it differentiates the sweep of ttn_integrator_step
+ * (include/ttns_lib/integrators/projector_splitting_integrator.hpp:136-169) by the
+ * reverse of every operation, with the state checkpointed every checkpoint_every steps
+ * and the segments recomputed.  op: dense d x d operator on `mode` (interleaved complex).
+ * Out: *J; grad_coeff[nterms] = dJ/dc_r for real perturbations of the term coefficients;
+ * grad_ops = cotangent of every operator matrix in binding order (d x d interleaved
+ * complex each; for an operator p B, dJ/dp = Re sum conj(grad) * B); grad_state (optional)
+ * = cotangent of the state psi is prepared into, node by node as ttn_state_download.
+ * Requires an FP64 integrator at step 0 and gauge factors of full rank (a generic state,
+ * not a product state); psi is left at the final state and the integrator at step nsteps.
+ * TTN_EINVAL on bad arguments, TTN_ENUMERIC on a singular gauge factor or a failed
+ * exponential. */
+int ttn_adjoint_grad(ttn_integrator* it, ttn_state* psi, double dt, double coeff_re, double coeff_im, int nsteps,
+                     const double* weights, int mode, const double* op, int checkpoint_every, int skip_prepare,
+                     double* J, double* grad_coeff, double* grad_ops, double* grad_state);
+
 /* ---- kernel-level entry points (parity checks and benchmarks) -------------------- */
 /* recompute every environment for the current node tensors, without gauge moves */
 int ttn_debug_refresh_env(ttn_integrator* it, ttn_state* psi);

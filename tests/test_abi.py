@@ -89,3 +89,12 @@ def test_batch_step_validates_on_host():
     with pytest.raises(ValueError):
         api.batch_step([object()], [], -1j)
 
+
+
+def test_adjoint_grad_validates_on_host():
+    L = api.lib()
+    J = C.c_double()
+    z = np.zeros(4)
+    dp = z.ctypes.data_as(C.POINTER(C.c_double))
+    assert L.ttn_adjoint_grad(None, None, 0.05, 0.0, -1.0, 1, dp, 0, dp, 1, 0, C.byref(J), dp, dp, None) == api.TTN_EINVAL
+    assert b"null argument" in L.ttn_last_error()

@@ -1,0 +1,74 @@
+"""The adjoint sweep on the device (ttn_adjoint_grad) against the oracle's adjoint sweep
+on the same inputs: the objective J = sum_t w_t Re <O>(t), dJ/dc_r for every term
+coefficient, the cotangent of every operator matrix and of the state.  The oracle's
+adjoint is itself checked against central finite differences
+(tests/test_adjoint_oracle.py).  Both differentiate the same discrete sweep; they differ
+by rounding, by the Krylov step control of the two exponentials (agreeing to ~1e-11 in
+the trajectories) and by converged quadratures, so the gradients agree to 1e-8 of the
+largest component."""
+import numpy as np
+import pytest
+
+from helpers import generic_state, rand_herm, random_sop, random_tree
+from oracle.oracle import Oracle
+from ttns_lib_gb300 import api
+from ttns_lib_gb300 import spin_boson as sb
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-8
+
+
+def _compare(topo, H, st, dt, wt, mode, O, ckpt):
+    orc = Oracle(topo, H, krylov_dim=10, krylov_tol=1e-13)
+    orc.set_state(st)
+    Jo, gco, gopo, gso = orc.adjoint(dt, len(wt), wt, mode, O, checkpoint_every=ckpt, state_cotangent=True)
+    A = api.httensor(topo, device=0)
+    A.set(st)
+    integ = api.fixed_step_projector_splitting_integrator(A, H, krylov_dim=10, krylov_tolerance=1e-13)
+    Jd, gcd, gopd, gsd = integ.adjoint(A, dt, len(wt), wt, mode, O, checkpoint_every=ckpt, state_cotangent=True)
+    assert abs(Jd - Jo) <= 1e-10 * max(1.0, abs(Jo))
+    scale = max(np.max(np.abs(gco)), max(np.max(np.abs(g)) for g in gopo))
+    assert np.max(np.abs(gcd - gco)) <= TOL * scale
+    for a, b in zip(gopd, gopo):
+        assert np.max(np.abs(a - b)) <= TOL * scale
+    gso_flat = np.asarray(gso)
+    gsd_flat = np.concatenate([g.ravel() for g in gsd])
+    assert np.max(np.abs(gsd_flat - gso_flat)) <= TOL * np.max(np.abs(gso_flat))
+    # the state is left at the end of the trajectory, as the oracle's
+    fin = np.concatenate([a.ravel() for a in A.get()])
+    ref = np.concatenate([a.ravel() for a in orc.get_state()])
+    assert np.max(np.abs(fin - ref)) <= 1e-9
+
+
+def test_device_adjoint_matches_oracle_spin_boson():
+    m = sb.build(N=4, alpha=0.4, wc=5.0, d=3, chi=3, eps=0.3, delta=1.0)
+    rng = np.random.default_rng(5)
+    st = generic_state(m.topology, rng)
+    wt = rng.uniform(size=3)
+    _compare(m.topology, m.sop, st, 0.05, wt, 0, sb.SZ, ckpt=2)
+
+
+def test_device_adjoint_matches_oracle_random_operator():
+    rng = np.random.default_rng(201)
+    dims = [int(x) for x in rng.integers(2, 4, size=5)]
+    topo = random_tree(rng, dims, chi=2)
+    H = random_sop(rng, dims, nterms=10)
+    st = generic_state(topo, rng)
+    wt = rng.uniform(size=2)
+    _compare(topo, H, st, 0.1, wt, 0, rand_herm(rng, dims[0]), ckpt=1)
+
+
+def test_device_adjoint_rejects_mixed_precision_and_used_integrators():
+    m = sb.build(N=2, alpha=0.4, wc=5.0, d=3, chi=3, eps=0.3, delta=1.0)
+    rng = np.random.default_rng(1)
+    st = generic_state(m.topology, rng)
+    A = api.httensor(m.topology, device=0)
+    A.set(st)
+    mixed = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=8, precision=api.PREC_MIXED)
+    with pytest.raises(api.TTNError):
+        mixed.adjoint(A, 0.05, 1, [1.0], 0, sb.SZ)
+    plain = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=8)
+    plain(A)
+    with pytest.raises(api.TTNError):
+        plain.adjoint(A, 0.05, 1, [1.0], 0, sb.SZ)

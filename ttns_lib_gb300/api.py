@@ -101,6 +101,7 @@ SIGNATURES = {
     "ttn_debug_qr": (_I, [_I, _I, _DP, _DP, _I]),
     "ttn_qr_noalloc": (_I, [_I, _I, _P, _P, _P, _I]),
     "ttn_bond_singular_values": (_I, [_P, _P, _I, _DP, C.POINTER(C.c_int)]),
+    "ttn_adjoint_grad": (_I, [_P, _P, _D, _D, _D, _I, _DP, _I, _DP, _I, _I, _DP, _DP, _DP, _DP]),
     "ttn_batch_step": (_I, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _I, _D, _D, _I, C.POINTER(C.c_int)]),
     "ttn_debug_tc_gemm": (_I, [_DP, _DP, _DP, _I, _I, _I]),
 }
@@ -269,6 +270,7 @@ class fixed_step_projector_splitting_integrator:
         _check(lib().ttn_integrator_create(self.tree.h, self.op.h, C.byref(cfg), C.byref(h)))
         self.h = h
         self._mel = matrix_element(self)
+        self._sop = H
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -367,6 +369,36 @@ class fixed_step_projector_splitting_integrator:
 
     def mel(self) -> matrix_element:
         return self._mel
+
+    def adjoint(self, A: httensor, dt: float, nsteps: int, weights, mode: int, op, checkpoint_every: int = 20,
+                coeff: complex = -1j, skip_prepare: bool = False, state_cotangent: bool = False):
+        """J = sum_k weights[k] Re <op on mode>(end of step k) over ``nsteps`` steps of ``dt``
+        from ``A`` (left at the final state) and its gradient by the adjoint sweep on the
+        device: (J, dJ/dc_r per term, cotangent of every operator matrix in binding order
+        [, cotangent of the prepared state as a list of node tensors]).  The integrator must
+        be FP64 and at step 0."""
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        if w.size != nsteps:
+            raise ValueError("one weight per step")
+        o = np.ascontiguousarray(op, dtype=np.complex128)
+        J = C.c_double()
+        gc = np.zeros(self._sop.nterms)
+        dims = [int(b.matrix.shape[0]) for b in self._sop.ops]
+        gops = np.zeros(sum(d * d for d in dims), dtype=np.complex128)
+        offs = self.topo.offsets()
+        gs = np.zeros(int(offs[-1]), dtype=np.complex128) if state_cotangent else None
+        _check(lib().ttn_adjoint_grad(self.h, A.h, float(dt), float(np.real(coeff)), float(np.imag(coeff)), int(nsteps),
+                                      _dp(w), int(mode), _dp(o.view(np.float64)), int(checkpoint_every),
+                                      int(skip_prepare), C.byref(J), _dp(gc), _dp(gops.view(np.float64)),
+                                      _dp(gs.view(np.float64)) if gs is not None else None))
+        ops, off = [], 0
+        for d in dims:
+            ops.append(gops[off:off + d * d].reshape(d, d))
+            off += d * d
+        out = (J.value, gc, ops)
+        if state_cotangent:
+            out = out + ([gs[offs[i]:offs[i + 1]].reshape(self.topo.node_shape(i)) for i in range(self.topo.nnodes)],)
+        return out
 
     def synchronize(self):
         _check(lib().ttn_integrator_synchronize(self.h))

@@ -24,6 +24,7 @@
 #include <thread>
 #include <complex>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <random>
 #include <stdexcept>
@@ -155,6 +156,7 @@ struct Sop {
   std::vector<cd> coeff;
   std::vector<std::vector<std::vector<cd>>> ops;  // [mode][k] dense d x d
   std::vector<std::vector<int>> opidx;            // [mode][r]
+  std::vector<std::pair<int, int>> op_order;      // (mode, k) of every operator in binding order
 };
 
 // ------------------------------------------------------------------ compiled term plan
@@ -165,8 +167,12 @@ struct Sop {
 // operator_container.hpp:426-444, 648-664.
 enum { G_S = 0, G_M = 1, G_1 = 2 };
 struct Item { int slot, grp; };
-struct SpfTuple { cd a; std::vector<Item> items; };
-struct MfKey { cd b; int pg; std::vector<Item> sib; };
+// a_mem / b_mem: the terms whose coefficients were summed into a / b (empty when the
+// scalar is the constant 1); the adjoint sweep returns scalar cotangents through them.
+struct SpfTuple { cd a; std::vector<Item> items; std::vector<int> a_mem; };
+struct MfKey { cd b; int pg; std::vector<Item> sib; std::vector<int> b_mem; };
+// operations of a sweep, as reported to Integrator::on_op
+enum { OP_AFP = 1, OP_R2L, OP_MF, OP_NODE, OP_L2R, OP_SPF, OP_BOND, OP_ATP };
 struct Group {
   int type = G_1;
   std::vector<int> members;
@@ -275,6 +281,7 @@ static void compile_plan(const Tree& T, const Sop& H, std::vector<std::vector<Gr
           cd a = 0.0;
           for (int r : mem) a += H.coeff[r];
           t.a = a;
+          t.a_mem = mem;
         } else t.a = 1.0;
         g.spf.push_back(t);
       }
@@ -324,6 +331,7 @@ static void compile_plan(const Tree& T, const Sop& H, std::vector<std::vector<Gr
           cd b = 0.0;
           for (int r : mem) b += H.coeff[r];
           k.b = b;
+          k.b_mem = mem;
         } else k.b = 1.0;
         g.mf.push_back(k);
       }
@@ -447,6 +455,9 @@ struct Integrator {
     }
   };
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // called before every operation of a sweep (OP_*, node, auxiliary index) while set: the
+  // adjoint sweep records the operations' inputs through it
+  std::function<void(int, int, int)> on_op;
 
   ~Integrator() {
     if (ev0) cudaEventDestroy(ev0);
@@ -750,6 +761,7 @@ struct Integrator {
 
   // bottom-up environment (single_particle_operator.hpp:26-103)
   void update_spf(int nd, const double2* A) {
+    if (on_op) on_op(OP_SPF, nd, 0);
     Prof pf(this, 5, nd);
     const long long sz = T.size(nd);
     const int r = T.hrank[nd];
@@ -766,6 +778,7 @@ struct Integrator {
   // top-down environment of child nd (mean_field_operator.hpp:37-184)
   void update_mf(int nd, const double2* Ap) {
     if (nd == 0) return;
+    if (on_op) on_op(OP_MF, nd, 0);
     Prof pf(this, 4, T.parent[nd]);
     const int p = T.parent[nd], mu = T.slot[nd];
     long long na, nb;
@@ -1106,6 +1119,7 @@ struct Integrator {
   }
   static double qr_flops(double m, double n) { return 2.0 * 8.0 * (m * n * n - n * n * n / 3.0); }
   void l2r(int nd, double2* A) {
+    if (on_op) on_op(OP_L2R, nd, 0);
     Prof pf(this, 3, nd);
     const long long m = T.dimen[nd];
     const int r = T.hrank[nd];
@@ -1113,6 +1127,7 @@ struct Integrator {
     qr(A, m, r, rmat[nd], 0);
   }
   void apply_to_parent(int nd, double2* Ap, int p) {
+    if (on_op) on_op(OP_ATP, nd, 0);
     Prof pf(this, 6, p);
     long long na, nb;
     int d;
@@ -1121,6 +1136,7 @@ struct Integrator {
     zcopy(Ap, w4, T.size(p), stream);
   }
   void r2l(int nd, int mu, double2* A) {
+    if (on_op) on_op(OP_R2L, nd, mu);
     Prof pf(this, 2, nd);
     long long pre = 1, post = T.hrank[nd];
     for (int i = 0; i < mu; ++i) pre *= T.dims[nd][i];
@@ -1132,6 +1148,7 @@ struct Integrator {
     unpermute_mode_last(w4, A, pre, dm, post, stream);
   }
   void apply_from_parent(int nd, double2* A) {
+    if (on_op) on_op(OP_AFP, nd, 0);
     Prof pf(this, 7, nd);
     const int p = T.parent[nd], r = T.hrank[nd];
     right_mul(A, rmat[p], T.dimen[nd], r, w4);
@@ -1140,10 +1157,14 @@ struct Integrator {
 
   // ---------------------------------------------------------------- sweep
   void evolve_node(ttn_state* S, int nd) {
+    if (on_op) on_op(OP_NODE, nd, 0);
     Prof pf(this, 0, nd);
     expm_dev(nd, 0, S->node(nd), T.size(nd), dt / 2.0, coeff, true);
   }
-  void evolve_bond(int nd, double2* R) {
+  // the bond matrix held in rmat[owner]: the node's own after l2r, its parent's after r2l
+  void evolve_bond(int nd, int owner) {
+    if (on_op) on_op(OP_BOND, nd, owner);
+    double2* R = rmat[owner];
     Prof pf(this, 1, nd);
     const long long rr = (long long)T.hrank[nd] * T.hrank[nd];
     expm_dev(nd, 1, R, rr, -dt / 2.0, coeff, false);
@@ -1164,7 +1185,7 @@ struct Integrator {
         if (id != 0) {
           l2r(id, A);
           update_spf(id, A);
-          if (evolve) evolve_bond(id, rmat[id]);
+          if (evolve) evolve_bond(id, id);
           apply_to_parent(id, S->node(T.parent[id]), T.parent[id]);
         }
       }
@@ -1180,7 +1201,7 @@ struct Integrator {
         int mode = T.nmodes[id] - (t + 1);
         if (t == 0) {
           if (id != 0) {
-            if (evolve) evolve_bond(id, rmat[T.parent[id]]);
+            if (evolve) evolve_bond(id, T.parent[id]);
             apply_from_parent(id, A);
           }
           if (evolve) evolve_node(S, id);
@@ -1356,6 +1377,8 @@ struct Integrator {
   }
 };
 
+#include "ttn_adjoint.hpp"
+
 static void check_same_tree(const Tree& a, const Tree& b) {
   TTN_REQUIRE(a.parent == b.parent && a.hrank == b.hrank && a.leaf_dim == b.leaf_dim && a.leaf_mode == b.leaf_mode,
               TTN_EINVAL, "state and integrator were built for different trees");
@@ -1449,6 +1472,7 @@ static void sop_bind(ttn_sop* s, int mode, std::vector<ttn::cd>&& M, const int* 
   for (auto& z : M) TTN_REQUIRE(std::isfinite(z.real()) && std::isfinite(z.imag()), TTN_EINVAL, "non-finite operator entry");
   int k = (int)s->H.ops[mode].size();
   s->H.ops[mode].push_back(std::move(M));
+  s->H.op_order.push_back({mode, k});
   for (int q = 0; q < nr; ++q) s->H.opidx[mode][r[q]] = k;
 }
 int ttn_sop_bind_dense(ttn_sop* s, int mode, const double* mat, const int* r, int nr) {
@@ -1751,6 +1775,54 @@ int ttn_bond_singular_values(ttn_integrator* it, ttn_state* psi, int node, doubl
   const auto sv = it->I.bond_sv(psi, node);
   for (size_t k = 0; k < sv.size(); ++k) out[k] = sv[k];
   if (n) *n = (int)sv.size();
+  TTN_API_END
+}
+int ttn_adjoint_grad(ttn_integrator* it, ttn_state* psi, double dt, double coeff_re, double coeff_im, int nsteps,
+                     const double* weights, int mode, const double* op, int checkpoint_every, int skip_prepare,
+                     double* J, double* grad_coeff, double* grad_ops, double* grad_state) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi && weights && op && J && grad_coeff && grad_ops, TTN_EINVAL, "null argument");
+  ttn::check_same_tree(it->I.T, psi->T);
+  ttn::Integrator& I = it->I;
+  TTN_REQUIRE(nsteps >= 1, TTN_EINVAL, "nsteps must be >= 1");
+  TTN_REQUIRE(std::isfinite(dt) && dt > 0.0, TTN_EINVAL, "dt must be positive and finite");
+  TTN_REQUIRE(mode >= 0 && mode < I.H.nmodes, TTN_EINVAL, "mode out of range");
+  TTN_REQUIRE(!I.mixed, TTN_EINVAL, "the adjoint sweep needs an FP64 integrator (TTN_PREC_FP64)");
+  TTN_REQUIRE(I.nsteps == 0, TTN_EINVAL, "the adjoint sweep starts from step 0 (a fresh or reset integrator)");
+  for (int k = 0; k < nsteps; ++k) TTN_REQUIRE(std::isfinite(weights[k]), TTN_EINVAL, "non-finite weight");
+  CK(cudaSetDevice(I.device));
+  const int d = I.H.mode_dim[mode];
+  std::vector<double2> oh((size_t)d * d);
+  for (size_t i = 0; i < oh.size(); ++i) {
+    TTN_REQUIRE(std::isfinite(op[2 * i]) && std::isfinite(op[2 * i + 1]), TTN_EINVAL, "non-finite operator entry");
+    oh[i] = make_double2(op[2 * i], op[2 * i + 1]);
+  }
+  ttn::DevBuf opd;
+  opd.alloc(oh.size() * sizeof(double2));
+  CK(cudaMemcpyAsync(opd.p, oh.data(), oh.size() * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  CK(cudaStreamSynchronize(I.stream));
+  ttn::DevAdjoint adj(I, psi);
+  *J = adj.run(dt, ttn::cd(coeff_re, coeff_im), nsteps, weights, mode, opd.as<double2>(), checkpoint_every,
+               skip_prepare != 0);
+  for (int r = 0; r < I.H.nterms; ++r) grad_coeff[r] = adj.gc[r];
+  size_t off = 0;
+  for (const auto& mk : I.H.op_order) {
+    const auto& G = adj.gop[mk.first][mk.second];
+    for (size_t i = 0; i < G.size(); ++i) {
+      grad_ops[2 * (off + i)] = G[i].real();
+      grad_ops[2 * (off + i) + 1] = G[i].imag();
+    }
+    off += G.size();
+  }
+  if (grad_state) {
+    size_t o = 0;
+    for (int i = 0; i < I.T.n; ++i) {
+      const long long sz = I.T.size(i);
+      CK(cudaMemcpyAsync(grad_state + 2 * o, adj.ab[i], sz * sizeof(double2), cudaMemcpyDeviceToHost, I.stream));
+      o += sz;
+    }
+    CK(cudaStreamSynchronize(I.stream));
+  }
   TTN_API_END
 }
 int ttn_norm2(ttn_integrator* it, ttn_state* psi, double* out) {

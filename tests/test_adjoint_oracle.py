@@ -131,3 +131,33 @@ def test_adjoint_objective_equals_plain_steps():
         o.step(0.05)
         ref += wt[k] * o.expect(0, sb.SZ).real
     assert J == ref
+
+
+def test_torch_objective_wrapper_returns_the_adjoint_gradient():
+    """The torch.autograd.Function wrapper (a check harness) around an adjoint evaluator:
+    autograd returns the adjoint gradient, which matches central differences of J."""
+    torch = pytest.importorskip("torch")
+    from ttns_lib_gb300 import api
+    N, d, chi, dt = 3, 3, 3, 0.05
+    w0, c0 = sb.ohmic_modes(N, 0.4, 5.0)
+    rng = np.random.default_rng(21)
+    topo = sb.build_from_modes(w0, c0, d, chi, 0.3, 1.0).topology
+    st = generic_state(topo, rng)
+    wt = rng.uniform(size=2)
+
+    def evaluate(theta):
+        m = sb.build_from_modes(w0, theta[2:], d, chi, theta[0], theta[1])
+        J, _, gops = _adjoint(topo, m.sop, st, dt, wt, 0, sb.SZ)
+        g = sb.parameter_gradient(m, gops)
+        return J, np.concatenate([[g["eps"], g["delta"]], g["coupling"]])
+
+    f = api.torch_objective(evaluate)
+    theta = torch.tensor(np.concatenate([[0.3, 1.0], c0]), dtype=torch.float64, requires_grad=True)
+    J = f(theta)
+    (grad,) = torch.autograd.grad(J, theta)
+    th = theta.detach().numpy()
+    fd = np.zeros_like(th)
+    for i in range(th.size):
+        e = np.zeros_like(th); e[i] = H_FD
+        fd[i] = (evaluate(th + e)[0] - evaluate(th - e)[0]) / (2 * H_FD)
+    assert np.max(np.abs(grad.numpy() - fd)) <= 1e-5 * np.max(np.abs(fd))

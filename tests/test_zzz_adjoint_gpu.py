@@ -72,3 +72,40 @@ def test_device_adjoint_rejects_mixed_precision_and_used_integrators():
     plain(A)
     with pytest.raises(api.TTNError):
         plain.adjoint(A, 0.05, 1, [1.0], 0, sb.SZ)
+
+
+def test_device_adjoint_through_torch_matches_plain_path_differences():
+    """dJ/d(eps, Delta, c_k) from the device adjoint through the torch.autograd wrapper
+    against central differences of J computed by the plain FP64 device path
+    (ttn_integrator_step and <sz> after every step), within 1e-5 relative."""
+    torch = pytest.importorskip("torch")
+    N, d, chi, dt, h = 3, 3, 3, 0.05, 1e-5
+    w0, c0 = sb.ohmic_modes(N, 0.4, 5.0)
+    rng = np.random.default_rng(21)
+    topo = sb.build_from_modes(w0, c0, d, chi, 0.3, 1.0).topology
+    st = generic_state(topo, rng)
+    wt = rng.uniform(size=3)
+    f = api.torch_objective(api.spin_boson_adjoint(w0, d, chi, st, dt, wt, krylov_dim=10, krylov_tolerance=1e-14,
+                                                   checkpoint_every=2))
+    theta = torch.tensor(np.concatenate([[0.3, 1.0], c0]), dtype=torch.float64, requires_grad=True)
+    (grad,) = torch.autograd.grad(f(theta), theta)
+
+    def plain_J(th):
+        m = sb.build_from_modes(w0, th[2:], d, chi, th[0], th[1])
+        A = api.httensor(topo, device=0)
+        A.set(st)
+        integ = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=10, krylov_tolerance=1e-14)
+        integ.dt = dt
+        J = 0.0
+        for k in range(len(wt)):
+            integ(A, m.sop, -1j)
+            J += wt[k] * integ.mel()(sb.SZ, 0, A).real
+        return J
+
+    th = theta.detach().numpy()
+    fd = np.zeros_like(th)
+    for i in range(th.size):
+        e = np.zeros_like(th)
+        e[i] = h
+        fd[i] = (plain_J(th + e) - plain_J(th - e)) / (2 * h)
+    assert np.max(np.abs(grad.numpy() - fd)) <= 1e-5 * np.max(np.abs(fd))

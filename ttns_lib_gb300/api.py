@@ -439,6 +439,50 @@ class fixed_step_projector_splitting_integrator:
         return out
 
 
+def torch_objective(evaluate):
+    """Wrap ``evaluate(theta) -> (J, dJ/dtheta)`` (numpy in, numpy out) as a function of a
+    1-D torch tensor whose backward returns that gradient, so that the adjoint sweep can
+    be checked with torch's autograd tooling (a check harness, not the product path: the
+    gradient itself comes from ``ttn_adjoint_grad``)."""
+    import torch
+
+    class _Objective(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, theta):
+            J, g = evaluate(theta.detach().cpu().numpy())
+            ctx.save_for_backward(torch.as_tensor(np.asarray(g), dtype=theta.dtype, device=theta.device))
+            return theta.new_tensor(float(J))
+
+        @staticmethod
+        def backward(ctx, gJ):
+            (g,) = ctx.saved_tensors
+            return gJ * g
+
+    return _Objective.apply
+
+
+def spin_boson_adjoint(omega, d: int, chi: int, state, dt: float, weights, krylov_dim: int = 12,
+                       krylov_tolerance: float = 1e-12, checkpoint_every: int = 20, device: int = 0):
+    """``evaluate(theta)`` for ``torch_objective``: theta = (eps, Delta, c_1..c_N) of a
+    zero-temperature spin-boson model with bath frequencies ``omega``; J = sum_t w_t <sz>(t)
+    over len(weights) steps from ``state``, gradient by the device adjoint sweep."""
+    from . import spin_boson as sb
+    omega = np.asarray(omega, dtype=np.float64)
+
+    def evaluate(theta):
+        theta = np.asarray(theta, dtype=np.float64)
+        m = sb.build_from_modes(omega, theta[2:], d, chi, float(theta[0]), float(theta[1]))
+        A = httensor(m.topology, device=device)
+        A.set(state)
+        integ = fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=krylov_dim,
+                                                          krylov_tolerance=krylov_tolerance)
+        J, _, gops = integ.adjoint(A, dt, len(weights), weights, 0, sb.SZ, checkpoint_every=checkpoint_every)
+        g = sb.parameter_gradient(m, gops)
+        return J, np.concatenate([[g["eps"], g["delta"]], g["coupling"]])
+
+    return evaluate
+
+
 def launch_count() -> int:
     out = C.c_ulonglong()
     _check(lib().ttn_launch_count(C.byref(out)))

@@ -305,7 +305,10 @@ static void compile_plan(const Tree& T, const SOP& H, Plan& P) {
     auto& G = P.groups[nd];
     auto add = [&](const std::vector<int>& mem, int type) {
       Group g; g.type = type; g.members = mem;
-      g.id_spf = Ls[mem[0]].empty();
+      // the identity below the node only if every member is: an M group may mix a term that
+      // acts below with one that does not (the latter contributes its coefficient times I)
+      g.id_spf = true;
+      for (int r : mem) g.id_spf = g.id_spf && Ls[r].empty();
       g.s = (type == G_1) ? H.coeff[mem[0]] : cd(1.0);
       for (int r : mem) P.group_of[nd][r] = (int)G.size();
       G.push_back(g);
@@ -321,7 +324,11 @@ static void compile_plan(const Tree& T, const SOP& H, Plan& P) {
       std::map<std::vector<int>, std::vector<int>> keys;  // key -> members
       for (int r : g.members) {
         std::vector<int> key;
-        if (T.leaf(nd)) key.push_back(H.opidx[T.leaf_mode[nd]][r]);
+        // at a leaf the key is the term's operator there; a member that is the identity on
+        // the leaf (possible in an M group) has an empty key, i.e. a tuple without items
+        if (T.leaf(nd)) {
+          if (H.opidx[T.leaf_mode[nd]][r] >= 0) key.push_back(H.opidx[T.leaf_mode[nd]][r]);
+        }
         else
           for (int s = 0; s < (int)T.children[nd].size(); ++s) {
             int c = T.children[nd][s];
@@ -339,7 +346,9 @@ static void compile_plan(const Tree& T, const SOP& H, Plan& P) {
         const auto& mem = keys[key];
         SpfTuple t;
         bool carrying = false;
-        if (T.leaf(nd)) t.items.push_back({-1, key[0]});
+        if (T.leaf(nd)) {
+          if (!key.empty()) t.items.push_back({-1, key[0]});
+        }
         else
           for (size_t q = 0; q < key.size(); q += 2) {
             int c = T.children[nd][key[q]];

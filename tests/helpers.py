@@ -85,3 +85,16 @@ def generic_state(topo, rng):
             a /= np.linalg.norm(a)
         st.append(np.ascontiguousarray(a))
     return st
+
+
+def random_case(seed, chi=None, max_children=None):
+    """A random tree, a random SOP operator of random shape (number of terms, modes per
+    term, sharing, duplicates) and a generic state.  The shapes include groups that mix
+    terms acting below a node with terms that are the identity there."""
+    rng = np.random.default_rng(seed)
+    dims = [int(x) for x in rng.integers(2, 4, size=int(rng.integers(3, 6)))]
+    mc = int(rng.integers(2, 4)) if max_children is None else max_children
+    topo = random_tree(rng, dims, max_children=mc, chi=chi)
+    H = random_sop(rng, dims, nterms=int(rng.integers(3, 12)))
+    st = generic_state(topo, rng)
+    return topo, H, st, dims

@@ -1,0 +1,241 @@
+// TEST DOUBLE, CPU only: stand-ins for the CUDA runtime calls and for the kernel
+// wrappers (ttn_kernels.cuh, ttn_expm.cuh) that the host orchestration in
+// ttns_lib_gb300/csrc/ttn_host.cpp calls, so that the orchestration itself -- sweeps,
+// term programs, the adjoint sweep's recording and reverse passes -- runs in the CPU
+// test suite and is compared with the oracle.  Linked only into the library that
+// tests/test_host_orchestration.py builds under tests/host_double/_build; the package
+// never loads it (its library is the CUDA build, which fails loudly when absent).
+//   * device memory is host memory; streams and events do nothing;
+//   * zgemm follows the operand maps of ZOperand / ZGemm literally;
+//   * the Householder QR is the oracle's (LAPACK zgeqrf / zungqr conventions);
+//   * the persistent Krylov kernel applies the term program (MODE / MF / AXPY / ZERO)
+//     exactly and evolves by a Taylor series of the dense matrix with sub-steps of norm
+//     at most 1/4 (errors near 1e-15), and leaves a Lanczos matrix of the start vector in
+//     the control block as the device kernel does.
+#include <cuda_runtime_api.h>
+#include <cstdlib>
+#include <cstring>
+#include <cmath>
+#include <complex>
+#include <vector>
+#include <atomic>
+#include <algorithm>
+#include "../../ttns_lib_gb300/csrc/ttn_kernels.cuh"
+#include "../../ttns_lib_gb300/csrc/ttn_expm.cuh"
+#include "../../ttns_lib_gb300/csrc/ttn_coop.cuh"
+
+#include "../../oracle/ttn_oracle.cpp"  // householder_qr
+
+typedef std::complex<double> zc;
+static inline zc Z(double2 v) { return zc(v.x, v.y); }
+static inline double2 D(zc v) { return make_double2(v.real(), v.imag()); }
+
+extern "C" {
+cudaError_t cudaMalloc(void** p, size_t b) { *p = std::calloc(1, b ? b : 16); return cudaSuccess; }
+cudaError_t cudaFree(void* p) { std::free(p); return cudaSuccess; }
+cudaError_t cudaMallocHost(void** p, size_t b) { *p = std::calloc(1, b ? b : 16); return cudaSuccess; }
+cudaError_t cudaFreeHost(void* p) { std::free(p); return cudaSuccess; }
+cudaError_t cudaMemcpy(void* d, const void* s, size_t b, enum cudaMemcpyKind) { std::memmove(d, s, b); return cudaSuccess; }
+cudaError_t cudaMemcpyAsync(void* d, const void* s, size_t b, enum cudaMemcpyKind, cudaStream_t) { std::memmove(d, s, b); return cudaSuccess; }
+cudaError_t cudaMemset(void* d, int v, size_t b) { std::memset(d, v, b); return cudaSuccess; }
+cudaError_t cudaMemsetAsync(void* d, int v, size_t b, cudaStream_t) { std::memset(d, v, b); return cudaSuccess; }
+cudaError_t cudaSetDevice(int) { return cudaSuccess; }
+cudaError_t cudaStreamCreate(cudaStream_t* s) { *s = (cudaStream_t)std::malloc(8); return cudaSuccess; }
+cudaError_t cudaStreamDestroy(cudaStream_t s) { std::free((void*)s); return cudaSuccess; }
+cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }
+cudaError_t cudaDeviceSynchronize(void) { return cudaSuccess; }
+cudaError_t cudaGetLastError(void) { return cudaSuccess; }
+const char* cudaGetErrorString(cudaError_t) { return "mock"; }
+cudaError_t cudaEventCreate(cudaEvent_t* e) { *e = (cudaEvent_t)std::malloc(8); return cudaSuccess; }
+cudaError_t cudaEventDestroy(cudaEvent_t e) { std::free((void*)e); return cudaSuccess; }
+cudaError_t cudaEventRecord(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
+cudaError_t cudaEventSynchronize(cudaEvent_t) { return cudaSuccess; }
+cudaError_t cudaEventElapsedTime(float* ms, cudaEvent_t, cudaEvent_t) { *ms = 1.0f; return cudaSuccess; }
+cudaError_t cudaDeviceGetAttribute(int* v, enum cudaDeviceAttr a, int) {
+  *v = (a == cudaDevAttrMultiProcessorCount) ? 152 : 1;
+  return cudaSuccess;
+}
+cudaError_t cudaGetDeviceProperties_v2(struct cudaDeviceProp* p, int) {
+  std::memset(p, 0, sizeof(*p));
+  std::strcpy(p->name, "mock");
+  p->multiProcessorCount = 152; p->major = 10; p->minor = 3;
+  return cudaSuccess;
+}
+cudaError_t cudaGetDeviceProperties(struct cudaDeviceProp* p, int d) { return cudaGetDeviceProperties_v2(p, d); }
+}
+
+namespace ttn {
+std::atomic<unsigned long long> g_launches{0};
+
+static zc opA(const ZOperand& o, long long i, long long k) {
+  const double2 v = o.p[i * o.s0 + (k / o.kdiv) * o.k1 + (k % o.kdiv) * o.k2];
+  return o.cj ? std::conj(Z(v)) : Z(v);
+}
+size_t zgemm_split_workspace_bytes(int M, int N, int K) { (void)K; return (size_t)4 * M * N * sizeof(double2); }
+void zgemm(const ZGemm& g, double2* ws, size_t ws_bytes, cudaStream_t s) {
+  (void)ws; (void)ws_bytes; (void)s;
+  for (int z = 0; z < g.batch; ++z) {
+    ZOperand A = g.A, B = g.B;
+    A.p += (long long)z * g.bsA; B.p += (long long)z * g.bsB;
+    double2* C = g.C + (long long)z * g.bsC;
+    for (int i = 0; i < g.M; ++i)
+      for (int j = 0; j < g.N; ++j) {
+        zc s = 0.0;
+        for (int k = 0; k < g.K; ++k) s += opA(A, i, k) * opA(B, j, k);
+        zc c = Z(g.alpha) * s;
+        double2& out = C[(long long)i * g.ci + (long long)j * g.cj];
+        if (g.beta.x != 0.0 || g.beta.y != 0.0) c += Z(g.beta) * Z(out);
+        out = D(c);
+      }
+  }
+  ++g_launches;
+}
+int coop_qr_grid(long long m, int n) { (void)m; (void)n; return 1; }
+int qr_blocked_max_grid() { return 1; }
+size_t qr_blocked_scratch_bytes(int g) { (void)g; return 1024; }
+cudaError_t householder_qr_blocked(double2* M, long long m, int n, double2* R, int Rt, double2* tau, double* scratch,
+                                   GridBarrier* bar, int* err, int grid, cudaStream_t s) {
+  (void)tau; (void)scratch; (void)bar; (void)err; (void)grid; (void)s;
+  std::vector<cd> Rr((size_t)n * n), t;
+  orc::householder_qr(reinterpret_cast<cd*>(M), (size_t)m, n, Rr.data(), t);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) R[(size_t)i * n + j] = D(Rt ? Rr[(size_t)j * n + i] : Rr[(size_t)i * n + j]);
+  ++g_launches;
+  return cudaSuccess;
+}
+void permute_mode_last(const double2* A, double2* M, long long pre, int dm, long long post, cudaStream_t) {
+  for (long long e = 0; e < pre * dm * post; ++e) {
+    long long x = e / ((long long)dm * post), rem = e % ((long long)dm * post), i = rem / post, y = rem % post;
+    M[(y * pre + x) * dm + i] = A[e];
+  }
+}
+void unpermute_mode_last(const double2* M, double2* A, long long pre, int dm, long long post, cudaStream_t) {
+  for (long long e = 0; e < pre * dm * post; ++e) {
+    long long x = e / ((long long)dm * post), rem = e % ((long long)dm * post), i = rem / post, y = rem % post;
+    A[e] = M[(y * pre + x) * dm + i];
+  }
+}
+void zcopy(double2* d, const double2* s, long long n, cudaStream_t) { std::memmove(d, s, n * sizeof(double2)); }
+void zaxpy(double2* out, const double2* x, double2 sc, long long n, bool acc, cudaStream_t) {
+  for (long long i = 0; i < n; ++i) { zc r = Z(sc) * Z(x[i]); if (acc) r += Z(out[i]); out[i] = D(r); }
+}
+void zfill(double2* d, double2 v, long long n, cudaStream_t) { for (long long i = 0; i < n; ++i) d[i] = v; }
+void zscale_identity(double2* d, int r, double2 v, cudaStream_t) {
+  for (int e = 0; e < r * r; ++e) d[e] = (e / r == e % r) ? v : make_double2(0.0, 0.0);
+}
+void ztrace(const double2* M, int r, double2* out, cudaStream_t) {
+  zc s = 0.0; for (int k = 0; k < r; ++k) s += Z(M[(long long)k * r + k]); *out = D(s);
+}
+void check_finite(const double2* x, long long n, int* status, int code, cudaStream_t) {
+  for (long long i = 0; i < n; ++i) if (!std::isfinite(x[i].x) || !std::isfinite(x[i].y)) { *status |= code; return; }
+}
+double measure_fp64_fma_tflops() { return 1.0; }
+cudaError_t tc_gemm_test(const double*, const double*, double*, int, int, int*, cudaStream_t) { return cudaSuccess; }
+int expm_coop_max_grid(int) { return 1; }
+size_t expm_partial_bytes(int g) { return (size_t)(2 * g + 1) * 64 * 16; }
+
+static void apply_prog(const ExpmArgs& a, const double2* x, double2* out) {
+  double2* b[5] = {const_cast<double2*>(x), out, a.t1, a.t2, a.t3};
+  const MvOp* ops = a.prog ? a.prog : &a.op1;
+  for (int q = 0; q < a.nops; ++q) {
+    const MvOp& o = ops[q];
+    const double2* in = b[o.in];
+    double2* ob = b[o.out];
+    const zc al = Z(o.alpha);
+    if (o.kind == MV_MODE) {
+      std::vector<zc> t((size_t)o.na * o.d * o.nb);
+      for (long long aa = 0; aa < o.na; ++aa)
+        for (int i = 0; i < o.d; ++i)
+          for (long long bb = 0; bb < o.nb; ++bb) {
+            zc s = 0.0;
+            for (int j = 0; j < o.d; ++j) s += Z(o.mat[(size_t)i * o.d + j]) * Z(in[(aa * o.d + j) * o.nb + bb]);
+            t[(aa * o.d + i) * o.nb + bb] = al * s;
+          }
+      for (size_t e = 0; e < t.size(); ++e) ob[e] = D(o.beta ? t[e] + Z(ob[e]) : t[e]);
+    } else if (o.kind == MV_MF) {
+      const int r = o.d;
+      std::vector<zc> t((size_t)o.na * r);
+      for (long long xx = 0; xx < o.na; ++xx)
+        for (int k = 0; k < r; ++k) {
+          zc s = 0.0;
+          for (int l = 0; l < r; ++l) s += Z(in[xx * r + l]) * Z(o.mat[(size_t)k * r + l]);
+          t[xx * r + k] = al * s;
+        }
+      for (size_t e = 0; e < t.size(); ++e) ob[e] = D(o.beta ? t[e] + Z(ob[e]) : t[e]);
+    } else if (o.kind == MV_AXPY) {
+      for (long long e = 0; e < o.na; ++e) { zc r = al * Z(in[e]); if (o.beta) r += Z(ob[e]); ob[e] = D(r); }
+    } else {
+      for (long long e = 0; e < o.na; ++e) ob[e] = make_double2(0.0, 0.0);
+    }
+  }
+}
+
+cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s, int threads) {
+  (void)grid; (void)s; (void)threads;
+  ++g_launches;
+  if (a.apply_only) { apply_prog(a, a.y, a.p); return cudaSuccess; }
+  const long long n = a.n;
+  std::vector<double2> tmp(n);
+  auto H = [&](const std::vector<zc>& v, std::vector<zc>& o) {
+    std::vector<double2> x(n), y(n);
+    for (long long i = 0; i < n; ++i) x[i] = D(v[i]);
+    apply_prog(a, x.data(), y.data());
+    o.resize(n);
+    for (long long i = 0; i < n; ++i) o[i] = Z(y[i]);
+  };
+  std::vector<zc> y(n);
+  for (long long i = 0; i < n; ++i) y[i] = Z(a.y[i]);
+  // Lanczos matrix of the start vector (what the device controller leaves behind)
+  {
+    KrylovCtl& c = *a.ctl;
+    const int m = std::min<long long>(a.m, n);
+    double nv = 0; for (auto& z : y) nv += std::norm(z); nv = std::sqrt(nv);
+    std::vector<zc> q(n), qp(n, 0.0), w;
+    for (long long i = 0; i < n; ++i) q[i] = nv > 0 ? y[i] / nv : zc(i == 0 ? 1.0 : 0.0);
+    double bprev = 0.0; int mb = 0;
+    for (int j = 0; j < m; ++j) {
+      H(q, w);
+      double al = 0; for (long long i = 0; i < n; ++i) al += (std::conj(q[i]) * w[i]).real();
+      for (long long i = 0; i < n; ++i) w[i] -= al * q[i] + bprev * qp[i];
+      double b = 0; for (auto& z : w) b += std::norm(z); b = std::sqrt(b);
+      c.alpha[j] = al; mb = j + 1;
+      if (b < 1e-12) break;
+      c.bet[j + 1] = b; qp = q; for (long long i = 0; i < n; ++i) q[i] = w[i] / b; bprev = b;
+    }
+    c.mb = mb;
+  }
+  // dense matrix, norm bound, Taylor with sub-steps
+  std::vector<std::vector<zc>> cols(n);
+  std::vector<zc> e(n, 0.0);
+  double n1 = 0, ninf = 0;
+  std::vector<double> rows(n, 0.0);
+  for (long long j = 0; j < n; ++j) {
+    std::fill(e.begin(), e.end(), zc(0.0)); e[j] = 1.0;
+    H(e, cols[j]);
+    double cs = 0; for (long long i = 0; i < n; ++i) { cs += std::abs(cols[j][i]); rows[i] += std::abs(cols[j][i]); }
+    n1 = std::max(n1, cs);
+  }
+  for (double r : rows) ninf = std::max(ninf, r);
+  const zc z = zc(a.cf_re, a.cf_im) * a.tau;
+  const double bound = std::sqrt(n1 * ninf) * std::abs(z);
+  const int steps = std::max(1, (int)std::ceil(bound / 0.25));
+  const zc zs = z / (double)steps;
+  for (int st = 0; st < steps; ++st) {
+    std::vector<zc> term = y, acc = y, nt(n);
+    for (int k = 1; k <= 40; ++k) {
+      for (long long i = 0; i < n; ++i) {
+        zc s = 0.0;
+        for (long long j = 0; j < n; ++j) s += cols[j][i] * term[j];
+        nt[i] = s * zs / (double)k;
+      }
+      term = nt;
+      for (long long i = 0; i < n; ++i) acc[i] += term[i];
+    }
+    y = acc;
+  }
+  for (long long i = 0; i < n; ++i) a.y[i] = D(y[i]);
+  if (a.napps_total) *a.napps_total += 1;
+  return cudaSuccess;
+}
+}  // namespace ttn
+extern "C" int ttn_qr_noalloc(int, int, double*, double*, void*, int) { return 1; }

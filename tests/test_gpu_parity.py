@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 import scipy.linalg as sla
 
-from helpers import generic_state, random_sop, random_tree
+from helpers import generic_state, random_case, random_sop, random_tree
 from oracle.oracle import Oracle, qr as oracle_qr
 from ttns_lib_gb300 import api
 from ttns_lib_gb300 import spin_boson as sb
@@ -65,6 +65,30 @@ def test_device_qr_tiny_columns_match_oracle():
     qo, ro = oracle_qr(a)
     assert np.isfinite(qd).all() and np.isfinite(rd).all()
     assert rel(qd, qo) < 1e-12 and rel(rd, ro) < 1e-12
+
+
+@pytest.mark.parametrize("seed", [310, 312, 338])
+def test_random_operator_shapes_match_oracle_and_dense_expm(seed):
+    """Operators whose groups mix terms acting below a node with terms that are the
+    identity there: H_eff of every node against the oracle, then sweeps against exp(-iHt)."""
+    topo, H, st, _ = random_case(seed)
+    orc, A, dev = make_pair(topo, H, st, m=10)
+    orc.refresh_env()
+    dev.refresh_env(A)
+    rng = np.random.default_rng(seed)
+    for node in range(topo.nnodes):
+        v = rng.normal(size=topo.node_shape(node)) + 1j * rng.normal(size=topo.node_shape(node))
+        assert rel(dev.heff(node, v), orc.heff(node, v)) < 1e-12
+        assert rel(dev.program_apply(node, v), orc.heff(node, v)) < 1e-12
+    psi = full_state(topo, st)
+    B = api.httensor(topo)
+    B.set(st)
+    integ = api.fixed_step_projector_splitting_integrator(B, H, krylov_dim=10)
+    integ.dt = 0.1
+    for k in range(3):
+        integ(B, H, -1j)
+        ex = sla.expm(-1j * H.dense() * (k + 1) * 0.1) @ psi
+        assert np.linalg.norm(full_state(topo, B.get()) - ex) < 1e-10
 
 
 def spin_boson_small():

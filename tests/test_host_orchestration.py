@@ -1,0 +1,128 @@
+"""The host orchestration of the CUDA library (ttns_lib_gb300/csrc/ttn_host.cpp, with the
+adjoint sweep of ttn_adjoint.hpp) run on the CPU against a test double of the CUDA
+runtime and of the kernel wrappers (tests/host_double/mock_cuda.cpp), and compared with
+the oracle: the plain sweep, and the adjoint sweep's objective and gradients.  This checks
+what the GPU tests cannot isolate -- the sequence of operations, their operands, the
+tape, the environment snapshots and the host-side cotangent algebra -- while the kernels
+themselves are checked on the GB300 by the gpu-marked tests.  The double is built here
+with g++ and loaded in a child process only."""
+import json
+import os
+import shutil
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HERE = os.path.join(ROOT, "tests", "host_double")
+OUT = os.path.join(HERE, "_build", "libttn_host_double.so")
+CUDA_INC = "/usr/local/cuda/include"
+
+
+def _build():
+    if shutil.which("g++") is None or not os.path.exists(os.path.join(CUDA_INC, "cuda_runtime_api.h")):
+        pytest.skip("g++ or the CUDA headers are missing")
+    srcs = [os.path.join(ROOT, "ttns_lib_gb300", "csrc", "ttn_host.cpp"), os.path.join(HERE, "mock_cuda.cpp")]
+    deps = srcs + [os.path.join(ROOT, "ttns_lib_gb300", "csrc", f) for f in os.listdir(os.path.join(ROOT, "ttns_lib_gb300", "csrc"))
+                   if f.endswith((".cuh", ".hpp"))]
+    deps += [os.path.join(ROOT, "include", "ttn_gb300.h"), os.path.join(ROOT, "oracle", "ttn_oracle.cpp"),
+             os.path.join(ROOT, "oracle", "ttn_adjoint.hpp")]
+    if os.path.exists(OUT) and os.path.getmtime(OUT) >= max(os.path.getmtime(d) for d in deps):
+        return OUT
+    os.makedirs(os.path.dirname(OUT), exist_ok=True)
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           "-I", os.path.join(ROOT, "include"), "-I", CUDA_INC, "-o", OUT]
+    for s in srcs:
+        cmd += ["-x", "c++", s]
+    subprocess.check_call(cmd)
+    return OUT
+
+
+CHILD = r"""
+import json, sys
+import numpy as np
+sys.path.insert(0, {root!r}); sys.path.insert(0, {tests!r})
+from ttns_lib_gb300 import api
+api.LIB_PATH = {lib!r}
+from ttns_lib_gb300 import spin_boson as sb
+from oracle.oracle import Oracle
+from helpers import generic_state, rand_herm, random_case, random_sop, random_tree
+
+out = {{}}
+
+def flat(ts):
+    return np.concatenate([np.asarray(t).ravel() for t in ts])
+
+def plain(name, topo, H, st, dt, steps):
+    A = api.httensor(topo, device=0); A.set(st)
+    integ = api.fixed_step_projector_splitting_integrator(A, H, krylov_dim=10, krylov_tolerance=1e-13)
+    integ.dt = dt
+    orc = Oracle(topo, H, krylov_dim=10, krylov_tol=1e-13); orc.set_state(st)
+    for _ in range(steps):
+        integ(A); orc.step(dt)
+    out[name] = float(np.max(np.abs(flat(A.get()) - flat(orc.get_state()))))
+
+def adjoint(name, topo, H, st, dt, wt, mode, O, ckpt):
+    orc = Oracle(topo, H, krylov_dim=10, krylov_tol=1e-13); orc.set_state(st)
+    Jo, gco, gopo, gso = orc.adjoint(dt, len(wt), wt, mode, O, checkpoint_every=ckpt, state_cotangent=True)
+    A = api.httensor(topo, device=0); A.set(st)
+    integ = api.fixed_step_projector_splitting_integrator(A, H, krylov_dim=10, krylov_tolerance=1e-13)
+    Jd, gcd, gopd, gsd = integ.adjoint(A, dt, len(wt), wt, mode, O, checkpoint_every=ckpt, state_cotangent=True)
+    scale = max(np.max(np.abs(gco)), max(np.max(np.abs(g)) for g in gopo))
+    out[name] = dict(J=abs(Jd - Jo) / max(1.0, abs(Jo)),
+                     coeff=float(np.max(np.abs(gcd - gco)) / scale),
+                     ops=float(max(np.max(np.abs(a - b)) for a, b in zip(gopd, gopo)) / scale),
+                     state=float(np.max(np.abs(flat(gsd) - gso)) / np.max(np.abs(gso))),
+                     final=float(np.max(np.abs(flat(A.get()) - flat(orc.get_state())))))
+
+m = sb.build(N=4, alpha=0.4, wc=5.0, d=3, chi=3, eps=0.3, delta=1.0)
+rng = np.random.default_rng(5)
+st = generic_state(m.topology, rng)
+plain("plain_spin_boson", m.topology, m.sop, st, 0.05, 3)
+adjoint("adjoint_spin_boson", m.topology, m.sop, st, 0.05, rng.uniform(size=3), 0, sb.SZ, 2)
+for seed, chi in ((201, 2), (202, None)):
+    rng = np.random.default_rng(seed)
+    dims = [int(x) for x in rng.integers(2, 4, size=5)]
+    topo = random_tree(rng, dims, chi=chi)
+    H = random_sop(rng, dims, nterms=10)
+    st = generic_state(topo, rng)
+    plain(f"plain_random_{{seed}}", topo, H, st, 0.1, 2)
+    adjoint(f"adjoint_random_{{seed}}", topo, H, st, 0.1, rng.uniform(size=2), 0, rand_herm(rng, dims[0]), 1)
+def heff(name, topo, H, st):
+    A = api.httensor(topo, device=0); A.set(st)
+    integ = api.fixed_step_projector_splitting_integrator(A, H, krylov_dim=10, krylov_tolerance=1e-13)
+    integ.refresh_env(A)
+    orc = Oracle(topo, H, krylov_dim=10, krylov_tol=1e-13); orc.set_state(st); orc.refresh_env()
+    rng = np.random.default_rng(1)
+    worst = 0.0
+    for nd in range(topo.nnodes):
+        v = rng.normal(size=topo.node_shape(nd)) + 1j * rng.normal(size=topo.node_shape(nd))
+        ho = orc.heff(nd, v)
+        for got in (integ.heff(nd, v), integ.program_apply(nd, v)):
+            worst = max(worst, float(np.max(np.abs(got - ho)) / max(1.0, np.max(np.abs(ho)))))
+    out[name] = worst
+
+for seed in (310, 312, 338):
+    topo, H, st, dims = random_case(seed)
+    heff(f"plain_heff_{{seed}}", topo, H, st)
+    plain(f"plain_case_{{seed}}", topo, H, st, 0.1, 2)
+    adjoint(f"adjoint_case_{{seed}}", topo, H, st, 0.1, np.random.default_rng(seed).uniform(size=2), 0,
+            rand_herm(np.random.default_rng(seed), dims[0]), 1)
+print(json.dumps(out))
+"""
+
+
+def test_host_orchestration_matches_oracle():
+    lib = _build()
+    code = CHILD.format(root=ROOT, tests=os.path.join(ROOT, "tests"), lib=lib)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-3000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    for k, v in res.items():
+        if k.startswith("plain"):
+            assert v < 1e-11, (k, v)
+        else:
+            assert v["J"] < 1e-12, (k, v)
+            assert v["coeff"] < 1e-10 and v["ops"] < 1e-10 and v["state"] < 1e-10, (k, v)
+            assert v["final"] < 1e-11, (k, v)

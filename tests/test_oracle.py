@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 import scipy.linalg as sla
 
-from helpers import generic_state, random_sop, random_tree
+from helpers import generic_state, random_case, random_sop, random_tree
 from oracle.oracle import Oracle, qr
 from ttns_lib_gb300 import spin_boson as sb
 from ttns_lib_gb300.model import full_state
@@ -45,6 +45,20 @@ def test_random_tree_random_sop_matches_dense_expm(seed):
         ex = sla.expm(-1j * Hd * (k + 1) * 0.1) @ psi
         got = full_state(topo, orc.get_state())
         assert np.linalg.norm(got - ex) < 1e-10
+
+
+# random operator shapes, among them groups that mix terms acting below a node with terms
+# that are the identity there (at a leaf: 310; at a branch node: 312, 338)
+@pytest.mark.parametrize("seed", [300, 304, 310, 312, 320, 338])
+def test_random_operator_shapes_match_dense_expm(seed):
+    topo, H, st, _ = random_case(seed)
+    psi = full_state(topo, st)
+    orc = Oracle(topo, H, krylov_dim=10, krylov_tol=1e-12)
+    orc.set_state(st)
+    for k in range(3):
+        orc.step(0.1)
+        ex = sla.expm(-1j * H.dense() * (k + 1) * 0.1) @ psi
+        assert np.linalg.norm(full_state(topo, orc.get_state()) - ex) < 1e-10
 
 
 def test_uncoupled_spin_precesses():

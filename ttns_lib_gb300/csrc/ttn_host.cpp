@@ -235,7 +235,10 @@ static void compile_plan(const Tree& T, const Sop& H, std::vector<std::vector<Gr
       Group g;
       g.type = type;
       g.members = mem;
-      g.id_spf = Ls[mem[0]].empty();
+      // the identity below the node only if every member is: an M group may mix a term that
+      // acts below with one that does not (the latter contributes its coefficient times I)
+      g.id_spf = true;
+      for (int r : mem) g.id_spf = g.id_spf && Ls[r].empty();
       g.s = (type == G_1) ? H.coeff[mem[0]] : cd(1.0);
       for (int r : mem) gof[nd][r] = (int)G[nd].size();
       G[nd].push_back(std::move(g));
@@ -251,7 +254,11 @@ static void compile_plan(const Tree& T, const Sop& H, std::vector<std::vector<Gr
       std::map<std::vector<int>, std::vector<int>> keys;
       for (int r : g.members) {
         std::vector<int> key;
-        if (T.leaf(nd)) key.push_back(H.opidx[T.leaf_mode[nd]][r]);
+        // at a leaf the key is the term's operator there; a member that is the identity on
+        // the leaf (possible in an M group) has an empty key, i.e. a tuple without items
+        if (T.leaf(nd)) {
+          if (H.opidx[T.leaf_mode[nd]][r] >= 0) key.push_back(H.opidx[T.leaf_mode[nd]][r]);
+        }
         else
           for (int s = 0; s < (int)T.children[nd].size(); ++s) {
             int c = T.children[nd][s], cg = gof[c][r];
@@ -267,7 +274,9 @@ static void compile_plan(const Tree& T, const Sop& H, std::vector<std::vector<Gr
         const auto& mem = keys[key];
         SpfTuple t;
         bool carrying = false;
-        if (T.leaf(nd)) t.items.push_back({-1, key[0]});
+        if (T.leaf(nd)) {
+          if (!key.empty()) t.items.push_back({-1, key[0]});
+        }
         else
           for (size_t q = 0; q < key.size(); q += 2) {
             int c = T.children[nd][key[q]];
@@ -723,6 +732,10 @@ struct Integrator {
     zgemm(g, gws, gws_bytes, stream);
   }
 
+  // A chain applies its scalar with its last product; a tuple without items (terms that act
+  // as the identity below the node, next to terms that do not) carries it in the
+  // accumulation that follows instead.
+  static cd chain_scale(const SpfTuple& t) { return t.items.empty() ? t.a : cd(1.0); }
   const double2* apply_items(int nd, const std::vector<Item>& items, const double2* v, double2* b1, double2* b2,
                              cd alpha_last = 1.0) {
     const double2* cur = v;
@@ -828,8 +841,8 @@ struct Integrator {
           mode_apply(S, d, v, out, na, nb, g.s * t.a, !first);
         } else {
           const double2* X = apply_items(nd, t.items, v, w1, w2, t.a);
-          if (direct) mode_identity_axpy(X, out, sz, g.s, !first);
-          else mf_apply(X, g.mf_dev, r, sz / r, out, g.s, !first);
+          if (direct) mode_identity_axpy(X, out, sz, g.s * chain_scale(t), !first);
+          else mf_apply(X, g.mf_dev, r, sz / r, out, g.s * chain_scale(t), !first);
         }
       } else {
         // several tuples: sum into w3 then one mean-field product
@@ -846,7 +859,7 @@ struct Integrator {
               mode_apply(S, d, v, out, na, nb, g.s * t.a, !f2);
             } else {
               const double2* X = apply_items(nd, t.items, v, w1, w2, t.a);
-              mode_identity_axpy(X, out, sz, g.s, !f2);
+              mode_identity_axpy(X, out, sz, g.s * chain_scale(t), !f2);
             }
             f2 = false;
           }
@@ -863,7 +876,7 @@ struct Integrator {
               mode_apply(S, d, v, w3, na, nb, t.a, !f2);
             } else {
               const double2* X = apply_items(nd, t.items, v, w1, w2, t.a);
-              mode_identity_axpy(X, w3, sz, 1.0, !f2);
+              mode_identity_axpy(X, w3, sz, chain_scale(t), !f2);
             }
             f2 = false;
           }
@@ -972,8 +985,8 @@ struct Integrator {
           B.emit(mk(MV_MODE, 0, 1, S, na, d, nb, g.s * t.a, !first));
         } else {
           int X = emit_chain(B, nd, t.items, 0, t.a);
-          if (direct) B.emit(mk(MV_AXPY, X, 1, nullptr, sz, 0, 0, g.s, !first));
-          else B.emit(mk(MV_MF, X, 1, g.mf_dev, sz / r, r, 0, g.s, !first));
+          if (direct) B.emit(mk(MV_AXPY, X, 1, nullptr, sz, 0, 0, g.s * chain_scale(t), !first));
+          else B.emit(mk(MV_MF, X, 1, g.mf_dev, sz / r, r, 0, g.s * chain_scale(t), !first));
         }
       } else {
         bool f2 = true;
@@ -987,7 +1000,7 @@ struct Integrator {
             B.emit(mk(MV_MODE, 0, acc_buf, S, na, d, nb, sc, accum));
           } else {
             int X = emit_chain(B, nd, t.items, 0, t.a);
-            B.emit(mk(MV_AXPY, X, acc_buf, nullptr, sz, 0, 0, direct ? g.s : cd(1.0), accum));
+            B.emit(mk(MV_AXPY, X, acc_buf, nullptr, sz, 0, 0, (direct ? g.s : cd(1.0)) * chain_scale(t), accum));
           }
           f2 = false;
         }

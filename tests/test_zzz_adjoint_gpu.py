@@ -69,6 +69,7 @@ def test_device_adjoint_rejects_mixed_precision_and_used_integrators():
     with pytest.raises(api.TTNError):
         mixed.adjoint(A, 0.05, 1, [1.0], 0, sb.SZ)
     plain = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=8)
+    plain.dt = 0.05
     plain(A)
     with pytest.raises(api.TTNError):
         plain.adjoint(A, 0.05, 1, [1.0], 0, sb.SZ)

@@ -17,7 +17,7 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(_HERE, f) for f in ("ttn_oracle.cpp", "ttn_adjoint.hpp")]
+    srcs = [os.path.join(_HERE, f) for f in ("ttn_oracle.cpp", "ttn_adjoint.hpp", "ttn_expansion.hpp")]
     if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < max(os.path.getmtime(s) for s in srcs):
         subprocess.check_call(["make", "-s", "-C", _HERE, "liboracle.so"])
     return _LIB
@@ -62,6 +62,9 @@ def lib():
         L.orc_node_times.argtypes = [P, dp]
         L.orc_reset_node_times.argtypes = [P]
         L.orc_tql2.argtypes = [C.c_int, dp, dp, dp]
+        L.orc_set_expansion.argtypes = [P, ip, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_uint]
+        L.orc_get_hrank.argtypes = [P, ip]
+        L.orc_expand_prepare.argtypes = [P, C.c_double, ip]
         L.orc_adjoint.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_int, dp, C.c_int, dp, C.c_int, C.c_int,
                                   dp, dp, dp, dp]
         _lib = L
@@ -110,14 +113,41 @@ class Oracle:
 
     def set_state(self, tensors):
         flat = np.concatenate([np.asarray(t, dtype=np.complex128).ravel() for t in tensors])
-        assert flat.size == self.offsets[-1]
+        assert flat.size == self.current_topology().offsets()[-1]
         self._check(lib().orc_set_state(self.h, _dp(flat.view(np.float64))))
 
     def get_state(self):
-        flat = np.zeros(int(self.offsets[-1]), dtype=np.complex128)
+        topo = self.current_topology()
+        offs = topo.offsets()
+        flat = np.zeros(int(offs[-1]), dtype=np.complex128)
         self._check(lib().orc_get_state(self.h, _dp(flat.view(np.float64))))
-        return [flat[self.offsets[i]:self.offsets[i + 1]].reshape(self.topo.node_shape(i)).copy()
-                for i in range(self.topo.nnodes)]
+        return [flat[offs[i]:offs[i + 1]].reshape(topo.node_shape(i)).copy() for i in range(topo.nnodes)]
+
+    def hrank(self):
+        out = np.zeros(self.topo.nnodes, dtype=np.int32)
+        self._check(lib().orc_get_hrank(self.h, _ip(out)))
+        return out
+
+    def current_topology(self):
+        """The tree with its current bond dimensions (they grow under subspace expansion)."""
+        from ttns_lib_gb300.model import Topology
+        return Topology(self.topo.parent, self.hrank(), self.topo.leaf_mode, self.topo.leaf_dim)
+
+    def set_expansion(self, capacity, spawning_threshold: float = 1e-12, unoccupied_threshold: float = 1e-12,
+                      minimum_unoccupied: int = 0, neigenvalues: int = 2, only_when_no_unoccupied: bool = False,
+                      seed: int = 0):
+        """Enable subspace expansion (adaptive bond dimension) for the following steps;
+        ``capacity`` is the largest bond dimension above every node."""
+        cap = np.ascontiguousarray(capacity, dtype=np.int32)
+        assert cap.size == self.topo.nnodes
+        self._check(lib().orc_set_expansion(self.h, _ip(cap), spawning_threshold, unoccupied_threshold,
+                                            int(minimum_unoccupied), int(neigenvalues), int(only_when_no_unoccupied),
+                                            int(seed)))
+
+    def expand_prepare(self, dt: float) -> bool:
+        grew = C.c_int(0)
+        self._check(lib().orc_expand_prepare(self.h, dt, C.byref(grew)))
+        return bool(grew.value)
 
     def step(self, dt: float, coeff: complex = -1j):
         self._check(lib().orc_step(self.h, dt, coeff.real, coeff.imag))

@@ -46,6 +46,8 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <memory>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -595,6 +597,11 @@ struct Engine {
   // Called before every operation of a sweep (kind OP_*, node, auxiliary index) while
   // set; the adjoint sweep uses it to record the operations' inputs.
   std::function<void(int, int, int)> on_op;
+  // Subspace expansion hooks (ttn_expansion.hpp): called after the root-to-leaf
+  // decomposition towards a child in the forward half-sweep, and after a node's
+  // leaf-to-root decomposition in the backward half-sweep; `expanded` records growth.
+  std::function<bool(int)> expand_down, expand_up;
+  bool expanded = false;
   std::chrono::steady_clock::time_point tmark;
   void tick() { tmark = std::chrono::steady_clock::now(); }
   void tock(int id) {
@@ -960,6 +967,7 @@ struct Engine {
         if (t == 0 && id != 0) { apply_from_parent(id); chk("apply_from_parent", id); }
         if (!T.leaf(id)) {
           r2l(id, mode); chk("r2l", id);
+          if (expand_down) expanded = expand_down(T.children[id][mode]) || expanded;
           update_mf(T.children[id][mode]); chk("update_mf", id);
         }
       } else {
@@ -996,6 +1004,7 @@ struct Engine {
       } else {
         if (id != 0) {
           l2r(id);
+          if (expand_up) expanded = expand_up(id) || expanded;
           apply_to_parent(id);
           update_spf(id);
         }
@@ -1134,6 +1143,7 @@ struct Engine {
 };
 
 #include "ttn_adjoint.hpp"
+#include "ttn_expansion.hpp"
 
 }  // namespace orc
 
@@ -1141,6 +1151,7 @@ struct Engine {
 struct OrcHandle {
   orc::Engine E;
   std::string err;
+  std::unique_ptr<orc::Expander> X;  // subspace expansion, when enabled
 };
 
 #define ORC_TRY(h, ...)                                   \
@@ -1234,7 +1245,46 @@ int orc_set_threads(void* p, int n) {
 }
 int orc_step(void* p, double dt, double cre, double cim) {
   OrcHandle* h = (OrcHandle*)p;
-  ORC_TRY(h, { h->E.step(dt, cd(cre, cim)); })
+  ORC_TRY(h, {
+    if (h->X) h->X->step(dt, cd(cre, cim));
+    else h->E.step(dt, cd(cre, cim));
+  })
+}
+// Subspace expansion (ttn_expansion.hpp) for the following steps: bond capacities per node
+// (cap[0] ignored; >= the current hrank), the reference's spawning / unoccupied thresholds,
+// minimum number of unoccupied functions, eigenvalues per expansion, only-when-no-
+// unoccupied flag and the random generator's seed.
+int orc_set_expansion(void* p, const int* cap, double spawning, double unoccupied, int min_unocc, int neig, int only_when,
+                      unsigned seed) {
+  OrcHandle* h = (OrcHandle*)p;
+  ORC_TRY(h, {
+    orc::Engine& E = h->E;
+    ORC_REQUIRE(E.nsteps == 0, "subspace expansion must be set before the first step");
+    ORC_REQUIRE(neig >= 1 && min_unocc >= 0, "bad expansion parameters");
+    h->X.reset(new orc::Expander(E));
+    h->X->cap.assign(cap, cap + E.T.n);
+    for (int i = 1; i < E.T.n; ++i) ORC_REQUIRE(h->X->cap[i] >= E.T.hrank[i], "capacity below the current bond dimension");
+    h->X->spawning_threshold = spawning;
+    h->X->unoccupied_threshold = unoccupied;
+    h->X->minimum_unoccupied = min_unocc;
+    h->X->neigenvalues = neig;
+    h->X->only_when_no_unoccupied = only_when != 0;
+    h->X->rng.seed(seed);
+  })
+}
+// the current bond dimension above every node (hrank)
+int orc_get_hrank(void* p, int* out) {
+  OrcHandle* h = (OrcHandle*)p;
+  ORC_TRY(h, { for (int i = 0; i < h->E.T.n; ++i) out[i] = h->E.T.hrank[i]; })
+}
+// subspace expansion only (prepare_evolution without evolution); returns 1 if anything grew
+int orc_expand_prepare(void* p, double dt, int* grew) {
+  OrcHandle* h = (OrcHandle*)p;
+  ORC_TRY(h, {
+    ORC_REQUIRE(h->X != nullptr, "subspace expansion is not enabled");
+    h->E.dt = dt;
+    *grew = h->X->prepare() ? 1 : 0;
+  })
 }
 // One plain sweep at the given dt (no first-step sub-stepping); used for bounded timing.
 int orc_sweep(void* p, double dt, double cre, double cim) {

@@ -20,12 +20,12 @@ TOL = 1e-8
 
 
 def _compare(topo, H, st, dt, wt, mode, O, ckpt):
-    orc = Oracle(topo, H, krylov_dim=10, krylov_tol=1e-13)
+    orc = Oracle(topo, H, krylov_dim=10, krylov_tol=1e-12)
     orc.set_state(st)
     Jo, gco, gopo, gso = orc.adjoint(dt, len(wt), wt, mode, O, checkpoint_every=ckpt, state_cotangent=True)
     A = api.httensor(topo, device=0)
     A.set(st)
-    integ = api.fixed_step_projector_splitting_integrator(A, H, krylov_dim=10, krylov_tolerance=1e-13)
+    integ = api.fixed_step_projector_splitting_integrator(A, H, krylov_dim=10, krylov_tolerance=1e-12)
     Jd, gcd, gopd, gsd = integ.adjoint(A, dt, len(wt), wt, mode, O, checkpoint_every=ckpt, state_cotangent=True)
     assert abs(Jd - Jo) <= 1e-10 * max(1.0, abs(Jo))
     scale = max(np.max(np.abs(gco)), max(np.max(np.abs(g)) for g in gopo))
@@ -80,13 +80,13 @@ def test_device_adjoint_through_torch_matches_plain_path_differences():
     against central differences of J computed by the plain FP64 device path
     (ttn_integrator_step and <sz> after every step), within 1e-5 relative."""
     torch = pytest.importorskip("torch")
-    N, d, chi, dt, h = 3, 3, 3, 0.05, 1e-5
+    N, d, chi, dt, h = 3, 3, 3, 0.05, 1e-4
     w0, c0 = sb.ohmic_modes(N, 0.4, 5.0)
     rng = np.random.default_rng(21)
     topo = sb.build_from_modes(w0, c0, d, chi, 0.3, 1.0).topology
     st = generic_state(topo, rng)
     wt = rng.uniform(size=3)
-    f = api.torch_objective(api.spin_boson_adjoint(w0, d, chi, st, dt, wt, krylov_dim=10, krylov_tolerance=1e-14,
+    f = api.torch_objective(api.spin_boson_adjoint(w0, d, chi, st, dt, wt, krylov_dim=10, krylov_tolerance=1e-12,
                                                    checkpoint_every=2))
     theta = torch.tensor(np.concatenate([[0.3, 1.0], c0]), dtype=torch.float64, requires_grad=True)
     (grad,) = torch.autograd.grad(f(theta), theta)
@@ -95,7 +95,7 @@ def test_device_adjoint_through_torch_matches_plain_path_differences():
         m = sb.build_from_modes(w0, th[2:], d, chi, th[0], th[1])
         A = api.httensor(topo, device=0)
         A.set(st)
-        integ = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=10, krylov_tolerance=1e-14)
+        integ = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=10, krylov_tolerance=1e-12)
         integ.dt = dt
         J = 0.0
         for k in range(len(wt)):

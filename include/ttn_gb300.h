@@ -149,6 +149,24 @@ int ttn_expect_leaf(ttn_integrator* it, ttn_state* psi, int mode, const double* 
                     double* im);
 int ttn_norm2(ttn_integrator* it, ttn_state* psi, double* out);
 
+/* ---- subspace expansion ------------------------------------------------------------ */
+/* Adaptive bond dimension for the following steps, replacing
+ * subspace_expansion_projector_splitting_integrator
+ * (include/ttns_lib/integrators/projector_splitting_integrator.hpp:221-393; engine
+ * include/ttns_lib/tdvp_core/subspace_expansion_projector_splitting_engine.hpp:207-585):
+ * capacity[nnodes] is the largest bond dimension above every node (the httensor capacity;
+ * capacity[0] equals the root's rank), spawning_threshold / unoccupied_threshold /
+ * minimum_unoccupied / neigenvalues / only_when_no_unoccupied are the reference's
+ * parameters of the same names, seed starts the random generator of the one-site
+ * fallback.  psi is re-laid in slabs sized for the capacities and must be the state
+ * stepped afterwards; its bond dimensions (ttn_state_hrank) grow during the steps.  FP64
+ * integrators at step 0 only; TTN_EINVAL otherwise. */
+int ttn_integrator_set_expansion(ttn_integrator* it, ttn_state* psi, const int* capacity, double spawning_threshold,
+                                 double unoccupied_threshold, int minimum_unoccupied, int neigenvalues,
+                                 int only_when_no_unoccupied, unsigned seed);
+/* current bond dimension above every node (out[nnodes]) */
+int ttn_state_hrank(const ttn_state* s, int* out);
+
 /* ---- adjoint sweep ----------------------------------------------------------------- */
 /* Gradient of J = sum_k weights[k] Re <psi(t_k)| O_mode |psi(t_k)>, t_k the end of step k,
  * over nsteps integrator steps of dt from psi (the first step sub-stepped like

@@ -109,6 +109,49 @@ for seed in (310, 312, 338):
     plain(f"plain_case_{{seed}}", topo, H, st, 0.1, 2)
     adjoint(f"adjoint_case_{{seed}}", topo, H, st, 0.1, np.random.default_rng(seed).uniform(size=2), 0,
             rand_herm(np.random.default_rng(seed), dims[0]), 1)
+# subspace expansion: preparation (deterministic) equal to the oracle's, the random
+# fallback equal to the oracle's, and steps at full capacity following exact dynamics
+import scipy.linalg as sla
+from helpers import full_rank
+from ttns_lib_gb300.model import full_state, SOPOperator, Topology
+w0, c0 = sb.ohmic_modes(4, 0.5, 5.0)
+m2 = sb.build_from_modes(w0, c0, 3, 2, 0.3, 1.0)
+cap = full_rank(sb.build_from_modes(w0, c0, 3, 27, 0.3, 1.0).topology).hrank
+st = generic_state(m2.topology, np.random.default_rng(4))
+orc = Oracle(m2.topology, m2.sop, krylov_dim=10, krylov_tol=1e-12); orc.set_state(st)
+orc.set_expansion(cap, spawning_threshold=1e-7)
+orc.expand_prepare(0.05)
+A = api.httensor(m2.topology, device=0); A.set(st)
+integ = api.subspace_expansion_projector_splitting_integrator(A, m2.sop, cap, krylov_dim=10, spawning_threshold=1e-7)
+integ.dt = 0.05
+integ.prepare(A)
+out["expansion_prepare_ranks"] = float(np.max(np.abs(A.hrank() - orc.hrank())))
+out["expansion_prepare_tensors"] = float(max(np.max(np.abs(a - b)) for a, b in zip(A.get(), orc.get_state())))
+B = api.httensor(m2.topology, device=0); B.set(st)
+i2 = api.subspace_expansion_projector_splitting_integrator(B, m2.sop, cap, krylov_dim=10, spawning_threshold=1e-12)
+i2.dt = 0.05
+for _ in range(20):
+    i2(B)
+ex = sla.expm(-1j * m2.sop.dense() * 1.0) @ full_state(m2.topology, st)
+out["expansion_exact_dynamics"] = float(np.linalg.norm(full_state(B.current_topology(), B.get()) - ex))
+out["expansion_full_capacity"] = float(np.max(np.abs(B.hrank() - cap)))
+topo = Topology(np.array([-1, 0, 0, 0]), np.array([1, 3, 1, 3]), np.array([-1, 0, 1, 2]), np.array([0, 3, 3, 3]))
+rng = np.random.default_rng(2)
+H = SOPOperator(3, [3, 3, 3])
+for r in range(3):
+    a = rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3))
+    H.bind_dense(a + a.conj().T, [r], r)
+st = generic_state(topo, rng)
+orc = Oracle(topo, H, krylov_dim=8, krylov_tol=1e-12); orc.set_state(st)
+orc.set_expansion(np.array([1, 3, 3, 3]), spawning_threshold=1e-12, minimum_unoccupied=2, seed=5)
+C2 = api.httensor(topo, device=0); C2.set(st)
+i3 = api.subspace_expansion_projector_splitting_integrator(C2, H, np.array([1, 3, 3, 3]), krylov_dim=8,
+                                                           spawning_threshold=1e-12, minimum_unoccupied=2, seed=5)
+i3.dt = 0.05
+for _ in range(2):
+    i3(C2); orc.step(0.05)
+out["expansion_random_fallback"] = float(np.max(np.abs(full_state(C2.current_topology(), C2.get())
+                                                       - full_state(orc.current_topology(), orc.get_state()))))
 print(json.dumps(out))
 """
 
@@ -120,7 +163,11 @@ def test_host_orchestration_matches_oracle():
     assert r.returncode == 0, r.stderr[-3000:]
     res = json.loads(r.stdout.strip().splitlines()[-1])
     for k, v in res.items():
-        if k.startswith("plain"):
+        if k.startswith("expansion"):
+            # ranks equal and tensors after the deterministic preparation equal to rounding;
+            # at full capacity the expanding integrator follows exp(-iHt)
+            assert v < (1e-6 if k == "expansion_exact_dynamics" else 1e-11), (k, v)
+        elif k.startswith("plain"):
             assert v < 1e-11, (k, v)
         else:
             assert v["J"] < 1e-12, (k, v)

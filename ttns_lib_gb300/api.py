@@ -101,6 +101,8 @@ SIGNATURES = {
     "ttn_debug_qr": (_I, [_I, _I, _DP, _DP, _I]),
     "ttn_qr_noalloc": (_I, [_I, _I, _P, _P, _P, _I]),
     "ttn_bond_singular_values": (_I, [_P, _P, _I, _DP, C.POINTER(C.c_int)]),
+    "ttn_integrator_set_expansion": (_I, [_P, _P, _IP, _D, _D, _I, _I, _I, C.c_uint]),
+    "ttn_state_hrank": (_I, [_P, _IP]),
     "ttn_adjoint_grad": (_I, [_P, _P, _D, _D, _D, _I, _DP, _I, _DP, _I, _I, _DP, _DP, _DP, _DP]),
     "ttn_batch_step": (_I, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _I, _D, _D, _I, C.POINTER(C.c_int)]),
     "ttn_debug_tc_gemm": (_I, [_DP, _DP, _DP, _I, _I, _I]),
@@ -194,17 +196,28 @@ class httensor:
             lib().ttn_state_destroy(self.h)
             self.h = None
 
+    def hrank(self) -> np.ndarray:
+        """Current bond dimension above every node (grows under subspace expansion)."""
+        out = np.zeros(self.topo.nnodes, dtype=np.int32)
+        _check(lib().ttn_state_hrank(self.h, _ip(out)))
+        return out
+
+    def current_topology(self) -> Topology:
+        return Topology(self.topo.parent, self.hrank(), self.topo.leaf_mode, self.topo.leaf_dim)
+
     def set(self, tensors: Sequence[np.ndarray]):
+        topo = self.current_topology()
         flat = np.concatenate([_cplx(t).ravel() for t in tensors])
-        if flat.size != self.offsets[-1]:
+        if flat.size != topo.offsets()[-1]:
             raise ValueError("tensor sizes do not match the topology")
         _check(lib().ttn_state_upload(self.h, _dp(flat.view(np.float64))))
 
     def get(self) -> List[np.ndarray]:
-        flat = np.zeros(int(self.offsets[-1]), dtype=np.complex128)
+        topo = self.current_topology()
+        offs = topo.offsets()
+        flat = np.zeros(int(offs[-1]), dtype=np.complex128)
         _check(lib().ttn_state_download(self.h, _dp(flat.view(np.float64))))
-        return [flat[self.offsets[i]:self.offsets[i + 1]].reshape(self.topo.node_shape(i)).copy()
-                for i in range(self.topo.nnodes)]
+        return [flat[offs[i]:offs[i + 1]].reshape(topo.node_shape(i)).copy() for i in range(topo.nnodes)]
 
     def upload_from(self, buf: "PinnedBuffer"):
         _check(lib().ttn_state_upload(self.h, C.cast(buf.ptr, _DP)))
@@ -370,6 +383,18 @@ class fixed_step_projector_splitting_integrator:
     def mel(self) -> matrix_element:
         return self._mel
 
+    def set_expansion(self, A: httensor, capacity, spawning_threshold: float = 1e-12,
+                      unoccupied_threshold: float = 1e-12, minimum_unoccupied: int = 0, neigenvalues: int = 2,
+                      only_when_no_unoccupied: bool = False, seed: int = 0):
+        """Adaptive bond dimension for the following steps (subspace expansion); ``A`` is
+        re-laid for the capacities and must be the state stepped afterwards."""
+        cap = np.ascontiguousarray(capacity, dtype=np.int32)
+        if cap.size != self.topo.nnodes:
+            raise ValueError("one capacity per node")
+        _check(lib().ttn_integrator_set_expansion(self.h, A.h, _ip(cap), float(spawning_threshold),
+                                                  float(unoccupied_threshold), int(minimum_unoccupied),
+                                                  int(neigenvalues), int(only_when_no_unoccupied), int(seed)))
+
     def adjoint(self, A: httensor, dt: float, nsteps: int, weights, mode: int, op, checkpoint_every: int = 20,
                 coeff: complex = -1j, skip_prepare: bool = False, state_cotangent: bool = False):
         """J = sum_k weights[k] Re <op on mode>(end of step k) over ``nsteps`` steps of ``dt``
@@ -437,6 +462,22 @@ class fixed_step_projector_splitting_integrator:
         out = np.zeros((r, r), dtype=np.complex128)
         _check(lib().ttn_debug_get_env(self.h, node, group, 0 if which == "spf" else 1, _dp(out.view(np.float64))))
         return out
+
+
+class subspace_expansion_projector_splitting_integrator(fixed_step_projector_splitting_integrator):
+    """The one-site integrator with subspace expansion (adaptive bond dimension), named and
+    parameterised like the reference's subspace_expansion_projector_splitting_integrator
+    (include/ttns_lib/integrators/projector_splitting_integrator.hpp:221-393): bonds grow
+    up to ``capacity`` (one entry per node; the root's own rank does not grow)."""
+
+    def __init__(self, A: httensor, H: SOPOperator, capacity, krylov_dim: int = 4, krylov_tolerance: float = 1e-12,
+                 spawning_threshold: float = 1e-12, unoccupied_threshold: float = 1e-12, minimum_unoccupied: int = 0,
+                 neigenvalues: int = 2, only_when_no_unoccupied: bool = False, seed: int = 0,
+                 device: Optional[int] = None):
+        super().__init__(A, H, krylov_dim=krylov_dim, krylov_tolerance=krylov_tolerance, precision=PREC_FP64,
+                         device=device)
+        self.set_expansion(A, capacity, spawning_threshold, unoccupied_threshold, minimum_unoccupied, neigenvalues,
+                           only_when_no_unoccupied, seed)
 
 
 def torch_objective(evaluate):

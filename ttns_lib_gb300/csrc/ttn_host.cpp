@@ -26,6 +26,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <memory>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -62,6 +63,14 @@ struct Tree {
 
   long long size(int i) const { return dimen[i] * hrank[i]; }
   bool leaf(int i) const { return children[i].empty(); }
+  // the bond above node c takes dimension r (subspace expansion)
+  void set_bond(int c, int r) {
+    hrank[c] = r;
+    const int p = parent[c];
+    dims[p][slot[c]] = r;
+    dimen[p] = 1;
+    for (int d : dims[p]) dimen[p] *= d;
+  }
 
   void build(int nn, const int* par, const int* hr, const int* lm, const int* ld) {
     TTN_REQUIRE(nn >= 1 && par && hr && lm && ld, TTN_EINVAL, "tree arrays must be non-null");
@@ -467,6 +476,14 @@ struct Integrator {
   // called before every operation of a sweep (OP_*, node, auxiliary index) while set: the
   // adjoint sweep records the operations' inputs through it
   std::function<void(int, int, int)> on_op;
+  // subspace expansion (ttn_expansion.hpp): bond capacities and the tree at capacity, which
+  // sizes every buffer; the expansion calls inside the half-sweeps and the step that
+  // replaces step() while expansion is on
+  std::vector<int> cap;
+  Tree Tsz;
+  std::function<bool(ttn_state*, int)> expand_down_fn, expand_up_fn;
+  std::function<void(ttn_state*, double, cd)> expanding_step;
+  bool expanded = false;
 
   ~Integrator() {
     if (ev0) cudaEventDestroy(ev0);
@@ -500,10 +517,20 @@ struct Integrator {
           o += align256(M.size() * sizeof(double2));
         }
     }
+    allocate_sized();
+    finish_setup();
+  }
+
+  // the tree that sizes every buffer: the capacities when bonds may grow, else the tree
+  const Tree& sizing() const { return cap.empty() ? T : Tsz; }
+
+  // environment, gauge-factor, observable and work buffers, sized for sizing()
+  void allocate_sized() {
+    const Tree& Z = sizing();
     // environments: one r x r matrix per non-identity spf / mf
     size_t eb = 0;
     for (int i = 0; i < T.n; ++i) {
-      size_t rr = (size_t)T.hrank[i] * T.hrank[i] * sizeof(double2);
+      size_t rr = (size_t)Z.hrank[i] * Z.hrank[i] * sizeof(double2);
       for (auto& g : G[i]) eb += (g.id_spf ? 0 : align256(rr)) + (g.id_mf ? 0 : align256(rr));
     }
     env_buf.alloc(eb);
@@ -512,7 +539,7 @@ struct Integrator {
       char* base = env_buf.as<char>();
       size_t o = 0;
       for (int i = 0; i < T.n; ++i) {
-        size_t rr = (size_t)T.hrank[i] * T.hrank[i] * sizeof(double2);
+        size_t rr = (size_t)Z.hrank[i] * Z.hrank[i] * sizeof(double2);
         for (auto& g : G[i]) {
           if (!g.id_spf) { g.spf_dev = (double2*)(base + o); o += align256(rr); }
           if (!g.id_mf) {
@@ -530,10 +557,10 @@ struct Integrator {
     // R matrices and observable scratch
     size_t rb = 0, mb = 0;
     for (int i = 0; i < T.n; ++i) {
-      long long rmx = T.hrank[i];
-      for (int d : T.dims[i]) rmx = std::max<long long>(rmx, d);
+      long long rmx = Z.hrank[i];
+      for (int d : Z.dims[i]) rmx = std::max<long long>(rmx, d);
       rb += align256((size_t)rmx * rmx * sizeof(double2));
-      mb += align256((size_t)T.hrank[i] * T.hrank[i] * sizeof(double2));
+      mb += align256((size_t)Z.hrank[i] * Z.hrank[i] * sizeof(double2));
     }
     r_buf.alloc(rb);
     mel_buf.alloc(mb);
@@ -542,25 +569,25 @@ struct Integrator {
     {
       size_t o = 0, o2 = 0;
       for (int i = 0; i < T.n; ++i) {
-        long long rmx = T.hrank[i];
-        for (int d : T.dims[i]) rmx = std::max<long long>(rmx, d);
+        long long rmx = Z.hrank[i];
+        for (int d : Z.dims[i]) rmx = std::max<long long>(rmx, d);
         rmat[i] = (double2*)(r_buf.as<char>() + o);
         o += align256((size_t)rmx * rmx * sizeof(double2));
         mel[i] = (double2*)(mel_buf.as<char>() + o2);
-        o2 += align256((size_t)T.hrank[i] * T.hrank[i] * sizeof(double2));
+        o2 += align256((size_t)Z.hrank[i] * Z.hrank[i] * sizeof(double2));
       }
     }
     // work space
     maxsize = 0;
-    for (int i = 0; i < T.n; ++i) maxsize = std::max(maxsize, T.size(i));
+    for (int i = 0; i < T.n; ++i) maxsize = std::max(maxsize, Z.size(i));
     ldv = (long long)(align256((size_t)maxsize * sizeof(double2)) / sizeof(double2));
     size_t gmax = 0;
     for (int i = 0; i < T.n; ++i) {
-      int r = T.hrank[i];
-      gmax = std::max(gmax, zgemm_split_workspace_bytes(r, r, (int)T.dimen[i]));
-      for (int m = 0; m < T.nmodes[i]; ++m) {
-        int d = T.dims[i][m];
-        gmax = std::max(gmax, zgemm_split_workspace_bytes(d, d, (int)(T.size(i) / d)));
+      int r = Z.hrank[i];
+      gmax = std::max(gmax, zgemm_split_workspace_bytes(r, r, (int)Z.dimen[i]));
+      for (int m = 0; m < Z.nmodes[i]; ++m) {
+        int d = Z.dims[i][m];
+        gmax = std::max(gmax, zgemm_split_workspace_bytes(d, d, (int)(Z.size(i) / d)));
       }
     }
     gws_bytes = align256(gmax + 16);
@@ -587,6 +614,10 @@ struct Integrator {
       qtau = take(kQrMaxCols * sizeof(double2));
       scal = take(64 * sizeof(double2));
     }
+  }
+
+  // control block, events, cooperative-kernel state and the term programs
+  void finish_setup() {
     ctl_buf.alloc(align256(sizeof(KrylovCtl)) + 512);
     ctl = ctl_buf.as<KrylovCtl>();
     status = (int*)(ctl_buf.as<char>() + align256(sizeof(KrylovCtl)));
@@ -1191,6 +1222,7 @@ struct Integrator {
         if (t == 0 && id != 0) apply_from_parent(id, A);
         if (!T.leaf(id)) {
           r2l(id, t, A);
+          if (expand_down_fn) expanded = expand_down_fn(S, T.children[id][t]) || expanded;
           update_mf(T.children[id][t], A);
         }
       } else {
@@ -1225,6 +1257,7 @@ struct Integrator {
         }
       } else if (id != 0) {
         l2r(id, A);
+        if (expand_up_fn) expanded = expand_up_fn(S, id) || expanded;
         apply_to_parent(id, S->node(T.parent[id]), T.parent[id]);
         update_spf(id, A);
       }
@@ -1242,6 +1275,11 @@ struct Integrator {
     backward(S, false);
   }
   void step(ttn_state* S, double step_dt, cd cf) {
+    if (expanding_step) {
+      expanding_step(S, step_dt, cf);
+      finish_check(S);
+      return;
+    }
     coeff = cf;
     if (nsteps == 0) {
       double tevolve = 0.0, sdt = step_dt / 1e5;
@@ -1391,6 +1429,7 @@ struct Integrator {
 };
 
 #include "ttn_adjoint.hpp"
+#include "ttn_expansion.hpp"
 
 static void check_same_tree(const Tree& a, const Tree& b) {
   TTN_REQUIRE(a.parent == b.parent && a.hrank == b.hrank && a.leaf_dim == b.leaf_dim && a.leaf_mode == b.leaf_mode,
@@ -1401,6 +1440,7 @@ static void check_same_tree(const Tree& a, const Tree& b) {
 
 struct ttn_integrator {
   ttn::Integrator I;
+  std::unique_ptr<ttn::DevExpander> X;  // subspace expansion, when enabled
 };
 
 // ====================================================================== C-ABI
@@ -1802,6 +1842,7 @@ int ttn_adjoint_grad(ttn_integrator* it, ttn_state* psi, double dt, double coeff
   TTN_REQUIRE(mode >= 0 && mode < I.H.nmodes, TTN_EINVAL, "mode out of range");
   TTN_REQUIRE(!I.mixed, TTN_EINVAL, "the adjoint sweep needs an FP64 integrator (TTN_PREC_FP64)");
   TTN_REQUIRE(I.nsteps == 0, TTN_EINVAL, "the adjoint sweep starts from step 0 (a fresh or reset integrator)");
+  TTN_REQUIRE(!it->X, TTN_EINVAL, "the adjoint sweep needs fixed bond dimensions (no subspace expansion)");
   for (int k = 0; k < nsteps; ++k) TTN_REQUIRE(std::isfinite(weights[k]), TTN_EINVAL, "non-finite weight");
   CK(cudaSetDevice(I.device));
   const int d = I.H.mode_dim[mode];
@@ -1838,6 +1879,65 @@ int ttn_adjoint_grad(ttn_integrator* it, ttn_state* psi, double dt, double coeff
   }
   TTN_API_END
 }
+int ttn_integrator_set_expansion(ttn_integrator* it, ttn_state* psi, const int* capacity, double spawning_threshold,
+                                 double unoccupied_threshold, int minimum_unoccupied, int neigenvalues,
+                                 int only_when_no_unoccupied, unsigned seed) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi && capacity, TTN_EINVAL, "null argument");
+  ttn::check_same_tree(it->I.T, psi->T);
+  ttn::Integrator& I = it->I;
+  TTN_REQUIRE(I.nsteps == 0, TTN_EINVAL, "subspace expansion must be enabled before the first step");
+  TTN_REQUIRE(!I.mixed, TTN_EINVAL, "subspace expansion needs an FP64 integrator (TTN_PREC_FP64)");
+  TTN_REQUIRE(!it->X, TTN_EINVAL, "subspace expansion is already enabled");
+  TTN_REQUIRE(neigenvalues >= 1 && minimum_unoccupied >= 0, TTN_EINVAL, "bad expansion parameters");
+  TTN_REQUIRE(capacity[0] == I.T.hrank[0], TTN_EINVAL, "the root's rank does not grow (capacity[0] must equal it)");
+  for (int i = 1; i < I.T.n; ++i)
+    TTN_REQUIRE(capacity[i] >= I.T.hrank[i], TTN_EINVAL, "capacity below the current bond dimension");
+  CK(cudaSetDevice(I.device));
+  ttn::Tree Z;
+  Z.build(I.T.n, I.T.parent.data(), capacity, I.T.leaf_mode.data(), I.T.leaf_dim.data());
+  I.cap.assign(capacity, capacity + I.T.n);
+  I.Tsz = Z;
+  I.allocate_sized();
+  I.compile_programs();
+  // the state in slabs sized for the capacities (the tensors at the start of each slab)
+  {
+    std::vector<size_t> off(Z.n + 1);
+    size_t o = 0;
+    for (int i = 0; i < Z.n; ++i) {
+      off[i] = o;
+      o += ttn::align256((size_t)Z.size(i) * sizeof(double2)) / sizeof(double2);
+    }
+    off[Z.n] = o;
+    ttn::DevBuf na;
+    na.alloc(o * sizeof(double2));
+    CK(cudaMemsetAsync(na.p, 0, na.bytes, I.stream));
+    for (int i = 0; i < Z.n; ++i)
+      CK(cudaMemcpyAsync(na.as<double2>() + off[i], psi->node(i), (size_t)psi->T.size(i) * sizeof(double2),
+                         cudaMemcpyDeviceToDevice, I.stream));
+    CK(cudaStreamSynchronize(I.stream));
+    std::swap(psi->arena.p, na.p);
+    std::swap(psi->arena.bytes, na.bytes);
+    psi->off = off;
+  }
+  it->X.reset(new ttn::DevExpander(I));
+  ttn::DevExpander* X = it->X.get();
+  X->state = psi;
+  X->spawning_threshold = spawning_threshold;
+  X->unoccupied_threshold = unoccupied_threshold;
+  X->minimum_unoccupied = minimum_unoccupied;
+  X->neigenvalues = neigenvalues;
+  X->only_when_no_unoccupied = only_when_no_unoccupied != 0;
+  X->rng.seed(seed);
+  I.expanding_step = [X](ttn_state* S, double dt, ttn::cd cf) { X->step(S, dt, cf); };
+  TTN_API_END
+}
+int ttn_state_hrank(const ttn_state* s, int* out) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(s && out, TTN_EINVAL, "null argument");
+  for (int i = 0; i < s->T.n; ++i) out[i] = s->T.hrank[i];
+  TTN_API_END
+}
 int ttn_norm2(ttn_integrator* it, ttn_state* psi, double* out) {
   double re = 0, im = 0;
   int rc = ttn_expect_leaf(it, psi, 0, nullptr, &re, &im);
@@ -1850,7 +1950,16 @@ int ttn_integrator_prepare(ttn_integrator* it, ttn_state* psi) {
   TTN_REQUIRE(it && psi, TTN_EINVAL, "null argument");
   ttn::check_same_tree(it->I.T, psi->T);
   CK(cudaSetDevice(it->I.device));
-  it->I.prepare_only(psi);
+  if (it->X) {
+    // prepare_evolution with subspace expansion: the expansion half-sweeps use dt
+    TTN_REQUIRE(psi == it->X->state, TTN_EINVAL, "with subspace expansion, prepare the state given to ttn_integrator_set_expansion");
+    TTN_REQUIRE(it->I.dt > 0.0, TTN_EINVAL, "set dt before preparing an expanding integrator");
+    it->X->prepare(psi);
+    it->I.nsteps = std::max<long long>(it->I.nsteps, 1);
+    it->I.finish_check(psi);
+  } else {
+    it->I.prepare_only(psi);
+  }
   TTN_API_END
 }
 int ttn_integrator_flops(const ttn_integrator* it, double* out) {

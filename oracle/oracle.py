@@ -64,6 +64,7 @@ def lib():
         L.orc_tql2.argtypes = [C.c_int, dp, dp, dp]
         L.orc_set_expansion.argtypes = [P, ip, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_uint]
         L.orc_get_hrank.argtypes = [P, ip]
+        L.orc_top_eig.argtypes = [C.c_int, C.c_int, dp, dp, dp]
         L.orc_expand_prepare.argtypes = [P, C.c_double, ip]
         L.orc_adjoint.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_int, dp, C.c_int, dp, C.c_int, C.c_int,
                                   dp, dp, dp, dp]
@@ -255,3 +256,14 @@ def qr(a):
     rc = lib().orc_qr(m, n, _dp(a.view(np.float64)), _dp(r.view(np.float64)))
     assert rc == 0
     return a, r
+
+
+def top_eig(G, k: int):
+    """The k largest eigenpairs of a Hermitian matrix as the subspace expansion computes them."""
+    G = np.ascontiguousarray(G, dtype=np.complex128)
+    g = G.shape[0]
+    vals = np.zeros(k)
+    vecs = np.zeros((k, g), dtype=np.complex128)
+    n = lib().orc_top_eig(g, k, _dp(G.view(np.float64)), _dp(vals), _dp(vecs.view(np.float64)))
+    assert n >= 0
+    return vals[:n], vecs[:n]

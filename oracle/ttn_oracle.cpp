@@ -1272,6 +1272,22 @@ int orc_set_expansion(void* p, const int* cap, double spawning, double unoccupie
     h->X->rng.seed(seed);
   })
 }
+// the k largest eigenpairs of a Hermitian g x g matrix (interleaved, row-major) as the
+// subspace expansion computes them (dense Jacobi up to g = 96, Lanczos above)
+int orc_top_eig(int g, int k, const double* G, double* vals, double* vecs) {
+  try {
+    std::vector<cd> A((size_t)g * g);
+    for (size_t i = 0; i < A.size(); ++i) A[i] = cd(G[2 * i], G[2 * i + 1]);
+    std::vector<double> w;
+    std::vector<std::vector<cd>> V;
+    orc::Expander::top_eig(A, (size_t)g, k, w, V);
+    for (size_t j = 0; j < w.size(); ++j) {
+      vals[j] = w[j];
+      for (int i = 0; i < g; ++i) { vecs[2 * (j * g + i)] = V[j][i].real(); vecs[2 * (j * g + i) + 1] = V[j][i].imag(); }
+    }
+    return (int)w.size();
+  } catch (...) { return -1; }
+}
 // the current bond dimension above every node (hrank)
 int orc_get_hrank(void* p, int* out) {
   OrcHandle* h = (OrcHandle*)p;

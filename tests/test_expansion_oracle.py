@@ -116,3 +116,21 @@ def test_random_fallback_adds_orthonormal_unoccupied_functions():
     assert orc.hrank()[2] == 3
     assert np.linalg.norm(full_state(orc.current_topology(), orc.get_state()) - psi) < 1e-13
     assert _isometries(orc) < 1e-13
+
+
+@pytest.mark.parametrize("g", [40, 150, 300])
+def test_dominant_eigenpairs_dense_and_lanczos(g):
+    """The top eigenpairs used to pick expansion directions: dense Jacobi for small Gram
+    matrices, Lanczos for large ones (g > 96), both against numpy."""
+    from oracle.oracle import top_eig
+    rng = np.random.default_rng(g)
+    M = rng.normal(size=(g, 60)) + 1j * rng.normal(size=(g, 60))
+    M[:, 0] *= 20.0
+    M[:, 1] *= 10.0
+    G = M @ M.conj().T
+    vals, vecs = top_eig(G, 2)
+    ref_w, ref_v = np.linalg.eigh(G)
+    assert np.allclose(vals, ref_w[::-1][:2], rtol=1e-10)
+    for j in range(2):
+        r = ref_v[:, -1 - j]
+        assert abs(abs(np.vdot(r, vecs[j])) - 1.0) < 1e-8

@@ -190,6 +190,69 @@ struct DevExpander {
     return down(M, (size_t)(mC * outer));
   }
 
+  // the k largest eigenpairs of a Hermitian g x g matrix G: a dense Jacobi solve up to
+  // g = 96, above that Lanczos (at most 48 steps, full re-orthogonalisation, twice) from a
+  // fixed start vector with the Ritz pairs of the tridiagonal
+  static void top_eig(const std::vector<cd>& G, size_t g, int k, std::vector<double>& vals,
+                      std::vector<std::vector<cd>>& vecs) {
+    vals.clear();
+    vecs.clear();
+    if (g <= 96) {
+      std::vector<double> w;
+      std::vector<cd> Z;
+      herm_eig_host(G, (int)g, w, Z);
+      for (int j = 0; j < std::min<int>(k, (int)g); ++j) {
+        vals.push_back(w[j]);
+        std::vector<cd> z(g);
+        for (size_t i = 0; i < g; ++i) z[i] = Z[i * g + j];
+        vecs.push_back(z);
+      }
+      return;
+    }
+    const int m = (int)std::min<size_t>(g, 48);
+    std::vector<std::vector<cd>> Q;
+    std::vector<double> al, be;
+    std::vector<cd> q(g), w(g);
+    double nq = 0.0;
+    for (size_t i = 0; i < g; ++i) { q[i] = 1.0 + 0.5 * std::sin((double)(i + 1)); nq += std::norm(q[i]); }
+    for (auto& z : q) z /= std::sqrt(nq);
+    for (int j = 0; j < m; ++j) {
+      Q.push_back(q);
+      for (size_t i = 0; i < g; ++i) { cd t = 0.0; for (size_t c = 0; c < g; ++c) t += G[i * g + c] * q[c]; w[i] = t; }
+      double a = 0.0;
+      for (size_t i = 0; i < g; ++i) a += (std::conj(q[i]) * w[i]).real();
+      al.push_back(a);
+      for (int pass = 0; pass < 2; ++pass)
+        for (const auto& u : Q) {
+          cd h = 0.0;
+          for (size_t i = 0; i < g; ++i) h += std::conj(u[i]) * w[i];
+          for (size_t i = 0; i < g; ++i) w[i] -= h * u[i];
+        }
+      double b = 0.0;
+      for (auto& z : w) b += std::norm(z);
+      b = std::sqrt(b);
+      if (j + 1 == m || b <= 1e-14 * (std::fabs(a) + (be.empty() ? 0.0 : be.back()) + 1e-300)) break;
+      be.push_back(b);
+      for (size_t i = 0; i < g; ++i) q[i] = w[i] / b;
+    }
+    const int mm = (int)al.size();
+    std::vector<cd> Tm((size_t)mm * mm, 0.0);
+    for (int i = 0; i < mm; ++i) {
+      Tm[(size_t)i * mm + i] = al[i];
+      if (i + 1 < mm) { Tm[(size_t)i * mm + i + 1] = be[i]; Tm[(size_t)(i + 1) * mm + i] = be[i]; }
+    }
+    std::vector<double> tw;
+    std::vector<cd> Y;
+    herm_eig_host(Tm, mm, tw, Y);
+    for (int j = 0; j < std::min(k, mm); ++j) {
+      vals.push_back(tw[j]);
+      std::vector<cd> z(g, 0.0);
+      for (int i = 0; i < mm; ++i)
+        for (size_t r = 0; r < g; ++r) z[r] += Y[(size_t)i * mm + j] * Q[i][r];
+      vecs.push_back(z);
+    }
+  }
+
   // dominant singular values and (right or left) vectors of M (m x n), at most k
   static void dominant(const std::vector<cd>& M, size_t m, size_t n, int k, bool right, std::vector<double>& sv,
                        std::vector<std::vector<cd>>& vecs) {
@@ -204,15 +267,14 @@ struct DevExpander {
         G[i * g + j] = s;
       }
     std::vector<double> w;
-    std::vector<cd> Z;
-    herm_eig_host(G, (int)g, w, Z);
+    std::vector<std::vector<cd>> Zv;
+    top_eig(G, g, k, w, Zv);
     sv.clear();
     vecs.clear();
-    for (int j = 0; j < std::min<int>(k, (int)g); ++j) {
+    for (int j = 0; j < (int)w.size(); ++j) {
       const double s2 = w[j];
       sv.push_back(s2 > 0.0 ? std::sqrt(s2) : 0.0);
-      std::vector<cd> z(g);
-      for (size_t i = 0; i < g; ++i) z[i] = Z[i * g + j];
+      const std::vector<cd>& z = Zv[j];
       if (right == !small_left) { vecs.push_back(z); continue; }
       const double s = sv.back();
       std::vector<cd> o(right ? n : m, 0.0);

@@ -168,6 +168,17 @@ struct DevAdjoint {
     CK(cudaStreamSynchronize(st));
     keep.clear();
     small_used = 0;
+    herm_cache.clear();
+  }
+  // S^H of a device matrix that stays unchanged until the next reset() (environments
+  // restored for one reverse operation, operators), uploaded once per reset
+  std::map<const double2*, double2*> herm_cache;
+  double2* herm_of(const double2* S, int d) {
+    auto it = herm_cache.find(S);
+    if (it != herm_cache.end()) return it->second;
+    double2* h = up(hmat(down(S, (size_t)d * d), d));
+    herm_cache[S] = h;
+    return h;
   }
   double2* small_out(size_t n) {
     const size_t need = (n + 15) / 16 * 16;
@@ -329,7 +340,7 @@ struct DevAdjoint {
       double2* t = small_out(dd);
       I.mode_contract(chain_slot(k), g, l.na, l.d, l.nb, t, 1.0, false);
       add_transposed(down(t, dd), l.d, l.Sb);
-      double2* SH = up(hmat(down(l.S, dd), l.d));
+      double2* SH = herm_of(l.S, l.d);
       I.mode_apply(SH, l.d, g, v[V_T1], l.na, l.nb, 1.0, false, false);
       copy(g, v[V_T1], n);
     }
@@ -420,7 +431,7 @@ struct DevAdjoint {
       double2* t = small_out((size_t)r * r);
       I.adj_mul(X, g, nx, r, t, 1.0, false);
       add_transposed(down(t, (size_t)r * r), r, mb[nd][gi].data(), std::conj(G.s));
-      double2* MH = up(hmat(down(M, (size_t)r * r), r));
+      double2* MH = herm_of(M, r);
       I.mf_apply(g, MH, r, nx, v[V_XB], std::conj(G.s), false, false);
     }
     if (G.type == G_1) gc[G.members[0]] += sig.real();

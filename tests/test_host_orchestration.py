@@ -152,6 +152,25 @@ for _ in range(2):
     i3(C2); orc.step(0.05)
 out["expansion_random_fallback"] = float(np.max(np.abs(full_state(C2.current_topology(), C2.get())
                                                        - full_state(orc.current_topology(), orc.get_state()))))
+# Gram matrices above 96 (formed by one GEMM, Lanczos eigenpairs): bond dimensions equal to
+# the oracle's, the state unchanged, every non-root node an isometry (the directions chosen
+# inside near-degenerate singular-value clusters may differ between the two at rounding)
+topo = Topology(np.array([-1, 0, 1, 1, 0, 0]), np.array([1, 4, 12, 12, 12, 12]), np.array([-1, -1, 0, 1, 2, 3]),
+                np.array([0, 0, 12, 12, 12, 12]))
+rng = np.random.default_rng(9)
+H = random_sop(rng, [12] * 4, nterms=8)
+st = generic_state(topo, rng)
+capb = np.array([1, 40, 12, 12, 12, 12])
+orc = Oracle(topo, H, krylov_dim=10, krylov_tol=1e-12); orc.set_state(st)
+orc.set_expansion(capb, spawning_threshold=1e-7)
+orc.expand_prepare(0.05)
+D = api.httensor(topo, device=0); D.set(st)
+i4 = api.subspace_expansion_projector_splitting_integrator(D, H, capb, krylov_dim=10, spawning_threshold=1e-7)
+i4.dt = 0.05
+i4.prepare(D)
+out["expansion_large_gram_ranks"] = float(np.max(np.abs(D.hrank() - orc.hrank())))
+out["expansion_large_gram_state"] = float(np.linalg.norm(full_state(D.current_topology(), D.get()) - full_state(topo, st)))
+out["expansion_large_gram_isometries"] = float(max(np.max(np.abs(a.conj().T @ a - np.eye(a.shape[1]))) for a in D.get()[1:]))
 print(json.dumps(out))
 """
 

@@ -254,18 +254,53 @@ struct DevExpander {
   }
 
   // dominant singular values and (right or left) vectors of M (m x n), at most k
-  static void dominant(const std::vector<cd>& M, size_t m, size_t n, int k, bool right, std::vector<double>& sv,
-                       std::vector<std::vector<cd>>& vecs) {
+  // the Gram matrix of the smaller side of M (still in m_buf on the device): M M^H when
+  // m <= n, else M^H M, by one GEMM, then to the host
+  std::vector<cd> gram_dev(size_t m, size_t n) {
     const bool small_left = m <= n;
     const size_t g = small_left ? m : n;
-    std::vector<cd> G(g * g, 0.0);
-    for (size_t i = 0; i < g; ++i)
-      for (size_t j = 0; j < g; ++j) {
-        cd s = 0.0;
-        if (small_left) for (size_t c = 0; c < n; ++c) s += M[i * n + c] * std::conj(M[j * n + c]);
-        else for (size_t rr = 0; rr < m; ++rr) s += std::conj(M[rr * n + i]) * M[rr * n + j];
-        G[i * g + j] = s;
-      }
+    DevBuf gb;
+    gb.alloc(g * g * sizeof(double2));
+    const double2* M = m_buf.as<double2>();
+    ZGemm z{};
+    z.M = (int)g; z.N = (int)g;
+    if (small_left) {
+      z.K = (int)n;
+      z.A = op_rowmajor(M, (long long)n);  // A(i,c) = M(i,c)
+      z.B = op_rowmajor(M, (long long)n);  // B(c,j) = conj M(j,c)
+      z.B.cj = 1;
+    } else {
+      z.K = (int)m;
+      z.A = op_colk(M, (long long)n, 1);   // A(i,r) = conj M(r,i)
+      z.A.cj = 1;
+      z.B = op_colk(M, (long long)n, 1);   // B(r,j) = M(r,j)
+    }
+    z.C = gb.as<double2>(); z.ci = (long long)g; z.cj = 1;
+    z.batch = 1;
+    z.alpha = make_double2(1.0, 0.0);
+    z.beta = make_double2(0.0, 0.0);
+    zgemm(z, I.gws, I.gws_bytes, I.stream);
+    return down(gb.as<double2>(), g * g);
+  }
+
+  // dominant singular values and (right or left) vectors of M (m x n), at most k; Gpre: the
+  // Gram matrix of the smaller side when already formed
+  static void dominant(const std::vector<cd>& M, size_t m, size_t n, int k, bool right, std::vector<double>& sv,
+                       std::vector<std::vector<cd>>& vecs, const std::vector<cd>* Gpre = nullptr) {
+    const bool small_left = m <= n;
+    const size_t g = small_left ? m : n;
+    std::vector<cd> G;
+    if (Gpre) G = *Gpre;
+    else {
+      G.assign(g * g, 0.0);
+      for (size_t i = 0; i < g; ++i)
+        for (size_t j = 0; j < g; ++j) {
+          cd s = 0.0;
+          if (small_left) for (size_t c = 0; c < n; ++c) s += M[i * n + c] * std::conj(M[j * n + c]);
+          else for (size_t rr = 0; rr < m; ++rr) s += std::conj(M[rr * n + i]) * M[rr * n + j];
+          G[i * g + j] = s;
+        }
+    }
     std::vector<double> w;
     std::vector<std::vector<cd>> Zv;
     top_eig(G, g, k, w, Zv);
@@ -388,7 +423,10 @@ struct DevExpander {
       const std::vector<cd> M = two_site_matrix(S, C, I.rmat[P]);
       std::vector<double> sv;
       std::vector<std::vector<cd>> V;
-      dominant(M, (size_t)T.dimen[C], (size_t)outer, neigenvalues, true, sv, V);
+      const size_t mm = (size_t)T.dimen[C], nn = (size_t)outer;
+      std::vector<cd> G;
+      if (std::min(mm, nn) > 96) G = gram_dev(mm, nn);
+      dominant(M, mm, nn, neigenvalues, true, sv, V, G.empty() ? nullptr : &G);
       for (double s : sv)
         if (s > 0.0 && std::isfinite(s) && s * I.dt / 2.0 > spawning_threshold) ++nadd;
       nadd = std::min(nadd, max_add);
@@ -432,7 +470,10 @@ struct DevExpander {
       const std::vector<cd> M = two_site_matrix(S, C, I.rmat[C]);
       std::vector<double> sv;
       std::vector<std::vector<cd>> U;
-      dominant(M, (size_t)mC, (size_t)(pre * post), neigenvalues, false, sv, U);
+      const size_t mm = (size_t)mC, nn = (size_t)(pre * post);
+      std::vector<cd> G;
+      if (std::min(mm, nn) > 96) G = gram_dev(mm, nn);
+      dominant(M, mm, nn, neigenvalues, false, sv, U, G.empty() ? nullptr : &G);
       for (double s : sv)
         if (s > 0.0 && std::isfinite(s) && s * I.dt / 2.0 > spawning_threshold) ++nadd;
       nadd = std::min(nadd, max_add);

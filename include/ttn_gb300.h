@@ -148,6 +148,18 @@ int ttn_bond_singular_values(ttn_integrator* it, ttn_state* psi, int node, doubl
 int ttn_expect_leaf(ttn_integrator* it, ttn_state* psi, int mode, const double* op, double* re,
                     double* im);
 int ttn_norm2(ttn_integrator* it, ttn_state* psi, double* out);
+/* <bra|ket> of two states of the integrator's tree (matrix_element::operator()(bra, ket),
+ * include/ttns_lib/observables/matrix_element.hpp:223-259) */
+int ttn_overlap(ttn_integrator* it, ttn_state* bra, ttn_state* ket, double* re, double* im);
+/* <bra| prod_k O_k |ket> with dense operators ops[k] (d x d of mode modes[k], concatenated,
+ * interleaved) on distinct modes and the identity elsewhere; bra may be ket
+ * (matrix_element::operator()(product operator, bra, ket), matrix_element.hpp:318-356,
+ * :441-481) */
+int ttn_expect_product(ttn_integrator* it, ttn_state* bra, ttn_state* ket, int nops, const int* modes,
+                       const double* ops, double* re, double* im);
+/* <bra| H |ket> of a sum-of-product operator (matrix_element::operator()(sop, ...),
+ * matrix_element.hpp:358-379, :483-500): the sum of the terms' product contractions */
+int ttn_expect_sop(ttn_integrator* it, ttn_state* bra, ttn_state* ket, const ttn_sop* op, double* re, double* im);
 
 /* ---- subspace expansion ------------------------------------------------------------ */
 /* Adaptive bond dimension for the following steps, replacing

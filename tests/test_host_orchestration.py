@@ -171,6 +171,22 @@ i4.prepare(D)
 out["expansion_large_gram_ranks"] = float(np.max(np.abs(D.hrank() - orc.hrank())))
 out["expansion_large_gram_state"] = float(np.linalg.norm(full_state(D.current_topology(), D.get()) - full_state(topo, st)))
 out["expansion_large_gram_isometries"] = float(max(np.max(np.abs(a.conj().T @ a - np.eye(a.shape[1]))) for a in D.get()[1:]))
+# general observables against dense contractions of the full state vectors
+mo = sb.build(N=4, alpha=0.5, wc=5.0, d=3, chi=3, eps=0.3, delta=1.0)
+rng = np.random.default_rng(13)
+sa, sb_ = generic_state(mo.topology, rng), generic_state(mo.topology, rng)
+Ao, Bo = api.httensor(mo.topology, device=0), api.httensor(mo.topology, device=0)
+Ao.set(sa); Bo.set(sb_)
+mel = api.fixed_step_projector_splitting_integrator(Ao, mo.sop, krylov_dim=8).mel()
+fa, fb = full_state(mo.topology, sa), full_state(mo.topology, sb_)
+dims = mo.topology.mode_dims()
+ops = {{0: sb.SZ, 2: rand_herm(rng, dims[2])}}
+K = np.array([[1.0 + 0j]])
+for mm, dd in enumerate(dims):
+    K = np.kron(K, ops.get(mm, np.eye(dd)))
+out["plain_obs_overlap"] = abs(mel.overlap(Ao, Bo) - np.vdot(fa, fb))
+out["plain_obs_product"] = abs(mel.product(ops, Ao, Bo) - np.vdot(fa, K @ fb))
+out["plain_obs_sop"] = abs(mel.sop(mo.sop, Ao, Bo) - np.vdot(fa, mo.sop.dense() @ fb))
 print(json.dumps(out))
 """
 

@@ -103,6 +103,9 @@ SIGNATURES = {
     "ttn_bond_singular_values": (_I, [_P, _P, _I, _DP, C.POINTER(C.c_int)]),
     "ttn_integrator_set_expansion": (_I, [_P, _P, _IP, _D, _D, _I, _I, _I, C.c_uint]),
     "ttn_state_hrank": (_I, [_P, _IP]),
+    "ttn_overlap": (_I, [_P, _P, _P, _DP, _DP]),
+    "ttn_expect_product": (_I, [_P, _P, _P, _I, _IP, _DP, _DP, _DP]),
+    "ttn_expect_sop": (_I, [_P, _P, _P, _P, _DP, _DP]),
     "ttn_adjoint_grad": (_I, [_P, _P, _D, _D, _D, _I, _DP, _I, _DP, _I, _I, _DP, _DP, _DP, _DP]),
     "ttn_batch_step": (_I, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _I, _D, _D, _I, C.POINTER(C.c_int)]),
     "ttn_debug_tc_gemm": (_I, [_DP, _DP, _DP, _I, _I, _I]),
@@ -256,6 +259,30 @@ class matrix_element:
 
     def __init__(self, integ: "fixed_step_projector_splitting_integrator"):
         self.integ = integ
+
+    def overlap(self, bra: "httensor", ket: "httensor") -> complex:
+        """<bra|ket> (matrix_element::operator()(bra, ket))."""
+        re, im = C.c_double(), C.c_double()
+        _check(lib().ttn_overlap(self.integ.h, bra.h, ket.h, C.byref(re), C.byref(im)))
+        return complex(re.value, im.value)
+
+    def product(self, ops_by_mode: dict, bra: "httensor", ket: Optional["httensor"] = None) -> complex:
+        """<bra| prod_m O_m |ket> for a {mode: dense operator} product (ket defaults to bra)."""
+        ket = bra if ket is None else ket
+        modes = np.array(sorted(ops_by_mode), dtype=np.int32)
+        flat = np.concatenate([_cplx(ops_by_mode[int(m)]).ravel() for m in modes]) if len(modes) else np.zeros(1, np.complex128)
+        re, im = C.c_double(), C.c_double()
+        _check(lib().ttn_expect_product(self.integ.h, bra.h, ket.h, len(modes), _ip(modes), _dp(flat.view(np.float64)),
+                                        C.byref(re), C.byref(im)))
+        return complex(re.value, im.value)
+
+    def sop(self, H: SOPOperator, bra: "httensor", ket: Optional["httensor"] = None) -> complex:
+        """<bra| H |ket> of a sum-of-product operator (ket defaults to bra)."""
+        ket = bra if ket is None else ket
+        op = Operator(H)
+        re, im = C.c_double(), C.c_double()
+        _check(lib().ttn_expect_sop(self.integ.h, bra.h, ket.h, op.h, C.byref(re), C.byref(im)))
+        return complex(re.value, im.value)
 
     def __call__(self, *args):
         if len(args) == 1:

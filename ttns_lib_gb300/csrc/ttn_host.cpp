@@ -1393,6 +1393,44 @@ struct Integrator {
     std::sort(sv.begin(), sv.end(), std::greater<double>());
     return sv;
   }
+  // <B| prod_m O_m |K> for states of this tree (B may be K): the leaf-to-root contraction
+  // of matrix_element.hpp:223-259 / :441-481 with a dense operator on each mode that has
+  // one (op_of_mode[m] != nullptr, d_m x d_m on the device) and the identity elsewhere
+  cd contract(ttn_state* B, ttn_state* K, const std::vector<const double2*>& op_of_mode) {
+    for (int id = T.n - 1; id >= 0; --id) {
+      const int r = T.hrank[id];
+      const long long sz = T.size(id);
+      const double2* Ab = B->node(id);
+      const double2* Ak = K->node(id);
+      const double2* X = Ak;
+      if (T.leaf(id)) {
+        const double2* op = op_of_mode[T.leaf_mode[id]];
+        if (op) {
+          mode_apply(op, T.dims[id][0], Ak, w1, 1, r, 1.0, false, false);
+          X = w1;
+        }
+      } else {
+        const double2* cur = Ak;
+        double2* nxt = w1;
+        for (int s = 0; s < T.nmodes[id]; ++s) {
+          long long na, nb;
+          int d;
+          r3(id, s, na, d, nb);
+          mode_apply(mel[T.children[id][s]], d, cur, nxt, na, nb, 1.0, false, false);
+          cur = nxt;
+          nxt = (nxt == w1) ? w2 : w1;
+        }
+        X = cur;
+      }
+      adj_mul(Ab, X, sz / r, r, mel[id], 1.0, false);
+    }
+    ztrace(mel[0], T.hrank[0], scal + 1, stream);
+    double2 h;
+    CK(cudaMemcpyAsync(&h, scal + 1, sizeof(double2), cudaMemcpyDeviceToHost, stream));
+    d2h_bytes += sizeof(double2);
+    CK(cudaStreamSynchronize(stream));
+    return cd(h.x, h.y);
+  }
   cd expect(ttn_state* S, int mode, const double2* op_dev) {
     for (int id = T.n - 1; id >= 0; --id) {
       const int r = T.hrank[id];
@@ -1817,6 +1855,84 @@ int ttn_expect_leaf(ttn_integrator* it, ttn_state* psi, int mode, const double* 
   ttn::cd v = it->I.expect(psi, mode, dop);
   if (re) *re = v.real();
   if (im) *im = v.imag();
+  TTN_API_END
+}
+// dense operators uploaded for one call: ops[k] (d_k x d_k interleaved) on modes[k]
+static std::vector<const double2*> upload_ops(ttn::Integrator& I, ttn::DevBuf& buf, int nops, const int* modes,
+                                              const double* ops) {
+  std::vector<const double2*> by_mode(I.H.nmodes, nullptr);
+  size_t total = 0;
+  for (int k = 0; k < nops; ++k) {
+    TTN_REQUIRE(modes[k] >= 0 && modes[k] < I.H.nmodes, TTN_EINVAL, "mode out of range");
+    TTN_REQUIRE(!by_mode[modes[k]], TTN_EINVAL, "one operator per mode");
+    by_mode[modes[k]] = reinterpret_cast<const double2*>(1);
+    total += (size_t)I.H.mode_dim[modes[k]] * I.H.mode_dim[modes[k]];
+  }
+  std::fill(by_mode.begin(), by_mode.end(), nullptr);
+  if (nops == 0) return by_mode;
+  for (size_t i = 0; i < 2 * total; ++i) TTN_REQUIRE(std::isfinite(ops[i]), TTN_EINVAL, "non-finite operator entry");
+  buf.alloc(total * sizeof(double2));
+  CK(cudaMemcpyAsync(buf.p, ops, total * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  CK(cudaStreamSynchronize(I.stream));
+  size_t off = 0;
+  for (int k = 0; k < nops; ++k) {
+    by_mode[modes[k]] = buf.as<double2>() + off;
+    off += (size_t)I.H.mode_dim[modes[k]] * I.H.mode_dim[modes[k]];
+  }
+  return by_mode;
+}
+int ttn_overlap(ttn_integrator* it, ttn_state* bra, ttn_state* ket, double* re, double* im) {
+  return ttn_expect_product(it, bra, ket, 0, nullptr, nullptr, re, im);
+}
+int ttn_expect_product(ttn_integrator* it, ttn_state* bra, ttn_state* ket, int nops, const int* modes, const double* ops,
+                       double* re, double* im) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && bra && ket && nops >= 0 && (nops == 0 || (modes && ops)), TTN_EINVAL, "null argument");
+  ttn::check_same_tree(it->I.T, bra->T);
+  ttn::check_same_tree(it->I.T, ket->T);
+  CK(cudaSetDevice(it->I.device));
+  ttn::DevBuf buf;
+  const auto by_mode = upload_ops(it->I, buf, nops, modes, ops);
+  const ttn::cd v = it->I.contract(bra, ket, by_mode);
+  if (re) *re = v.real();
+  if (im) *im = v.imag();
+  TTN_API_END
+}
+int ttn_expect_sop(ttn_integrator* it, ttn_state* bra, ttn_state* ket, const ttn_sop* op, double* re, double* im) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && bra && ket && op, TTN_EINVAL, "null argument");
+  ttn::check_same_tree(it->I.T, bra->T);
+  ttn::check_same_tree(it->I.T, ket->T);
+  const ttn::Sop& H = op->H;
+  TTN_REQUIRE(H.nmodes == it->I.H.nmodes && H.mode_dim == it->I.H.mode_dim, TTN_EINVAL, "operator modes differ from the tree's");
+  CK(cudaSetDevice(it->I.device));
+  // every primitive operator on the device once, then one contraction per term
+  size_t total = 0;
+  for (int m = 0; m < H.nmodes; ++m)
+    for (auto& M : H.ops[m]) total += M.size();
+  ttn::DevBuf buf;
+  buf.alloc(std::max<size_t>(total, 1) * sizeof(double2));
+  std::vector<std::vector<const double2*>> dev(H.nmodes);
+  {
+    std::vector<double2> h(total);
+    size_t off = 0;
+    for (int m = 0; m < H.nmodes; ++m)
+      for (auto& M : H.ops[m]) {
+        dev[m].push_back(buf.as<double2>() + off);
+        for (size_t i = 0; i < M.size(); ++i) h[off + i] = ttn::d2(M[i]);
+        off += M.size();
+      }
+    CK(cudaMemcpyAsync(buf.p, h.data(), total * sizeof(double2), cudaMemcpyHostToDevice, it->I.stream));
+    CK(cudaStreamSynchronize(it->I.stream));
+  }
+  ttn::cd sum = 0.0;
+  std::vector<const double2*> by_mode(H.nmodes);
+  for (int r = 0; r < H.nterms; ++r) {
+    for (int m = 0; m < H.nmodes; ++m) by_mode[m] = H.opidx[m][r] >= 0 ? dev[m][H.opidx[m][r]] : nullptr;
+    sum += H.coeff[r] * it->I.contract(bra, ket, by_mode);
+  }
+  if (re) *re = sum.real();
+  if (im) *im = sum.imag();
   TTN_API_END
 }
 int ttn_bond_singular_values(ttn_integrator* it, ttn_state* psi, int node, double* out, int* n) {

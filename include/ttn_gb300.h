@@ -124,6 +124,15 @@ int ttn_integrator_step(ttn_integrator* it, ttn_state* psi, double coeff_re, dou
                         double* dt_out);
 int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out);
 int ttn_integrator_reset(ttn_integrator* it);
+/* Checkpoints (the reference serialises integrator and state with cereal,
+ * include/ttns_lib/integrators/projector_splitting_integrator.hpp:50-68, :198-216 and
+ * include/ttns_lib/httensor.hpp:101-118): the tree, the integrator's step count, dt,
+ * time, coefficient and H-application count, and every node tensor, in one little-endian
+ * file.  Loading into an integrator and state of the same tree resumes the run exactly
+ * (the environments the next step carries in are recomputed from the tensors).  Not for
+ * integrators with subspace expansion. */
+int ttn_integrator_save(ttn_integrator* it, ttn_state* psi, const char* path);
+int ttn_integrator_load(ttn_integrator* it, ttn_state* psi, const char* path);
 /* wait for all queued device work of this integrator */
 int ttn_integrator_synchronize(ttn_integrator* it);
 

@@ -187,6 +187,25 @@ for mm, dd in enumerate(dims):
 out["plain_obs_overlap"] = abs(mel.overlap(Ao, Bo) - np.vdot(fa, fb))
 out["plain_obs_product"] = abs(mel.product(ops, Ao, Bo) - np.vdot(fa, K @ fb))
 out["plain_obs_sop"] = abs(mel.sop(mo.sop, Ao, Bo) - np.vdot(fa, mo.sop.dense() @ fb))
+# checkpoint and resume: identical continuation
+import tempfile
+with tempfile.TemporaryDirectory() as td:
+    path = td + "/run.ckpt"
+    mo = sb.build(N=4, alpha=0.5, wc=5.0, d=3, chi=3, eps=0.3, delta=1.0)
+    st = generic_state(mo.topology, np.random.default_rng(3))
+    Ac = api.httensor(mo.topology, device=0); Ac.set(st)
+    ref = api.fixed_step_projector_splitting_integrator(Ac, mo.sop, krylov_dim=8)
+    ref.dt = 0.05
+    for k in range(5):
+        ref(Ac)
+        if k == 2:
+            ref.save(Ac, path)
+    Bc = api.httensor(mo.topology, device=0)
+    res = api.fixed_step_projector_splitting_integrator(Bc, mo.sop, krylov_dim=8)
+    res.load(Bc, path)
+    for _ in range(2):
+        res(Bc)
+    out["plain_checkpoint_resume"] = float(max(np.max(np.abs(a - b)) for a, b in zip(Ac.get(), Bc.get())))
 print(json.dumps(out))
 """
 

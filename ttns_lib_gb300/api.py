@@ -104,6 +104,8 @@ SIGNATURES = {
     "ttn_integrator_set_expansion": (_I, [_P, _P, _IP, _D, _D, _I, _I, _I, C.c_uint]),
     "ttn_state_hrank": (_I, [_P, _IP]),
     "ttn_overlap": (_I, [_P, _P, _P, _DP, _DP]),
+    "ttn_integrator_save": (_I, [_P, _P, C.c_char_p]),
+    "ttn_integrator_load": (_I, [_P, _P, C.c_char_p]),
     "ttn_expect_product": (_I, [_P, _P, _P, _I, _IP, _DP, _DP, _DP]),
     "ttn_expect_sop": (_I, [_P, _P, _P, _P, _DP, _DP]),
     "ttn_adjoint_grad": (_I, [_P, _P, _D, _D, _D, _I, _DP, _I, _DP, _I, _I, _DP, _DP, _DP, _DP]),
@@ -409,6 +411,14 @@ class fixed_step_projector_splitting_integrator:
 
     def mel(self) -> matrix_element:
         return self._mel
+
+    def save(self, A: httensor, path: str):
+        """Checkpoint of this integrator and the state A (resumable with ``load``)."""
+        _check(lib().ttn_integrator_save(self.h, A.h, os.fsencode(path)))
+
+    def load(self, A: httensor, path: str):
+        """Resume from a checkpoint written by ``save`` (same tree)."""
+        _check(lib().ttn_integrator_load(self.h, A.h, os.fsencode(path)))
 
     def set_expansion(self, A: httensor, capacity, spawning_threshold: float = 1e-12,
                       unoccupied_threshold: float = 1e-12, minimum_unoccupied: int = 0, neigenvalues: int = 2,

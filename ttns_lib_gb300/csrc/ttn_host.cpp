@@ -24,6 +24,7 @@
 #include <thread>
 #include <complex>
 #include <cstring>
+#include <cstdio>
 #include <functional>
 #include <map>
 #include <memory>
@@ -1823,6 +1824,102 @@ int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out) {
   *out = it->I.nh;
   TTN_API_END
 }
+// ---- checkpoints: integrator scalars and the state in one little-endian file
+namespace {
+const char kCkptMagic[8] = {'T', 'T', 'N', 'C', 'K', 'P', 'T', '1'};
+struct FileCloser {
+  FILE* f;
+  ~FileCloser() { if (f) std::fclose(f); }
+};
+void put_raw(FILE* f, const void* p, size_t elem, size_t n) {
+  TTN_REQUIRE(std::fwrite(p, elem, n, f) == n, TTN_EINVAL, "checkpoint: write failed");
+}
+void get_raw(FILE* f, void* p, size_t elem, size_t n) {
+  TTN_REQUIRE(std::fread(p, elem, n, f) == n, TTN_EINVAL, "checkpoint: truncated file");
+}
+#define CKPT_PUT(f, p, n) put_raw(f, p, sizeof(*(p)), n)
+#define CKPT_GET(f, p, n) get_raw(f, p, sizeof(*(p)), n)
+}  // namespace
+int ttn_integrator_save(ttn_integrator* it, ttn_state* psi, const char* path) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi && path, TTN_EINVAL, "null argument");
+  ttn::check_same_tree(it->I.T, psi->T);
+  ttn::Integrator& I = it->I;
+  CK(cudaSetDevice(I.device));
+  CK(cudaStreamSynchronize(I.stream));
+  FileCloser fc{std::fopen(path, "wb")};
+  TTN_REQUIRE(fc.f, TTN_EINVAL, std::string("checkpoint: cannot open ") + path);
+  CKPT_PUT(fc.f, kCkptMagic, 8);
+  const int n = I.T.n;
+  CKPT_PUT(fc.f, &n, 1);
+  CKPT_PUT(fc.f, I.T.parent.data(), n);
+  CKPT_PUT(fc.f, I.T.hrank.data(), n);
+  CKPT_PUT(fc.f, I.T.leaf_mode.data(), n);
+  CKPT_PUT(fc.f, I.T.leaf_dim.data(), n);
+  const long long nsteps = I.nsteps, nh = I.nh;
+  const double sc[3] = {I.dt, I.t_engine, I.coeff.real()};
+  const double ci = I.coeff.imag();
+  CKPT_PUT(fc.f, &nsteps, 1);
+  CKPT_PUT(fc.f, &nh, 1);
+  CKPT_PUT(fc.f, sc, 3);
+  CKPT_PUT(fc.f, &ci, 1);
+  for (int i = 0; i < n; ++i) {
+    std::vector<double2> h((size_t)psi->T.size(i));
+    CK(cudaMemcpyAsync(h.data(), psi->node(i), h.size() * sizeof(double2), cudaMemcpyDeviceToHost, I.stream));
+    CK(cudaStreamSynchronize(I.stream));
+    CKPT_PUT(fc.f, h.data(), h.size());
+  }
+  TTN_API_END
+}
+int ttn_integrator_load(ttn_integrator* it, ttn_state* psi, const char* path) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi && path, TTN_EINVAL, "null argument");
+  ttn::check_same_tree(it->I.T, psi->T);
+  ttn::Integrator& I = it->I;
+  TTN_REQUIRE(!it->X, TTN_EINVAL, "checkpoint: not supported with subspace expansion");
+  CK(cudaSetDevice(I.device));
+  FileCloser fc{std::fopen(path, "rb")};
+  TTN_REQUIRE(fc.f, TTN_EINVAL, std::string("checkpoint: cannot open ") + path);
+  char magic[8];
+  CKPT_GET(fc.f, magic, 8);
+  TTN_REQUIRE(std::memcmp(magic, kCkptMagic, 8) == 0, TTN_EINVAL, "checkpoint: not a checkpoint file");
+  int n = 0;
+  CKPT_GET(fc.f, &n, 1);
+  TTN_REQUIRE(n == I.T.n, TTN_EINVAL, "checkpoint: different tree");
+  std::vector<int> a(n);
+  for (const std::vector<int>* want : {&I.T.parent, &I.T.hrank, &I.T.leaf_mode, &I.T.leaf_dim}) {
+    CKPT_GET(fc.f, a.data(), n);
+    TTN_REQUIRE(a == *want, TTN_EINVAL, "checkpoint: different tree");
+  }
+  long long nsteps = 0, nh = 0;
+  double sc[3], ci = 0.0;
+  CKPT_GET(fc.f, &nsteps, 1);
+  CKPT_GET(fc.f, &nh, 1);
+  CKPT_GET(fc.f, sc, 3);
+  CKPT_GET(fc.f, &ci, 1);
+  for (int i = 0; i < n; ++i) {
+    std::vector<double2> h((size_t)psi->T.size(i));
+    CKPT_GET(fc.f, h.data(), h.size());
+    for (const double2& z : h) TTN_REQUIRE(std::isfinite(z.x) && std::isfinite(z.y), TTN_EINVAL, "checkpoint: non-finite tensor");
+    CK(cudaMemcpyAsync(psi->node(i), h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+    CK(cudaStreamSynchronize(I.stream));
+  }
+  I.nsteps = nsteps;
+  I.nh = nh;
+  I.dt = sc[0];
+  I.t_engine = sc[1];
+  I.coeff = ttn::cd(sc[2], ci);
+  // the single-particle environments the next step carries in: consistent with the state
+  // (each was last written from its node's final tensor), so recomputed bottom-up they
+  // equal the saved run's
+  if (nsteps > 0)
+    for (int id = I.T.n - 1; id >= 1; --id) I.update_spf(id, psi->node(id));
+  CK(cudaMemcpyAsync(I.nh_dev, &nh, sizeof(long long), cudaMemcpyHostToDevice, I.stream));
+  CK(cudaStreamSynchronize(I.stream));
+  TTN_API_END
+}
+#undef CKPT_PUT
+#undef CKPT_GET
 int ttn_integrator_reset(ttn_integrator* it) {
   TTN_API_BEGIN
   TTN_REQUIRE(it, TTN_EINVAL, "null argument");

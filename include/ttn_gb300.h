@@ -170,6 +170,16 @@ int ttn_expect_product(ttn_integrator* it, ttn_state* bra, ttn_state* ket, int n
  * matrix_element.hpp:358-379, :483-500): the sum of the terms' product contractions */
 int ttn_expect_sop(ttn_integrator* it, ttn_state* bra, ttn_state* ket, const ttn_sop* op, double* re, double* im);
 
+/* ---- time-dependent primitive operators --------------------------------------------- */
+/* fn(user, mode, op, t, dt, mat) is called before every leaf evolution for each operator
+ * bound on the leaf's mode -- the reference's primitive::update(t, dt) hook
+ * (include/ttns_lib/tdvp_core/projector_splitting_engine.hpp:139, called with the engine
+ * time and dt/2): op is the operator's binding index, mat its d x d matrix (interleaved),
+ * updated in place on the host and copied to the device.  fn = NULL removes the hook.
+ * FP64 integrators only. */
+typedef void (*ttn_op_update_fn)(void* user, int mode, int op, double t, double dt, double* mat);
+int ttn_integrator_set_op_update(ttn_integrator* it, ttn_op_update_fn fn, void* user);
+
 /* ---- subspace expansion ------------------------------------------------------------ */
 /* Adaptive bond dimension for the following steps, replacing
  * subspace_expansion_projector_splitting_integrator

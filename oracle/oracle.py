@@ -65,6 +65,7 @@ def lib():
         L.orc_set_expansion.argtypes = [P, ip, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_uint]
         L.orc_get_hrank.argtypes = [P, ip]
         L.orc_top_eig.argtypes = [C.c_int, C.c_int, dp, dp, dp]
+        L.orc_set_op_update.argtypes = [P, P, P]
         L.orc_expand_prepare.argtypes = [P, C.c_double, ip]
         L.orc_adjoint.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_int, dp, C.c_int, dp, C.c_int, C.c_int,
                                   dp, dp, dp, dp]
@@ -100,6 +101,7 @@ class Oracle:
         L.orc_set_threads(self.h, threads)
         self.offsets = topo.offsets()
         self._nterms = sop.nterms
+        self._mode_dims = list(sop.mode_dims)
         self._opdims = [int(sop.mode_dims[m]) for m in op_mode]
         self._opsize = sum(d * d for d in self._opdims)
 
@@ -123,6 +125,24 @@ class Oracle:
         flat = np.zeros(int(offs[-1]), dtype=np.complex128)
         self._check(lib().orc_get_state(self.h, _dp(flat.view(np.float64))))
         return [flat[offs[i]:offs[i + 1]].reshape(topo.node_shape(i)).copy() for i in range(topo.nnodes)]
+
+    def set_op_update(self, callback):
+        """Time-dependent primitive operators: ``callback(mode, op, t, dt, mat)`` before
+        every leaf evolution (``mat`` updated in place); ``None`` removes the hook."""
+        if callback is None:
+            self._check(lib().orc_set_op_update(self.h, None, None))
+            self._op_cb = None
+            return
+        dims = self._mode_dims
+        fn_t = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double))
+
+        def trampoline(user, mode, op, t, dt, mat):
+            d = dims[mode]
+            arr = np.ctypeslib.as_array(mat, shape=(2 * d * d,)).view(np.complex128).reshape(d, d)
+            callback(mode, op, t, dt, arr)
+
+        self._op_cb = fn_t(trampoline)
+        self._check(lib().orc_set_op_update(self.h, C.cast(self._op_cb, C.c_void_p), None))
 
     def hrank(self):
         out = np.zeros(self.topo.nnodes, dtype=np.int32)

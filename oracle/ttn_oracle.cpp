@@ -601,6 +601,9 @@ struct Engine {
   // decomposition towards a child in the forward half-sweep, and after a node's
   // leaf-to-root decomposition in the backward half-sweep; `expanded` records growth.
   std::function<bool(int)> expand_down, expand_up;
+  // optional update of the primitive operators of a leaf's mode before its evolution
+  // (mode, index within the mode, t, dt/2, matrix in place)
+  std::function<void(int, int, double, double, cd*)> op_update;
   bool expanded = false;
   std::chrono::steady_clock::time_point tmark;
   void tick() { tmark = std::chrono::steady_clock::now(); }
@@ -927,6 +930,12 @@ struct Engine {
   // ---- node and bond evolution (projector_splitting_engine.hpp:117-165)
   void evolve_node(int nd) {
     if (on_op) on_op(OP_NODE, nd, 0);
+    // time-dependent primitive operators: op.update(leaf, t, dt/2) before a leaf's
+    // evolution (projector_splitting_engine.hpp:139)
+    if (op_update && T.leaf(nd)) {
+      const int mode = T.leaf_mode[nd];
+      for (size_t k = 0; k < H.ops[mode].size(); ++k) op_update(mode, (int)k, t_engine, dt / 2.0, H.ops[mode][k].data());
+    }
     nh += expm([&](const cd* v, cd* o) { heff(nd, v, o); }, A[nd].data(), T.size(nd), dt / 2.0, coeff);
   }
   // R: the bond matrix held in rmat[owner] (the node's own after l2r, its parent's after r2l)
@@ -1287,6 +1296,23 @@ int orc_top_eig(int g, int k, const double* G, double* vals, double* vecs) {
     }
     return (int)w.size();
   } catch (...) { return -1; }
+}
+// Time-dependent primitive operators: fn(user, mode, op, t, dt, mat) is called before every
+// leaf evolution for each operator bound on the leaf's mode (op = its binding index; mat
+// the d x d matrix, interleaved, updated in place); fn = NULL removes the hook.
+typedef void (*orc_op_update_fn)(void* user, int mode, int op, double t, double dt, double* mat);
+int orc_set_op_update(void* p, orc_op_update_fn fn, void* user) {
+  OrcHandle* h = (OrcHandle*)p;
+  ORC_TRY(h, {
+    orc::Engine& E = h->E;
+    if (!fn) { E.op_update = nullptr; return 0; }
+    std::vector<std::vector<int>> global(E.H.nmodes);
+    for (int m = 0; m < E.H.nmodes; ++m) global[m].assign(E.H.ops[m].size(), -1);
+    for (size_t g = 0; g < E.H.op_order.size(); ++g) global[E.H.op_order[g].first][E.H.op_order[g].second] = (int)g;
+    E.op_update = [fn, user, global](int mode, int k, double t, double dt, cd* mat) {
+      fn(user, mode, global[mode][k], t, dt, reinterpret_cast<double*>(mat));
+    };
+  })
 }
 // the current bond dimension above every node (hrank)
 int orc_get_hrank(void* p, int* out) {

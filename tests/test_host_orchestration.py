@@ -206,6 +206,21 @@ with tempfile.TemporaryDirectory() as td:
     for _ in range(2):
         res(Bc)
     out["plain_checkpoint_resume"] = float(max(np.max(np.abs(a - b)) for a, b in zip(Ac.get(), Bc.get())))
+# time-dependent primitive operators through the update hook, against the oracle
+def upd(mode, op, t, dt, mat):
+    if op == 0:
+        mat[:] = 0.5 * (0.3 + 0.8 * np.cos(3.0 * (t + dt / 2))) * sb.SZ + 0.5 * sb.SX
+w0, c0 = sb.ohmic_modes(4, 0.5, 5.0)
+mt = sb.build_from_modes(w0, c0, 3, 3, 0.3, 1.0)
+st = generic_state(mt.topology, np.random.default_rng(2))
+orc = Oracle(mt.topology, mt.sop, krylov_dim=10, krylov_tol=1e-12); orc.set_state(st); orc.set_op_update(upd)
+At = api.httensor(mt.topology, device=0); At.set(st)
+it_ = api.fixed_step_projector_splitting_integrator(At, mt.sop, krylov_dim=10)
+it_.set_op_update(upd)
+it_.dt = 0.05
+for _ in range(6):
+    it_(At); orc.step(0.05)
+out["plain_time_dependent"] = float(max(np.max(np.abs(a - b)) for a, b in zip(At.get(), orc.get_state())))
 print(json.dumps(out))
 """
 

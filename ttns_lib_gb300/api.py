@@ -105,6 +105,7 @@ SIGNATURES = {
     "ttn_state_hrank": (_I, [_P, _IP]),
     "ttn_overlap": (_I, [_P, _P, _P, _DP, _DP]),
     "ttn_integrator_save": (_I, [_P, _P, C.c_char_p]),
+    "ttn_integrator_set_op_update": (_I, [_P, _P, _P]),
     "ttn_integrator_load": (_I, [_P, _P, C.c_char_p]),
     "ttn_expect_product": (_I, [_P, _P, _P, _I, _IP, _DP, _DP, _DP]),
     "ttn_expect_sop": (_I, [_P, _P, _P, _P, _DP, _DP]),
@@ -114,6 +115,9 @@ SIGNATURES = {
 }
 
 _lib = None
+
+# void (*)(void* user, int mode, int op, double t, double dt, double* mat)
+OP_UPDATE_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double))
 
 
 def lib():
@@ -411,6 +415,25 @@ class fixed_step_projector_splitting_integrator:
 
     def mel(self) -> matrix_element:
         return self._mel
+
+    def set_op_update(self, callback):
+        """Time-dependent primitive operators: ``callback(mode, op, t, dt, mat)`` is called
+        before every leaf evolution for each operator bound on the leaf's mode (``op`` its
+        binding index, ``mat`` its d x d complex matrix, to be updated in place);
+        ``None`` removes the hook (primitive::update(t, dt) of the reference)."""
+        if callback is None:
+            _check(lib().ttn_integrator_set_op_update(self.h, None, None))
+            self._op_cb = None
+            return
+        dims = self._sop.mode_dims
+
+        def trampoline(user, mode, op, t, dt, mat):
+            d = dims[mode]
+            arr = np.ctypeslib.as_array(mat, shape=(2 * d * d,)).view(np.complex128).reshape(d, d)
+            callback(mode, op, t, dt, arr)
+
+        self._op_cb = OP_UPDATE_FN(trampoline)
+        _check(lib().ttn_integrator_set_op_update(self.h, C.cast(self._op_cb, C.c_void_p), None))
 
     def save(self, A: httensor, path: str):
         """Checkpoint of this integrator and the state A (resumable with ``load``)."""

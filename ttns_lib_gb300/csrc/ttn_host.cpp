@@ -484,6 +484,25 @@ struct Integrator {
   Tree Tsz;
   std::function<bool(ttn_state*, int)> expand_down_fn, expand_up_fn;
   std::function<void(ttn_state*, double, cd)> expanding_step;
+  // time-dependent primitive operators (ttn_integrator_set_op_update)
+  ttn_op_update_fn op_update_fn = nullptr;
+  void* op_update_user = nullptr;
+  std::vector<std::vector<int>> op_global;  // [mode][k] -> binding index
+  // op.update(leaf, t, dt/2) before a leaf's evolution (projector_splitting_engine.hpp:139):
+  // the user updates each operator of the mode on the host; the device copy follows
+  void update_leaf_ops(int mode) {
+    for (size_t k = 0; k < H.ops[mode].size(); ++k) {
+      std::vector<cd>& M = H.ops[mode][k];
+      op_update_fn(op_update_user, mode, op_global[mode][k], t_engine, dt / 2.0, reinterpret_cast<double*>(M.data()));
+      std::vector<double2> h(M.size());
+      for (size_t i = 0; i < M.size(); ++i) {
+        TTN_REQUIRE(std::isfinite(M[i].real()) && std::isfinite(M[i].imag()), TTN_ENUMERIC, "operator update produced a non-finite entry");
+        h[i] = d2(M[i]);
+      }
+      CK(cudaMemcpyAsync(leaf_ops[mode][k], h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, stream));
+      CK(cudaStreamSynchronize(stream));  // h is pageable and goes out of scope
+    }
+  }
   bool expanded = false;
 
   ~Integrator() {
@@ -1203,6 +1222,7 @@ struct Integrator {
   // ---------------------------------------------------------------- sweep
   void evolve_node(ttn_state* S, int nd) {
     if (on_op) on_op(OP_NODE, nd, 0);
+    if (op_update_fn && T.leaf(nd)) update_leaf_ops(T.leaf_mode[nd]);
     Prof pf(this, 0, nd);
     expm_dev(nd, 0, S->node(nd), T.size(nd), dt / 2.0, coeff, true);
   }
@@ -2056,6 +2076,7 @@ int ttn_adjoint_grad(ttn_integrator* it, ttn_state* psi, double dt, double coeff
   TTN_REQUIRE(!I.mixed, TTN_EINVAL, "the adjoint sweep needs an FP64 integrator (TTN_PREC_FP64)");
   TTN_REQUIRE(I.nsteps == 0, TTN_EINVAL, "the adjoint sweep starts from step 0 (a fresh or reset integrator)");
   TTN_REQUIRE(!it->X, TTN_EINVAL, "the adjoint sweep needs fixed bond dimensions (no subspace expansion)");
+  TTN_REQUIRE(!I.op_update_fn, TTN_EINVAL, "the adjoint sweep needs time-independent operators");
   for (int k = 0; k < nsteps; ++k) TTN_REQUIRE(std::isfinite(weights[k]), TTN_EINVAL, "non-finite weight");
   CK(cudaSetDevice(I.device));
   const int d = I.H.mode_dim[mode];
@@ -2143,6 +2164,18 @@ int ttn_integrator_set_expansion(ttn_integrator* it, ttn_state* psi, const int* 
   X->only_when_no_unoccupied = only_when_no_unoccupied != 0;
   X->rng.seed(seed);
   I.expanding_step = [X](ttn_state* S, double dt, ttn::cd cf) { X->step(S, dt, cf); };
+  TTN_API_END
+}
+int ttn_integrator_set_op_update(ttn_integrator* it, ttn_op_update_fn fn, void* user) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it, TTN_EINVAL, "null argument");
+  ttn::Integrator& I = it->I;
+  TTN_REQUIRE(!fn || !I.mixed, TTN_EINVAL, "time-dependent operators need an FP64 integrator");
+  I.op_update_fn = fn;
+  I.op_update_user = user;
+  I.op_global.assign(I.H.nmodes, {});
+  for (int m = 0; m < I.H.nmodes; ++m) I.op_global[m].assign(I.H.ops[m].size(), -1);
+  for (size_t g = 0; g < I.H.op_order.size(); ++g) I.op_global[I.H.op_order[g].first][I.H.op_order[g].second] = (int)g;
   TTN_API_END
 }
 int ttn_state_hrank(const ttn_state* s, int* out) {

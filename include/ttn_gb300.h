@@ -123,6 +123,11 @@ int ttn_batch_step(ttn_integrator* const* its, ttn_state* const* states, int n, 
 int ttn_integrator_step(ttn_integrator* it, ttn_state* psi, double coeff_re, double coeff_im,
                         double* dt_out);
 int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out);
+/* one-site and two-site subspace expansions so far (Nonesite / Ntwosite,
+ * include/ttns_lib/tdvp_core/subspace_expansion_projector_splitting_engine.hpp:513-514):
+ * the descent counts every two-site attempt, the ascent only the attempts that grew a
+ * bond, as the reference does; both zero without expansion */
+int ttn_integrator_expansion_counts(const ttn_integrator* it, long long* onesite, long long* twosite);
 int ttn_integrator_reset(ttn_integrator* it);
 /* Checkpoints (the reference serialises integrator and state with cereal,
  * include/ttns_lib/integrators/projector_splitting_integrator.hpp:50-68, :198-216 and

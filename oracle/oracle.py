@@ -67,6 +67,8 @@ def lib():
         L.orc_top_eig.argtypes = [C.c_int, C.c_int, dp, dp, dp]
         L.orc_set_op_update.argtypes = [P, P, P]
         L.orc_expand_prepare.argtypes = [P, C.c_double, ip]
+        L.orc_expansion_counts.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+        L.orc_init_product.argtypes = [P, dp, C.c_uint]
         L.orc_adjoint.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_int, dp, C.c_int, dp, C.c_int, C.c_int,
                                   dp, dp, dp, dp]
         _lib = L
@@ -190,6 +192,20 @@ class Oracle:
     @property
     def nh_applications(self) -> int:
         return int(lib().orc_nh(self.h))
+
+    def expansion_counts(self):
+        """(one-site, two-site) expansions so far."""
+        a, b = C.c_longlong(), C.c_longlong()
+        self._check(lib().orc_expansion_counts(self.h, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
+
+    def init_product(self, psi0=None, seed: int = 0):
+        """The spin-boson driver's start state drawn with std::mt19937(seed)."""
+        if psi0 is None:
+            self._check(lib().orc_init_product(self.h, None, int(seed)))
+        else:
+            p = np.ascontiguousarray(psi0, dtype=np.complex128)
+            self._check(lib().orc_init_product(self.h, _dp(p.view(np.float64)), int(seed)))
 
     def expect(self, mode: int, op) -> complex:
         out = np.zeros(2)

@@ -409,8 +409,8 @@ struct Expander {
           for (auto& z : f[j]) z = std::conj(z);
         }
         grow(C, f, {}, true);
-        ++n_twosite;
       }
+      ++n_twosite;  // down counts every two-site attempt
     } else {
       while (nadd < required) {
         const std::vector<cd> x = random_orthogonal(outer, parent_slices(C));
@@ -450,7 +450,7 @@ struct Expander {
       if (nadd) {
         U.resize(nadd);
         grow(C, {}, U, false);
-        ++n_twosite;
+        ++n_twosite;  // up counts only the attempts that grew the bond
       }
     } else {
       while (nadd < required) {

@@ -1350,6 +1350,74 @@ int orc_prepare(void* p) {
 }
 double orc_t(void* p) { OrcHandle* h = (OrcHandle*)p; return h->E.nsteps * h->E.dt; }
 long long orc_nh(void* p) { return ((OrcHandle*)p)->E.nh; }
+// one-site and two-site expansions so far (subspace_expansion_projector_splitting_engine
+// Nonesite / Ntwosite, include/ttns_lib/tdvp_core/subspace_expansion_projector_splitting_
+// engine.hpp:513-514); zero without expansion
+int orc_expansion_counts(void* p, long long* onesite, long long* twosite) {
+  OrcHandle* h = (OrcHandle*)p;
+  *onesite = h->X ? h->X->n_onesite : 0;
+  *twosite = h->X ? h->X->n_twosite : 0;
+  return 0;
+}
+// The spin-boson driver's start state (src/spin_boson.cpp:584-649), in pre-order over the
+// nodes with one std::mt19937(seed) stream: at a leaf, SPF 0 is psi0 (mode 0, when given)
+// or the first basis state, and SPFs 1.. are random vectors -- per element a uniform phase
+// in [0, 2 pi) then a standard-normal length, both distributions created afresh at every
+// leaf -- normalised and Gram-Schmidt orthogonalised against the earlier SPFs, redrawn
+// when the remainder is below 1e-12; interior nodes are identities and the root is e_0.
+int orc_init_product(void* p, const double* psi0, unsigned seed) {
+  OrcHandle* h = (OrcHandle*)p;
+  ORC_TRY(h, {
+    orc::Engine& E = h->E;
+    std::mt19937 rng(seed);
+    for (int i = 0; i < E.T.n; ++i) {
+      const long long d = E.T.dimen[i];
+      const int r = E.T.hrank[i];
+      std::vector<cd>& A = E.A[i];
+      std::fill(A.begin(), A.end(), cd(0.0));
+      if (E.T.leaf(i)) {
+        std::vector<std::vector<cd>> spf(r, std::vector<cd>(d, 0.0));
+        if (E.T.leaf_mode[i] == 0 && psi0) {
+          for (long long j = 0; j < d; ++j) spf[0][j] = cd(psi0[2 * j], psi0[2 * j + 1]);
+        } else {
+          spf[0][0] = 1.0;
+        }
+        std::uniform_real_distribution<double> phase(0, 2.0 * std::acos(-1.0));
+        std::normal_distribution<double> length(0, 1);
+        for (int k = 1; k < r; ++k) {
+          for (;;) {
+            for (long long j = 0; j < d; ++j) {
+              const double th = phase(rng);
+              spf[k][j] = length(rng) * cd(std::cos(th), std::sin(th));
+            }
+            cd n2 = 0.0;
+            for (const cd& z : spf[k]) n2 += std::conj(z) * z;
+            const cd sn = std::sqrt(n2);
+            for (cd& z : spf[k]) z /= sn;
+            for (int q = 0; q < k; ++q) {
+              cd ov = 0.0;
+              for (long long j = 0; j < d; ++j) ov += std::conj(spf[q][j]) * spf[k][j];
+              for (long long j = 0; j < d; ++j) spf[k][j] -= ov * spf[q][j];
+            }
+            double nrm = 0.0;
+            for (const cd& z : spf[k]) nrm += std::norm(z);
+            nrm = std::sqrt(nrm);
+            if (nrm > 1e-12) {
+              for (cd& z : spf[k]) z /= nrm;
+              break;
+            }
+          }
+        }
+        for (long long j = 0; j < d; ++j)
+          for (int k = 0; k < r; ++k) A[(size_t)j * r + k] = spf[k][j];
+      } else if (i != 0) {
+        for (long long j = 0; j < d && j < r; ++j) A[(size_t)j * r + j] = 1.0;
+      } else {
+        A[0] = 1.0;
+      }
+    }
+  })
+}
 long long orc_nsteps(void* p) { return ((OrcHandle*)p)->E.nsteps; }
 
 int orc_expect(void* p, int mode, const double* op, double* out) {

@@ -1,0 +1,207 @@
+"""The spin-boson driver (ttns_lib_gb300/driver.py, bath.py) against the reference's own
+example outputs (tests/golden/driver_examples.json, made by make_driver_fixtures.py from
+the reference's inputs/ and example_outputs/): the tree each input lays out, the output
+format, and -- through the oracle -- the first step of the dynamics; plus known answers
+for the bath discretisation and the block operators."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from ttns_lib_gb300 import bath as B
+from ttns_lib_gb300 import driver as D
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "driver_examples.json")
+WITH_BONDS = ["beta_10/ohmic/spin_boson_debye", "beta_10/ohmic/spin_boson_exponential",
+              "beta_10/ohmic/spin_boson_sudden"]
+
+
+def _golden():
+    with open(GOLDEN) as f:
+        return json.load(f)
+
+
+def test_inputs_parse_with_the_reference_key_rules():
+    g = _golden()
+    for case, v in g.items():
+        inp = D.parse_input(v["input"])
+        assert inp.nmodes == 512 and inp.dt == 5e-3
+        assert len(inp.ops) == 4
+        assert np.allclose(inp.ops[1], [[0, -1j], [1j, 0]])
+        assert inp.minimum_unoccupied == 2 and inp.krylov_dim == 12
+        assert inp.bath.nonzero_temperature == case.startswith("beta")
+    d = dict(g[WITH_BONDS[0]]["input"])
+    d["  Max   Frequency Cutoff "] = d.pop("max frequency cutoff")
+    assert D.parse_input(d).max_frequency_cutoff == 500
+    bad = dict(g[WITH_BONDS[0]]["input"])
+    bad["psi0"] = [1, 0, 0]
+    with pytest.raises(ValueError, match="wavefunction"):
+        D.parse_input(bad)
+    bad = dict(g[WITH_BONDS[0]]["input"])
+    bad["bath"] = {"type": "lorentzian", "wc": 1.0}
+    with pytest.raises(ValueError, match="unknown bath"):
+        D.parse_input(bad)
+
+
+@pytest.mark.parametrize("case", WITH_BONDS)
+def test_tree_matches_the_reference_example(case):
+    """The bond dimension of every node on the first output row: pins the frequency
+    window, the Gauss nodes (they decide how many modes share a block), the partition
+    and the tree builder with its level-dependent bond dimensions."""
+    v = _golden()[case]
+    inp = D.parse_input(v["input"])
+    wk, gk = D.bath_modes(inp)
+    blocks = D.make_blocks(inp, wk, gk)
+    topo = D.driver_topology(inp.hsys.shape[0], [b.nstates for b in blocks], inp.nspf, inp.nspf_lower)
+    assert np.array_equal(topo.hrank[1:], np.array(v["rows"][0]["hrank"]))
+
+
+@pytest.mark.parametrize("case", sorted(json.load(open(GOLDEN))))
+def test_output_rows_are_formatted_like_the_reference(case):
+    v = _golden()[case]
+    r0, r1 = v["rows"][0], v["rows"][1]
+    assert D.format_row(r0["t"], r0["values"], None, None, r0["hrank"] or None) == v["text"][0]
+    assert D.format_row(r1["t"], r1["values"], r1["counts"], r1["nh_per_node"], r1["hrank"] or None) == v["text"][1]
+    assert D.nsteps_for(5.0, 5e-3) == 1000 and D.nsteps_for(0.0105, 5e-3) == 3
+
+
+def test_first_step_matches_the_reference_example():
+    """The oracle stepping the driver's model of beta_10/ohmic/spin_boson_debye (343
+    blocks, 687 nodes) from the driver's start state: after one step the observables
+    agree with the reference's printed values to 1e-8; the two-site expansion count (which
+    includes the start-up expansion sweeps) to 2 %; and almost every bond dimension.  The
+    reference finds the dominant two-site directions with a 12-vector Krylov eigensolver
+    and this build with an exact eigensolver, so the bonds that sit at the spawning
+    threshold can differ by one."""
+    from oracle.oracle import Oracle
+    v = _golden()[WITH_BONDS[0]]
+    inp = D.parse_input(v["input"])
+    m = D.build_model(inp)
+    orc = Oracle(m.topology, m.hamiltonian, krylov_dim=inp.krylov_dim, krylov_tol=inp.krylov_tolerance)
+    orc.init_product(inp.psi0, inp.seed)
+    for (r0, x) in zip(v["rows"][0]["values"], [orc.expect(0, op).real for op in inp.ops]):
+        assert abs(r0 - x) < 1e-14
+    orc.set_expansion(m.capacity, spawning_threshold=inp.spawning_parameter,
+                      unoccupied_threshold=inp.unoccupied_threshold, minimum_unoccupied=inp.minimum_unoccupied, seed=0)
+    orc.step(inp.dt)
+    row = v["rows"][1]
+    vals = [orc.expect(0, op).real for op in inp.ops]
+    assert np.max(np.abs(np.array(vals) - row["values"])) < 1e-8
+    one, two = orc.expansion_counts()
+    assert one == row["counts"][0]
+    assert abs(two - row["counts"][1]) <= 0.02 * row["counts"][1]
+    hr = orc.hrank()[1:]
+    ref = np.array(row["hrank"])
+    assert np.mean(hr == ref) > 0.95 and np.max(np.abs(hr - ref)) <= 2
+
+
+# ---- bath discretisation ------------------------------------------------------------
+
+def test_gauss_rule_of_a_jacobi_measure_is_gauss_jacobi():
+    """J(w) = c (w/wc)^s (1 - w/wc)^q on [0, wc] is a Jacobi weight: its Gauss rule is the
+    Gauss-Jacobi rule (both endpoints singular, exercising the Gauss-Jacobi panels)."""
+    from scipy.special import roots_jacobi
+    b = B.JacobiCutoff(alpha=0.7, wc=3.0, s=0.5, q=1.5)
+    N = 40
+    w, W = B.gauss_rule(b, 0.0, 3.0, N)
+    t, tw = roots_jacobi(N, 1.5, 0.5)   # weight (1 - t)^1.5 (1 + t)^0.5
+    x = 1.5 * (1.0 + t)
+    c = b._pref() * b.wc / b.wc ** b.s / b.wc ** b.q   # J = c w^s (wc - w)^q
+    Wx = c * tw * 1.5 ** (1.0 + b.s + b.q)
+    assert np.allclose(np.sort(w), np.sort(x), rtol=0, atol=1e-12)
+    assert np.allclose(W[np.argsort(w)], Wx[np.argsort(x)], rtol=1e-11)
+
+
+@pytest.mark.parametrize("bath,lo,hi", [
+    (B.Exponential(2.0, 25.0, 1.0), 0.0, 500.0),
+    (B.Exponential(2.0, 25.0, 0.5), 0.0, 172.7),
+    (B.Debye(2.0, 25.0, beta=10.0), -2.0, 500.0),
+    (B.Sudden(2.0, 25.0, 1.0, beta=10.0), -1.0, 25.0),
+])
+def test_gauss_rule_integrates_polynomials_exactly(bath, lo, hi):
+    """sum_k W_k p(w_k) = int p dmu for p = Chebyshev polynomials of the window up to
+    degree 2N - 1 (mu = J, or J / (1 - exp(-beta w)) at finite temperature)."""
+    from scipy.integrate import quad
+    N = 64
+    w, W = B.gauss_rule(bath, lo, hi, N)
+    assert np.all(W > 0) and np.all(np.diff(w) > 0) and lo < w[0] and w[-1] < hi
+    y = (2.0 * w - (hi + lo)) / (hi - lo)
+    pts = sorted({p for p, *_ in bath.breakpoints() if lo < p < hi} | ({0.0} if lo < 0 < hi else set()))
+    for k in (0, 1, 7, 40, 2 * N - 1):
+        f = lambda x: float(bath.measure(np.float64(x))) * math.cos(k * math.acos(max(-1.0, min(1.0, (2 * x - hi - lo) / (hi - lo)))))
+        exact = quad(f, lo, hi, points=pts or None, limit=2000, epsabs=0, epsrel=1e-13)[0]
+        got = float(np.sum(W * np.cos(k * np.arccos(np.clip(y, -1, 1)))))
+        assert abs(got - exact) <= 1e-10 * float(np.sum(W)), k
+
+
+def test_frequency_window_and_couplings():
+    b = B.Exponential(2.0, 25.0, 1.0, beta=10.0)
+    lo, hi = b.frequency_bounds(1e-3)
+    assert hi == pytest.approx(25.0 * math.log(1000.0), rel=1e-15)
+    # the negative bound keeps 1 - tol of the Boltzmann-weighted density
+    from scipy.integrate import quad
+    rho = lambda x: float(b.density(np.float64(x))) * math.exp(-10.0 * x)
+    tot = quad(rho, 0, hi, epsrel=1e-13)[0]
+    assert quad(rho, 0, -lo, epsrel=1e-13)[0] == pytest.approx((1 - 1e-3) * tot, rel=1e-10)
+    w, g = B.discretise(b, 32, lo, hi)
+    assert lo < 0 and np.all(np.diff(np.abs(w)) >= 0) and w.min() >= lo
+    assert np.sum(math.pi * g ** 2) == pytest.approx(quad(lambda x: float(b.measure(np.float64(x))), lo, hi, points=[0.0],
+                                                          epsrel=1e-13)[0], rel=1e-10)
+    d = B.Debye(alpha=0.0, wc=4.0)
+    assert B.load_bath({"type": "Debye", "wc": 4.0, "lambda": 2.0}).alpha == pytest.approx(1.0)
+    assert B.load_bath({"type": "exponential", "wc": 1, "alpha": 1, "s": 1, "T": 0}).beta is None
+    assert B.load_bath({"type": "exponential", "wc": 1, "alpha": 1, "s": 1, "T": 0.5}).beta == 2.0
+    assert d.upper_bound(0.08) == pytest.approx(4.0 * math.tan(0.92 * math.pi / 2))
+
+
+# ---- blocks ---------------------------------------------------------------------------
+
+def test_block_operators_are_the_harmonic_ones():
+    """A two-mode block: H0 = sum w_j n_j and Hc = sum g_j (a_j + a_j^dagger) in the
+    product basis, first mode slowest, against Kronecker products."""
+    wk = np.array([10.0, 11.0])
+    gk = np.array([0.3, 0.7])
+    blk = D.make_block(wk, gk, 3000.0, 5)
+    assert blk.nstates == 25
+    a = np.diag(np.sqrt(np.arange(1, 5)), 1)
+    n = np.diag(np.arange(5.0))
+    I = np.eye(5)
+    H0 = wk[0] * np.kron(n, I) + wk[1] * np.kron(I, n)
+    Hc = gk[0] * np.kron(a + a.T, I) + gk[1] * np.kron(I, a + a.T)
+    assert np.allclose(np.diag(blk.h0), H0)
+    assert np.allclose(blk.hc_dense(), Hc)
+    # the first row's entries: lowering in mode order, then raising in reverse mode order
+    assert list(blk.hc_indices[blk.hc_indptr[6]:blk.hc_indptr[7]]) == [1, 5, 7, 11]
+
+
+def test_block_dimension_follows_its_lowest_frequency():
+    """Every mode of a block keeps the first (lowest) mode's count, so the block holds
+    nper(w_0)^n states; when a later mode keeps fewer, the rows past the product basis
+    have no energy and no coupling."""
+    wk = np.array([300.0, 340.0])          # floor(3000/w) = 10, 8
+    blk = D.make_block(wk, np.array([0.1, 0.2]), 3000.0, 10)
+    assert blk.nstates == 100 and blk.occupations.shape[0] == 80
+    H = blk.hc_dense()
+    assert np.allclose(H, H.T) and not np.any(H[80:]) and not np.any(blk.h0[80:])
+
+
+def test_partition_groups_modes_under_the_target_dimension():
+    """Blocks grow from the lowest frequency while nper(w_first)^n stays under the target:
+    low modes keep 30 states (900 <= 1000 < 27000: pairs), modes above wc = 50 keep
+    min(10, floor(3000 / w)) (pairs of 10 or 9, triples of 6 for w >= 430)."""
+    wk = np.array([0.5, 1.0, 2.0, 60.0, 300.0, 310.0, 320.0, 430.0, 440.0, 450.0])
+    assert D.partition_modes(wk, 3000.0, 50.0, 1000, 250, 30, 10) == [2, 2, 2, 2, 2]
+    assert D.partition_modes(np.array([430.0, 440.0, 450.0, 460.0]), 3000.0, 50.0, 1000, 250, 30, 10) == [3, 1]
+    # a lone mode above the target still forms a block
+    assert D.partition_modes(np.array([0.1, 0.2]), 3000.0, 50.0, 20, 250, 30, 10) == [1, 1]
+    with pytest.raises(ValueError):
+        D.partition_modes(wk[::-1], 3000.0, 50.0, 1000, 250, 30, 10)
+
+
+def test_level_ranks_interpolate_geometrically():
+    f = D.level_ranks(8, 4, 8)
+    assert [f(l) for l in range(10)] == [8, 7, 6, 6, 5, 5, 4, 4, 4, 4]
+    g = D.level_ranks(4, 4, 3)
+    assert [g(l) for l in range(5)] == [4, 4, 4, 4, 4]

@@ -77,6 +77,7 @@ SIGNATURES = {
     "ttn_integrator_t": (_I, [_P, _DP]),
     "ttn_integrator_step": (_I, [_P, _P, _D, _D, _DP]),
     "ttn_integrator_nh_applications": (_I, [_P, _LLP]),
+    "ttn_integrator_expansion_counts": (_I, [_P, _LLP, _LLP]),
     "ttn_integrator_reset": (_I, [_P]),
     "ttn_integrator_synchronize": (_I, [_P]),
     "ttn_integrator_prepare": (_I, [_P, _P]),
@@ -349,6 +350,12 @@ class fixed_step_projector_splitting_integrator:
         out = C.c_longlong()
         _check(lib().ttn_integrator_nh_applications(self.h, C.byref(out)))
         return out.value
+
+    def expansion_counts(self):
+        """(Nonesite, Ntwosite): one-site and two-site subspace expansions so far."""
+        a, b = C.c_longlong(), C.c_longlong()
+        _check(lib().ttn_integrator_expansion_counts(self.h, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
 
     def prepare(self, A: httensor):
         _check(lib().ttn_integrator_prepare(self.h, A.h))

@@ -437,8 +437,8 @@ struct DevExpander {
           for (auto& z : f[j]) z = std::conj(z);
         }
         grow(S, C, f, {}, true);
-        ++n_twosite;
       }
+      ++n_twosite;  // down counts every two-site attempt
     } else {
       while (nadd < required) {
         const std::vector<cd> x = random_orthogonal((size_t)outer, parent_slices(S, C));
@@ -480,7 +480,7 @@ struct DevExpander {
       if (nadd) {
         U.resize(nadd);
         grow(S, C, {}, U, false);
-        ++n_twosite;
+        ++n_twosite;  // up counts only the attempts that grew the bond
       }
     } else {
       while (nadd < required) {

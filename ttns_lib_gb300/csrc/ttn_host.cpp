@@ -1844,6 +1844,13 @@ int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out) {
   *out = it->I.nh;
   TTN_API_END
 }
+int ttn_integrator_expansion_counts(const ttn_integrator* it, long long* onesite, long long* twosite) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && onesite && twosite, TTN_EINVAL, "null argument");
+  *onesite = it->X ? it->X->n_onesite : 0;
+  *twosite = it->X ? it->X->n_twosite : 0;
+  TTN_API_END
+}
 // ---- checkpoints: integrator scalars and the state in one little-endian file
 namespace {
 const char kCkptMagic[8] = {'T', 'T', 'N', 'C', 'K', 'P', 'T', '1'};

@@ -242,3 +242,48 @@ def test_host_orchestration_matches_oracle():
             assert v["J"] < 1e-12, (k, v)
             assert v["coeff"] < 1e-10 and v["ops"] < 1e-10 and v["state"] < 1e-10, (k, v)
             assert v["final"] < 1e-11, (k, v)
+
+
+DRIVER_CHILD = r"""
+import json, sys
+import numpy as np
+sys.path.insert(0, {root!r})
+from ttns_lib_gb300 import api
+api.LIB_PATH = {lib!r}
+from ttns_lib_gb300 import driver as D
+from oracle.oracle import Oracle
+g = json.load(open({golden!r}))
+doc = dict(g["beta_10/ohmic/spin_boson_sudden"]["input"]); doc["nmodes"] = 16
+inp = D.parse_input(doc)
+m = D.build_model(inp)
+r = D.SpinBosonRun(inp, m, device=0)
+orc = Oracle(m.topology, m.hamiltonian, krylov_dim=inp.krylov_dim, krylov_tol=inp.krylov_tolerance)
+orc.init_product(inp.psi0, inp.seed)
+orc.set_expansion(m.capacity, spawning_threshold=inp.spawning_parameter, unoccupied_threshold=inp.unoccupied_threshold,
+                  minimum_unoccupied=inp.minimum_unoccupied, seed=0)
+out = dict(first=r.first_row(), start=float(max(np.max(np.abs(a - b)) for a, b in zip(r.A.get(), orc.get_state()))),
+           steps=[])
+for k in range(2):
+    r.step(); orc.step(inp.dt)
+    out["steps"].append(dict(values=float(max(abs(a - orc.expect(0, op).real) for a, op in zip(r.observables(), inp.ops))),
+                             counts=[list(r.tdvp.expansion_counts()), list(orc.expansion_counts())],
+                             hrank=bool(np.array_equal(r.hrank(), orc.hrank()[1:]))))
+print(json.dumps(out))
+"""
+
+
+def test_driver_device_path_matches_oracle():
+    """The spin-boson driver's device path (start state, expansion set-up, steps, leaf
+    observables, expansion counters) on the test double against the oracle, on a 16-mode
+    version of the reference's sudden-cutoff example: the same start state bit for bit,
+    the same bond dimensions and counts, observables to rounding."""
+    lib = _build()
+    code = DRIVER_CHILD.format(root=ROOT, lib=lib, golden=os.path.join(ROOT, "tests", "golden", "driver_examples.json"))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-3000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    assert res["first"].startswith("0 0 0 1 1  0 0 0 2 2 ")
+    assert res["start"] == 0.0
+    for s in res["steps"]:
+        assert s["values"] < 1e-11 and s["hrank"], s
+        assert s["counts"][0] == s["counts"][1], s

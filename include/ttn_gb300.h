@@ -202,6 +202,13 @@ int ttn_integrator_set_expansion(ttn_integrator* it, ttn_state* psi, const int* 
                                  int only_when_no_unoccupied, unsigned seed);
 /* current bond dimension above every node (out[nnodes]) */
 int ttn_state_hrank(const ttn_state* s, int* out);
+/* orthogonaliser::operator() (include/ttns_lib/decompositions/orthogonaliser.hpp:83-112):
+ * makes every non-root node of psi an isometry (children before parents: A = Q R, A <- Q,
+ * R into the parent's slot), leaving the state unchanged and its norm at the root, so
+ * that an arbitrary, non-orthogonal state can be stepped.  Uses the integrator's device
+ * QR; psi must have the integrator's tree.  After the first step the integrator's
+ * environments are refreshed for the new gauge. */
+int ttn_state_orthogonalise(ttn_integrator* it, ttn_state* psi);
 
 /* ---- adjoint sweep ----------------------------------------------------------------- */
 /* Gradient of J = sum_k weights[k] Re <psi(t_k)| O_mode |psi(t_k)>, t_k the end of step k,

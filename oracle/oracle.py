@@ -69,6 +69,7 @@ def lib():
         L.orc_expand_prepare.argtypes = [P, C.c_double, ip]
         L.orc_expansion_counts.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
         L.orc_init_product.argtypes = [P, dp, C.c_uint]
+        L.orc_orthogonalise.argtypes = [P]
         L.orc_adjoint.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_int, dp, C.c_int, dp, C.c_int, C.c_int,
                                   dp, dp, dp, dp]
         _lib = L
@@ -198,6 +199,10 @@ class Oracle:
         a, b = C.c_longlong(), C.c_longlong()
         self._check(lib().orc_expansion_counts(self.h, C.byref(a), C.byref(b)))
         return int(a.value), int(b.value)
+
+    def orthogonalise(self):
+        """Every non-root node made an isometry, the rest carried to the root."""
+        self._check(lib().orc_orthogonalise(self.h))
 
     def init_product(self, psi0=None, seed: int = 0):
         """The spin-boson driver's start state drawn with std::mt19937(seed)."""

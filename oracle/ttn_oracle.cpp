@@ -1149,6 +1149,18 @@ struct Engine {
     for (int id = T.n - 1; id >= 1; --id) update_spf(id);
     for (int id = 1; id < T.n; ++id) update_mf(id);
   }
+  // orthogonaliser::operator() (include/ttns_lib/decompositions/orthogonaliser.hpp:83-112):
+  // children before parents, every non-root node A = Q R, A <- Q and R into the parent's
+  // slot, so that every non-root node is an isometry and the root holds the norm; the
+  // single-particle environments follow the new gauge when the run has started
+  void orthogonalise() {
+    for (int id = T.n - 1; id >= 1; --id) {
+      l2r(id);
+      apply_to_parent(id);
+    }
+    if (nsteps > 0)
+      for (int id = T.n - 1; id >= 1; --id) update_spf(id);
+  }
 };
 
 #include "ttn_adjoint.hpp"
@@ -1350,6 +1362,10 @@ int orc_prepare(void* p) {
 }
 double orc_t(void* p) { OrcHandle* h = (OrcHandle*)p; return h->E.nsteps * h->E.dt; }
 long long orc_nh(void* p) { return ((OrcHandle*)p)->E.nh; }
+int orc_orthogonalise(void* p) {
+  OrcHandle* h = (OrcHandle*)p;
+  ORC_TRY(h, { h->E.orthogonalise(); })
+}
 // one-site and two-site expansions so far (subspace_expansion_projector_splitting_engine
 // Nonesite / Ntwosite, include/ttns_lib/tdvp_core/subspace_expansion_projector_splitting_
 // engine.hpp:513-514); zero without expansion

@@ -221,6 +221,23 @@ it_.dt = 0.05
 for _ in range(6):
     it_(At); orc.step(0.05)
 out["plain_time_dependent"] = float(max(np.max(np.abs(a - b)) for a, b in zip(At.get(), orc.get_state())))
+# the orthogonaliser on an arbitrary state, then steps, against the oracle
+rng = np.random.default_rng(21)
+st = [rng.normal(size=t.shape) + 1j * rng.normal(size=t.shape) for t in generic_state(mt.topology, rng)]
+from ttns_lib_gb300.model import full_state
+st[0] = st[0] / np.linalg.norm(full_state(mt.topology, st))
+orc = Oracle(mt.topology, mt.sop, krylov_dim=10, krylov_tol=1e-12); orc.set_state(st); orc.orthogonalise()
+Ao = api.httensor(mt.topology, device=0); Ao.set(st)
+io = api.fixed_step_projector_splitting_integrator(Ao, mt.sop, krylov_dim=10)
+io.orthogonalise(Ao)
+out["plain_orthogonalise"] = float(max(np.max(np.abs(a - b)) for a, b in zip(Ao.get(), orc.get_state())))
+io.dt = 0.05
+for _ in range(3):
+    io(Ao); orc.step(0.05)
+io.orthogonalise(Ao); orc.orthogonalise()
+for _ in range(2):
+    io(Ao); orc.step(0.05)
+out["plain_orthogonalise_steps"] = float(max(np.max(np.abs(a - b)) for a, b in zip(Ao.get(), orc.get_state())))
 print(json.dumps(out))
 """
 

@@ -155,3 +155,28 @@ def test_time_dependent_operators_converge_to_driven_dynamics():
         errs.append(np.linalg.norm(full_state(topo, orc.get_state()) - x))
     assert errs[1] < 1e-6
     assert 3.0 < errs[0] / errs[1] < 5.0
+
+
+def test_orthogonaliser_keeps_the_state_and_makes_isometries():
+    """orthogonaliser (include/ttns_lib/decompositions/orthogonaliser.hpp:83-112) on an
+    arbitrary state of a random tree: the full state vector is unchanged, every non-root
+    node is an isometry, and a full-rank tree then follows exp(-iHt)."""
+    from helpers import full_rank, generic_state, random_sop, random_tree
+    from ttns_lib_gb300.model import full_state
+    import scipy.linalg as sla
+    rng = np.random.default_rng(31)
+    topo = full_rank(random_tree(rng, [2, 3, 2, 2], max_children=3))
+    H = random_sop(rng, topo.mode_dims())
+    st = [rng.normal(size=t.shape) + 1j * rng.normal(size=t.shape) for t in generic_state(topo, rng)]
+    psi = full_state(topo, st)
+    orc = Oracle(topo, H, krylov_dim=12, krylov_tol=1e-13)
+    orc.set_state(st)
+    orc.orthogonalise()
+    got = orc.get_state()
+    assert np.linalg.norm(full_state(topo, got) - psi) < 1e-13 * np.linalg.norm(psi)
+    for t in got[1:]:
+        assert np.max(np.abs(t.conj().T @ t - np.eye(t.shape[1]))) < 1e-14
+    for _ in range(4):
+        orc.step(0.05)
+    ex = sla.expm(-1j * H.dense() * 0.2) @ psi
+    assert np.linalg.norm(full_state(topo, orc.get_state()) - ex) < 1e-9 * np.linalg.norm(psi)

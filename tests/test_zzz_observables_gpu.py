@@ -41,3 +41,33 @@ def test_overlap_product_and_sop_expectations_match_dense():
     H = m.sop.dense()
     assert abs(mel.sop(m.sop, A, B) - np.vdot(fa, H @ fb)) < 1e-11
     assert abs(mel.sop(m.sop, A) - np.vdot(fa, H @ fa)) < 1e-11
+
+
+def test_orthogonaliser_on_the_device():
+    """orthogonaliser(A) for an arbitrary (non-orthogonal) state: the state is unchanged,
+    every non-root node becomes an isometry, the tensors equal the oracle's (same
+    Householder gauge), and stepping afterwards follows the oracle."""
+    from oracle.oracle import Oracle
+    m = sb.build(N=4, alpha=0.5, wc=5.0, d=3, chi=3, eps=0.3, delta=1.0)
+    topo = m.topology
+    rng = np.random.default_rng(21)
+    st = [rng.normal(size=t.shape) + 1j * rng.normal(size=t.shape) for t in generic_state(topo, rng)]
+    st[0] = st[0] / np.linalg.norm(full_state(topo, st))
+    psi = full_state(topo, st)
+    A = api.httensor(topo)
+    A.set(st)
+    integ = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=10, krylov_tolerance=1e-13)
+    integ.orthogonalise(A)
+    got = A.get()
+    assert np.linalg.norm(full_state(topo, got) - psi) < 1e-12 * np.linalg.norm(psi)
+    for t in got[1:]:
+        assert np.max(np.abs(t.conj().T @ t - np.eye(t.shape[1]))) < 1e-13
+    orc = Oracle(topo, m.sop, krylov_dim=10, krylov_tol=1e-13)
+    orc.set_state(st)
+    orc.orthogonalise()
+    assert max(np.max(np.abs(a - b)) for a, b in zip(got, orc.get_state())) < 1e-12
+    integ.dt = 0.05
+    for _ in range(3):
+        integ(A)
+        orc.step(0.05)
+    assert max(np.max(np.abs(a - b)) for a, b in zip(A.get(), orc.get_state())) < 1e-10

@@ -78,6 +78,7 @@ SIGNATURES = {
     "ttn_integrator_step": (_I, [_P, _P, _D, _D, _DP]),
     "ttn_integrator_nh_applications": (_I, [_P, _LLP]),
     "ttn_integrator_expansion_counts": (_I, [_P, _LLP, _LLP]),
+    "ttn_state_orthogonalise": (_I, [_P, _P]),
     "ttn_integrator_reset": (_I, [_P]),
     "ttn_integrator_synchronize": (_I, [_P]),
     "ttn_integrator_prepare": (_I, [_P, _P]),
@@ -350,6 +351,10 @@ class fixed_step_projector_splitting_integrator:
         out = C.c_longlong()
         _check(lib().ttn_integrator_nh_applications(self.h, C.byref(out)))
         return out.value
+
+    def orthogonalise(self, A: httensor):
+        """orthogonaliser(A): every non-root node of A made an isometry, the state unchanged."""
+        _check(lib().ttn_state_orthogonalise(self.h, A.h))
 
     def expansion_counts(self):
         """(Nonesite, Ntwosite): one-site and two-site subspace expansions so far."""

@@ -1295,6 +1295,17 @@ struct Integrator {
     forward(S, false);
     backward(S, false);
   }
+  // orthogonaliser::operator() (include/ttns_lib/decompositions/orthogonaliser.hpp:83-112):
+  // children before parents, A = Q R on the device, A <- Q, R applied to the parent's slot;
+  // the single-particle environments follow the new gauge once the run has started
+  void orthogonalise(ttn_state* S) {
+    for (int id = T.n - 1; id >= 1; --id) {
+      l2r(id, S->node(id));
+      apply_to_parent(id, S->node(T.parent[id]), T.parent[id]);
+    }
+    if (nsteps > 0)
+      for (int id = T.n - 1; id >= 1; --id) update_spf(id, S->node(id));
+  }
   void step(ttn_state* S, double step_dt, cd cf) {
     if (expanding_step) {
       expanding_step(S, step_dt, cf);
@@ -1842,6 +1853,17 @@ int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out) {
   TTN_API_BEGIN
   TTN_REQUIRE(it && out, TTN_EINVAL, "null argument");
   *out = it->I.nh;
+  TTN_API_END
+}
+int ttn_state_orthogonalise(ttn_integrator* it, ttn_state* psi) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && psi, TTN_EINVAL, "null argument");
+  TTN_REQUIRE(psi->T.n == it->I.T.n, TTN_EINVAL, "state and integrator trees differ");
+  for (int i = 0; i < it->I.T.n; ++i)
+    TTN_REQUIRE(psi->T.hrank[i] == it->I.T.hrank[i] && psi->T.dimen[i] == it->I.T.dimen[i], TTN_EINVAL,
+                "state and integrator trees differ");
+  it->I.orthogonalise(psi);
+  it->I.finish_check(psi);
   TTN_API_END
 }
 int ttn_integrator_expansion_counts(const ttn_integrator* it, long long* onesite, long long* twosite) {

@@ -205,3 +205,56 @@ def test_level_ranks_interpolate_geometrically():
     assert [f(l) for l in range(10)] == [8, 7, 6, 6, 5, 5, 4, 4, 4, 4]
     g = D.level_ranks(4, 4, 3)
     assert [g(l) for l in range(5)] == [4, 4, 4, 4, 4]
+
+
+def _small_driver_model():
+    from helpers import full_rank
+    doc = {"Hsys": [[0, 1], [1, 0]], "Scoup": [[1, 0], [0, -1]], "psi0": [1, 0],
+           "bath": {"type": "exponential", "wc": 2.0, "alpha": 0.2, "s": 1},
+           "max frequency cutoff": 6.0, "tmax": 1.0, "dt": 0.05, "nspf": 2, "nspf lower": 2,
+           "nmodes": 4, "maximum dimension": 5, "target dimension": 5, "ops": [[1, 0], [0, -1]]}
+    inp = D.parse_input(doc)
+    wk, gk = D.bath_modes(inp)
+    blocks = D.make_blocks(inp, wk, gk)
+    topo = full_rank(D.driver_topology(2, [b.nstates for b in blocks], 2, 2))
+    return inp, blocks, topo
+
+
+def test_interaction_picture_coupling_converges_to_the_schroedinger_picture():
+    """interaction_picture_sb_operator through the time-dependent operator hook: without
+    the bath's H0 and with each block's coupling averaged over every evolution interval,
+    <sz>(t) converges at second order or better to exact dense Schroedinger-picture
+    dynamics (full-rank tree, so the only error is the time dependence), and the averaged
+    couplings are the interval means of g exp(i w s) (the end-point value below
+    |w dt| = 1e-5, as the reference computes them)."""
+    import scipy.linalg as sla
+    from scipy.integrate import quad
+    from oracle.oracle import Oracle
+    from ttns_lib_gb300.model import full_state
+    inp, blocks, topo = _small_driver_model()
+    ip = D.InteractionPictureCoupling(blocks[1])
+    w, g = blocks[1].wk[0], blocks[1].gk[0]
+    mean = (quad(lambda s: math.cos(w * s), 0.3, 0.4)[0] + 1j * quad(lambda s: math.sin(w * s), 0.3, 0.4)[0]) / 0.1
+    assert abs(ip.averaged_couplings(0.3, 0.1)[0] - g * mean) < 1e-14
+    te = 0.3 + 1e-7  # below |w dt| = 1e-5 the reference's series gives the end-point value
+    assert abs(ip.averaged_couplings(0.3, 1e-7)[0] - g * complex(math.cos(w * te), math.sin(w * te))) < 1e-15
+    assert np.allclose(ip.matrix(0.0, 0.0), blocks[1].hc_dense())
+    HS = D.build_hamiltonian(inp, blocks)
+    HI, upd = D.build_interaction_picture_hamiltonian(inp, blocks)
+    o = Oracle(topo, HS, krylov_dim=12, krylov_tol=1e-13)
+    o.init_product(inp.psi0, 0)
+    st = o.get_state()
+    psi = full_state(topo, st)
+    ex = sla.expm(-1j * HS.dense() * 1.0) @ psi
+    sz = np.kron(np.diag([1.0, -1.0]), np.eye(len(psi) // 2))
+    ref = np.vdot(ex, sz @ ex).real
+    errs = []
+    for dt in (0.05, 0.025, 0.0125):
+        oi = Oracle(topo, HI, krylov_dim=12, krylov_tol=1e-13)
+        oi.set_state(st)
+        oi.set_op_update(upd)
+        for _ in range(int(round(1.0 / dt))):
+            oi.step(dt)
+        errs.append(abs(oi.expect(0, np.diag([1.0, -1.0])).real - ref))
+    assert errs[0] < 2e-4 and errs[2] < 5e-6
+    assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5

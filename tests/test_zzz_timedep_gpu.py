@@ -35,3 +35,35 @@ def test_driven_sweep_matches_oracle():
     assert abs(integ.mel()(sb.SZ, 0, A).real - orc.expect(0, sb.SZ).real) < 1e-10
     for a, b in zip(A.get(), orc.get_state()):
         assert np.max(np.abs(a - b)) < 1e-9
+
+
+def test_interaction_picture_coupling_matches_oracle():
+    """The driver's interaction-picture coupling (interaction_picture_sb_operator) through
+    the device hook: a four-block spin-boson model stepped on the device and by the oracle
+    with the same hook."""
+    from helpers import full_rank
+    from ttns_lib_gb300 import driver as D
+    doc = {"Hsys": [[0, 1], [1, 0]], "Scoup": [[1, 0], [0, -1]], "psi0": [1, 0],
+           "bath": {"type": "exponential", "wc": 2.0, "alpha": 0.2, "s": 1},
+           "max frequency cutoff": 6.0, "tmax": 1.0, "dt": 0.05, "nspf": 2, "nspf lower": 2,
+           "nmodes": 4, "maximum dimension": 5, "target dimension": 5, "ops": [[1, 0], [0, -1]]}
+    inp = D.parse_input(doc)
+    wk, gk = D.bath_modes(inp)
+    blocks = D.make_blocks(inp, wk, gk)
+    topo = full_rank(D.driver_topology(2, [b.nstates for b in blocks], 2, 2))
+    H, upd = D.build_interaction_picture_hamiltonian(inp, blocks)
+    st = generic_state(topo, np.random.default_rng(3))
+    orc = Oracle(topo, H, krylov_dim=12, krylov_tol=1e-13)
+    orc.set_state(st)
+    orc.set_op_update(upd)
+    A = api.httensor(topo)
+    A.set(st)
+    integ = api.fixed_step_projector_splitting_integrator(A, H, krylov_dim=12, krylov_tolerance=1e-13)
+    integ.set_op_update(upd)
+    integ.dt = 0.05
+    for _ in range(8):
+        integ(A, H, -1j)
+        orc.step(0.05)
+    assert abs(integ.mel()(sb.SZ, 0, A).real - orc.expect(0, sb.SZ).real) < 1e-10
+    for a, b in zip(A.get(), orc.get_state()):
+        assert np.max(np.abs(a - b)) < 1e-9

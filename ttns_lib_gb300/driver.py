@@ -399,6 +399,92 @@ def build_hamiltonian(inp: DriverInput, blocks: Sequence[Block], dense: bool = T
     return H
 
 
+class InteractionPictureCoupling:
+    """The coupling of one block in the interaction picture of its H0, for the
+    time-dependent operator hook (``set_op_update``): ``interaction_picture_sb_operator``
+    (src/system_bath_coupling_interaction_picture_operator.hpp:10-207, built from a block
+    by ``Hc_interact``, src/mode_data.hpp:315-320).
+
+    Before a leaf evolution over [t, t + dt] the matrix becomes
+    sum_j (gt_j a_j^dagger + conj(gt_j) a_j), where gt_j is g_j exp(i w_j s) averaged over
+    s in [t, t + dt]: g_j e^{i w_j t} (e^{i w_j dt} - 1) / (i w_j dt).  When |w_j dt| < 1e-5
+    the reference sums the 20-term series of e^x, x = i w_j dt, in place of (e^x - 1)/x, so
+    it uses the value at the end of the interval, g_j e^{i w_j (t + dt)}; that is kept (it
+    differs from the mean by less than 1e-5 |g_j| / 2).  The block's own H0 is left out of
+    the Hamiltonian (``build_interaction_picture_hamiltonian``).
+    """
+
+    def __init__(self, block: Block):
+        self.block = block
+        b = block
+        rows = np.repeat(np.arange(b.nstates), np.diff(b.hc_indptr))
+        cols = b.hc_indices
+        occ = b.occupations
+        n = occ.shape[1]
+        # classify every CSR entry: lowering (column = row - e_j, a^dagger element) or raising
+        mode = np.zeros(len(cols), dtype=np.int64)
+        up = np.zeros(len(cols), dtype=bool)
+        amp = np.zeros(len(cols))
+        stride = np.ones(n, dtype=np.int64)
+        per = [int(occ[:, j].max()) + 1 for j in range(n)] if occ.shape[0] else [1] * n
+        for j in range(n - 2, -1, -1):
+            stride[j] = stride[j + 1] * per[j + 1]
+        for q, (r, c) in enumerate(zip(rows, cols)):
+            diff = int(c) - int(r)
+            j = int(np.nonzero(stride == abs(diff))[0][0]) if n > 1 else 0
+            mode[q] = j
+            if diff < 0:            # <n|a_j^dagger|n - 1> = sqrt(n)
+                amp[q] = math.sqrt(float(occ[r, j]))
+            else:                   # <n|a_j|n + 1> = sqrt(n + 1)
+                up[q] = True
+                amp[q] = math.sqrt(float(occ[r, j] + 1))
+        self._rows, self._cols, self._mode, self._up, self._amp = rows, cols, mode, up, amp
+
+    def averaged_couplings(self, t: float, dt: float) -> np.ndarray:
+        w = self.block.wk
+        g = self.block.gk
+        out = np.zeros(len(w), dtype=np.complex128)
+        for i in range(len(w)):
+            ukt = complex(math.cos(w[i] * t), math.sin(w[i] * t))
+            x = 1j * w[i] * dt
+            if abs(w[i] * dt) < 1e-5:
+                s, f = 0.0 + 0.0j, 1.0 + 0.0j
+                for k in range(20):
+                    s += f
+                    f *= x / (k + 1.0)
+                out[i] = g[i] * ukt * s
+            else:
+                out[i] = g[i] * ukt * (complex(math.cos(w[i] * dt), math.sin(w[i] * dt)) - 1.0) / x
+        return out
+
+    def matrix(self, t: float, dt: float) -> np.ndarray:
+        gt = self.averaged_couplings(t, dt)
+        m = np.zeros((self.block.nstates, self.block.nstates), dtype=np.complex128)
+        vals = np.where(self._up, np.conj(gt[self._mode]), gt[self._mode]) * self._amp
+        m[self._rows, self._cols] = vals
+        return m
+
+
+def build_interaction_picture_hamiltonian(inp: DriverInput, blocks: Sequence[Block]):
+    """H(t) = Hsys + sum_b Scoup Hc_b(t) in the interaction picture of the bath (term 0 is
+    Hsys, term 1 + b couples block b) and the hook that updates every Hc_b(t); pass the
+    hook to ``set_op_update`` of the integrator (or of the oracle)."""
+    nb = len(blocks)
+    dims = [inp.hsys.shape[0]] + [b.nstates for b in blocks]
+    H = SOPOperator(1 + nb, dims)
+    H.bind_dense(inp.hsys, [0], 0)
+    H.bind_dense(inp.scoup, [1 + i for i in range(nb)], 0)
+    ops = [InteractionPictureCoupling(b) for b in blocks]
+    for i, op in enumerate(ops):
+        H.bind_dense(op.matrix(0.0, 0.0), [1 + i], i + 1)
+
+    def update(mode, op, t, dt, mat):
+        if mode >= 1:
+            mat[:] = ops[mode - 1].matrix(t, dt)
+
+    return H, update
+
+
 @dataclass
 class DriverModel:
     inp: DriverInput

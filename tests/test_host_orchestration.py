@@ -238,6 +238,26 @@ io.orthogonalise(Ao); orc.orthogonalise()
 for _ in range(2):
     io(Ao); orc.step(0.05)
 out["plain_orthogonalise_steps"] = float(max(np.max(np.abs(a - b)) for a, b in zip(Ao.get(), orc.get_state())))
+# bonds wider than the cooperative QR kernels (70 > 64): the wide QR route in both gauge moves
+import ctypes
+from ttns_lib_gb300.model import Topology
+tw = Topology(np.array([-1, 0, 1, 1, 0]), np.array([1, 70, 9, 9, 70]), np.array([-1, -1, 0, 1, 2]),
+              np.array([0, 0, 9, 9, 70]))
+rng = np.random.default_rng(41)
+Hw = random_sop(rng, tw.mode_dims(), nterms=6)
+sw = generic_state(tw, rng)
+orc = Oracle(tw, Hw, krylov_dim=10, krylov_tol=1e-12); orc.set_state(sw)
+Aw = api.httensor(tw, device=0); Aw.set(sw)
+iw = api.fixed_step_projector_splitting_integrator(Aw, Hw, krylov_dim=10)
+iw.dt = 0.05
+count = ctypes.CDLL({lib!r}).mock_wide_qr_count
+count.restype = ctypes.c_ulonglong
+before = count()
+for _ in range(2):
+    iw(Aw); orc.step(0.05)
+if count() - before < 6:
+    raise SystemExit("the wide QR route was not taken")
+out["plain_wide_bonds"] = float(max(np.max(np.abs(a - b)) for a, b in zip(Aw.get(), orc.get_state())))
 print(json.dumps(out))
 """
 

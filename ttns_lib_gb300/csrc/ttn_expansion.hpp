@@ -88,7 +88,7 @@ struct DevExpander {
 
   explicit DevExpander(Integrator& in) : I(in) {
     const size_t vb = align256((size_t)I.maxsize * sizeof(double2));
-    s_buf.alloc(vb * 6 + align256((size_t)kQrMaxCols * kQrMaxCols * sizeof(double2)));
+    s_buf.alloc(vb * 6 + align256((size_t)kMaxBond * kMaxBond * sizeof(double2)));
   }
   double2* scratch(int k) const { return reinterpret_cast<double2*>(static_cast<char*>(s_buf.p) + align256((size_t)I.maxsize * sizeof(double2)) * k); }
 

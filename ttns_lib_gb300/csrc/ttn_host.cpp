@@ -135,7 +135,7 @@ struct Tree {
       }
     }
     for (int i = 0; i < n; ++i) {
-      TTN_REQUIRE(hrank[i] <= kQrMaxCols, TTN_ENOTSUP, "bond dimensions above 64 are not supported by this build");
+      TTN_REQUIRE(hrank[i] <= kMaxBond, TTN_ENOTSUP, "bond dimensions above 256 are not supported by this build");
       if (!children[i].empty())
         for (int m = 0; m < nmodes[i]; ++m) {
           long long d2 = dims[i][m], d1 = dimen[i] * hrank[i] / d2;
@@ -425,6 +425,7 @@ struct Integrator {
   std::vector<double2*> rmat, mel;
   double2 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w4 = nullptr, *V = nullptr, *p = nullptr,
           *gws = nullptr, *qtau = nullptr, *scal = nullptr;
+  WideQr* wide = nullptr;  // cuSOLVER QR of matricisations wider than kQrMaxCols
   size_t gws_bytes = 0;
   long long maxsize = 0, ldv = 0;
   KrylovCtl* ctl = nullptr;
@@ -506,6 +507,7 @@ struct Integrator {
   bool expanded = false;
 
   ~Integrator() {
+    wide_qr_destroy(wide);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -634,6 +636,23 @@ struct Integrator {
       qtau = take(kQrMaxCols * sizeof(double2));
       scal = take(64 * sizeof(double2));
     }
+    // bonds wider than the cooperative QR kernels take: cuSOLVER workspace for every
+    // matricisation that can be wider (gauge moves towards the root and the leaves)
+    {
+      std::vector<long long> ms;
+      std::vector<int> ns;
+      for (int i = 0; i < T.n; ++i) {
+        if (i != 0 && Z.hrank[i] > kQrMaxCols) { ms.push_back((long long)Z.dimen[i]); ns.push_back(Z.hrank[i]); }
+        if (Z.leaf(i)) continue;  // root-to-leaf moves factor branch nodes only
+        for (int mu = 0; mu < Z.nmodes[i]; ++mu) {
+          const int d = Z.dims[i][mu];
+          if (d > kQrMaxCols) { ms.push_back((long long)Z.dimen[i] * Z.hrank[i] / d); ns.push_back(d); }
+        }
+      }
+      wide_qr_destroy(wide);
+      wide = nullptr;
+      if (!ns.empty()) CK(wide_qr_create(&wide, ms.data(), ns.data(), (int)ns.size(), stream));
+    }
   }
 
   // control block, events, cooperative-kernel state and the term programs
@@ -660,6 +679,8 @@ struct Integrator {
       expm_max_grid = std::max(1, expm_coop_max_grid(0));
       expm_max_grid_tc = std::max(1, expm_coop_max_grid(1));
       if (mixed) {
+        for (int i = 0; i < T.n; ++i)
+          TTN_REQUIRE(sizing().hrank[i] <= kQrMaxCols, TTN_ENOTSUP, "mixed precision takes bonds of at most 64");
         // the tensor-core contractions need sm_100-family tensor memory
         cudaDeviceProp prop{};
         CK(cudaGetDeviceProperties(&prop, device));
@@ -1178,6 +1199,11 @@ struct Integrator {
   // Householder QR on as many CTAs as the height allows (one row block per CTA)
   int qr_rows_per_cta = 32;  // rows of the matrix per CTA of the cooperative QR
   void qr(double2* M, long long m, int n, double2* R, int Rt) {
+    if (n > kQrMaxCols) {
+      TTN_REQUIRE(wide, TTN_EINVAL, "no workspace for a QR wider than 64 columns");
+      CK(householder_qr_wide(wide, M, m, n, R, Rt, stream));
+      return;
+    }
     int g = (int)std::max(1LL, std::min<long long>(m / qr_rows_per_cta, qr_max_grid));
     CK(householder_qr_blocked(M, m, n, R, Rt, qtau, qr_scratch, bar, status, g, stream));
   }
@@ -2480,8 +2506,26 @@ int ttn_debug_tc_gemm(const double* A, const double* B, double* D, int K, int N,
 }
 int ttn_debug_qr(int m, int n, double* a, double* r, int device) {
   TTN_API_BEGIN
-  TTN_REQUIRE(a && r && m >= n && n >= 1 && n <= ttn::kQrMaxCols, TTN_EINVAL, "bad QR shape");
+  TTN_REQUIRE(a && r && m >= n && n >= 1 && n <= ttn::kMaxBond, TTN_EINVAL, "bad QR shape");
   CK(cudaSetDevice(device));
+  if (n > ttn::kQrMaxCols) {
+    ttn::DevBuf wb;
+    wb.alloc(((size_t)m * n + (size_t)n * n) * sizeof(double2));
+    double2* dA = wb.as<double2>();
+    double2* dR = dA + (size_t)m * n;
+    CK(cudaMemcpy(dA, a, (size_t)m * n * sizeof(double2), cudaMemcpyHostToDevice));
+    long long mm = m;
+    ttn::WideQr* q = nullptr;
+    CK(ttn::wide_qr_create(&q, &mm, &n, 1, 0));
+    cudaError_t e = ttn::householder_qr_wide(q, dA, m, n, dR, 0, 0);
+    cudaError_t e2 = cudaDeviceSynchronize();
+    ttn::wide_qr_destroy(q);
+    CK(e);
+    CK(e2);
+    CK(cudaMemcpy(a, dA, (size_t)m * n * sizeof(double2), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(r, dR, (size_t)n * n * sizeof(double2), cudaMemcpyDeviceToHost));
+    return TTN_OK;
+  }
   ttn::DevBuf buf;
   buf.alloc(((size_t)m * n + (size_t)n * n + ttn::kQrMaxCols) * sizeof(double2));
   double2* dA = buf.as<double2>();

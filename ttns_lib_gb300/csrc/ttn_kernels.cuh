@@ -59,7 +59,8 @@ struct KrylovCtl {
   long long napps;       // H applications (including the error-estimate one)
 };
 
-constexpr int kQrMaxCols = 64;   // widest matrix the device QR accepts
+constexpr int kQrMaxCols = 64;   // widest matrix the cooperative device QR kernels accept
+constexpr int kMaxBond = 256;    // widest bond of the FP64 sweep (QRs above kQrMaxCols: ttn_qr_wide.cu)
 constexpr int kKrylovMax = 64;   // largest Krylov dimension
 
 // ---- Householder QR --------------------------------------------------------------
@@ -81,6 +82,14 @@ size_t qr_blocked_scratch_bytes(int max_grid);
 int qr_blocked_max_grid();
 cudaError_t householder_qr_blocked(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws,
                                    double* scratch, GridBarrier* bar, int* err, int grid, cudaStream_t s);
+// QR of matrices with kQrMaxCols < n <= kMaxBond (cuSOLVER zgeqrf / zungqr on a
+// column-major copy; same conventions and arguments as householder_qr_coop).  The
+// workspace is sized at creation for the (m, n) shapes listed; a later call with a
+// larger shape returns cudaErrorInvalidValue.
+struct WideQr;
+cudaError_t wide_qr_create(WideQr** out, const long long* ms, const int* ns, int nshapes, cudaStream_t s);
+void wide_qr_destroy(WideQr* q);
+cudaError_t householder_qr_wide(WideQr* q, double2* M, long long m, int n, double2* R, int Rt, cudaStream_t s);
 // r2l matricisation: M(y*pre + x, i) = A((x*dm + i)*post + y) and its inverse.
 void permute_mode_last(const double2* A, double2* M, long long pre, int dm, long long post, cudaStream_t s);
 void unpermute_mode_last(const double2* M, double2* A, long long pre, int dm, long long post, cudaStream_t s);

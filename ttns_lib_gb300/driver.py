@@ -36,7 +36,7 @@ from .model import SOPOperator, Topology, _flatten, _NTree
 
 ECUT = 3000.0          # energy cutoff of a combined block basis (spin_boson.cpp:242)
 NMAX_HIGH_TARGET = 250  # target block dimension above twice the high-frequency bound (:418)
-MAX_BOND = 64           # widest bond of the device build (kQrMaxCols, csrc/ttn_kernels.cuh)
+MAX_BOND = 256          # widest bond of the device build (kMaxBond, csrc/ttn_kernels.cuh)
 
 
 # --------------------------------------------------------------------------------------

@@ -295,24 +295,24 @@ def make_block(wk: np.ndarray, gk: np.ndarray, ecut: float, nmax: int) -> Block:
     stride = np.ones(n, dtype=np.int64)
     for j in range(n - 2, -1, -1):
         stride[j] = stride[j + 1] * per[j + 1]
+    # entries (row, order within the row, column, value): lowering entries in mode order,
+    # then raising entries in reverse mode order; row i of the product basis is i itself
+    rows, keys, cols, vals = [], [], [], []
+    idx = np.arange(P, dtype=np.int64)
+    for j in range(n):
+        lo = occ[:, j] > 0
+        rows.append(idx[lo]); keys.append(np.full(int(lo.sum()), j)); cols.append(idx[lo] - stride[j])
+        vals.append(np.sqrt(occ[lo, j].astype(np.float64)) * gk[j])
+        up = occ[:, j] + 1 < per[j]
+        rows.append(idx[up]); keys.append(np.full(int(up.sum()), 2 * n - 1 - j)); cols.append(idx[up] + stride[j])
+        vals.append(np.sqrt(occ[up, j].astype(np.float64) + 1.0) * gk[j])
+    rows, keys, cols, vals = (np.concatenate(a) for a in (rows, keys, cols, vals))
+    order = np.lexsort((keys, rows))
     indptr = np.zeros(nstates + 1, dtype=np.int64)
-    indices: List[int] = []
-    data: List[float] = []
-    for i in range(nstates):
-        if i < P:
-            row = occ[i]
-            base = int(row @ stride)
-            for j in range(n):
-                if row[j] > 0:
-                    indices.append(base - int(stride[j]))
-                    data.append(math.sqrt(float(row[j])) * gk[j])
-            for j in range(n - 1, -1, -1):
-                if row[j] + 1 < per[j]:
-                    indices.append(base + int(stride[j]))
-                    data.append(math.sqrt(float(row[j] + 1)) * gk[j])
-        indptr[i + 1] = len(indices)
-    return Block(wk, gk, int(nmax), int(nstates), occ, h0, indptr, np.asarray(indices, dtype=np.int64),
-                 np.asarray(data, dtype=np.float64))
+    indptr[1:P + 1] = np.cumsum(np.bincount(rows, minlength=P))
+    indptr[P + 1:] = indptr[P]
+    return Block(wk, gk, int(nmax), int(nstates), occ, h0, indptr, cols[order].astype(np.int64),
+                 vals[order].astype(np.float64))
 
 
 def make_blocks(inp: DriverInput, wk: np.ndarray, gk: np.ndarray) -> List[Block]:

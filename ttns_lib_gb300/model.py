@@ -239,10 +239,10 @@ class SOPOperator:
 
     def bind_csr(self, indptr, indices, data, terms, mode: int):
         d = self.mode_dims[mode]
+        indptr = np.asarray(indptr, dtype=np.int64)
+        rows = np.repeat(np.arange(d), np.diff(indptr[:d + 1]))
         m = np.zeros((d, d), dtype=np.complex128)
-        for i in range(d):
-            for q in range(indptr[i], indptr[i + 1]):
-                m[i, indices[q]] += data[q]
+        np.add.at(m, (rows, np.asarray(indices, dtype=np.int64)[:len(rows)]), np.asarray(data)[:len(rows)])
         self._bind(m, terms, mode)
 
     def set_coeff(self, r: int, c: complex):

@@ -62,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             if verbose and msg:
                 print(msg, file=sys.stderr)
     if force or jobs or _stale(OUT, objs):
-        cmd = [nvcc] + ARCH + ["-shared", "-cudart", "shared", "-o", OUT] + objs + ["-lcusolver"]
+        cmd = [nvcc] + ARCH + ["-shared", "-cudart", "shared", "-o", OUT] + objs + ["-ldl"]
         run(cmd)
     return OUT
 

@@ -5,17 +5,62 @@
 // cooperative kernels and the oracle), on a column-major copy: the row-major m x n node
 // matrix is transposed by the r2l permutation kernel, factorised, R is read from the
 // upper triangle before zungqr overwrites it with Q, and Q is transposed back.
+//
+// cuSOLVER is loaded on first use (dlopen), not linked: the library and its callers that
+// never grow a bond past 64 do not depend on it, and a missing cuSOLVER fails only the
+// wide-bond integrators, with an error.
 #include "ttn_kernels.cuh"
 
-#include <cusolverDn.h>
+#include <dlfcn.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 namespace ttn {
 
+namespace {
+
+// the cuSOLVER dense entry points used here (status 0 is success; cuDoubleComplex has the
+// layout of double2)
+struct Solver {
+  int (*create)(void**) = nullptr;
+  int (*destroy)(void*) = nullptr;
+  int (*set_stream)(void*, cudaStream_t) = nullptr;
+  int (*geqrf_bs)(void*, int, int, double2*, int, int*) = nullptr;
+  int (*geqrf)(void*, int, int, double2*, int, double2*, double2*, int, int*) = nullptr;
+  int (*ungqr_bs)(void*, int, int, int, const double2*, int, const double2*, int*) = nullptr;
+  int (*ungqr)(void*, int, int, int, double2*, int, const double2*, double2*, int, int*) = nullptr;
+  bool ok = false;
+};
+
+const Solver& solver() {
+  static Solver S;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* h = nullptr;
+    for (const char* name : {"libcusolver.so.12", "libcusolver.so.13", "libcusolver.so.11", "libcusolver.so"})
+      if ((h = dlopen(name, RTLD_NOW | RTLD_LOCAL))) break;
+    if (!h) return;
+    S.create = reinterpret_cast<int (*)(void**)>(dlsym(h, "cusolverDnCreate"));
+    S.destroy = reinterpret_cast<int (*)(void*)>(dlsym(h, "cusolverDnDestroy"));
+    S.set_stream = reinterpret_cast<int (*)(void*, cudaStream_t)>(dlsym(h, "cusolverDnSetStream"));
+    S.geqrf_bs = reinterpret_cast<int (*)(void*, int, int, double2*, int, int*)>(dlsym(h, "cusolverDnZgeqrf_bufferSize"));
+    S.geqrf = reinterpret_cast<int (*)(void*, int, int, double2*, int, double2*, double2*, int, int*)>(
+        dlsym(h, "cusolverDnZgeqrf"));
+    S.ungqr_bs = reinterpret_cast<int (*)(void*, int, int, int, const double2*, int, const double2*, int*)>(
+        dlsym(h, "cusolverDnZungqr_bufferSize"));
+    S.ungqr = reinterpret_cast<int (*)(void*, int, int, int, double2*, int, const double2*, double2*, int, int*)>(
+        dlsym(h, "cusolverDnZungqr"));
+    S.ok = S.create && S.destroy && S.set_stream && S.geqrf_bs && S.geqrf && S.ungqr_bs && S.ungqr;
+  });
+  return S;
+}
+
+}  // namespace
+
 struct WideQr {
-  cusolverDnHandle_t h = nullptr;
+  void* h = nullptr;
   double2* colmaj = nullptr;  // m x n column-major copy, then Q
   double2* tau = nullptr;     // n reflector scalars
   double2* work = nullptr;    // LAPACK workspace
@@ -36,15 +81,15 @@ __global__ void k_upper_r(const double2* __restrict__ F, long long m, int n, dou
   }
 }
 
-cudaError_t status_to_cuda(cusolverStatus_t s) { return s == CUSOLVER_STATUS_SUCCESS ? cudaSuccess : cudaErrorUnknown; }
+cudaError_t status_to_cuda(int s) { return s == 0 ? cudaSuccess : cudaErrorUnknown; }
 
-cudaError_t lwork_for(cusolverDnHandle_t h, long long m, int n, double2* A, double2* tau, int* lw) {
+cudaError_t lwork_for(void* h, long long m, int n, double2* A, double2* tau, int* lw) {
+  const Solver& S = solver();
   int a = 0, b = 0;
-  cusolverStatus_t s = cusolverDnZgeqrf_bufferSize(h, (int)m, n, reinterpret_cast<cuDoubleComplex*>(A), (int)m, &a);
-  if (s != CUSOLVER_STATUS_SUCCESS) return status_to_cuda(s);
-  s = cusolverDnZungqr_bufferSize(h, (int)m, n, n, reinterpret_cast<const cuDoubleComplex*>(A), (int)m,
-                                  reinterpret_cast<const cuDoubleComplex*>(tau), &b);
-  if (s != CUSOLVER_STATUS_SUCCESS) return status_to_cuda(s);
+  int s = S.geqrf_bs(h, (int)m, n, A, (int)m, &a);
+  if (s != 0) return status_to_cuda(s);
+  s = S.ungqr_bs(h, (int)m, n, n, A, (int)m, tau, &b);
+  if (s != 0) return status_to_cuda(s);
   *lw = std::max(a, b);
   return cudaSuccess;
 }
@@ -61,8 +106,10 @@ cudaError_t wide_qr_create(WideQr** out, const long long* ms, const int* ns, int
     q->max_n = std::max(q->max_n, ns[k]);
   }
   if (q->max_n == 0) return fail(cudaErrorInvalidValue);
-  if (cusolverDnCreate(&q->h) != CUSOLVER_STATUS_SUCCESS) return fail(cudaErrorUnknown);
-  if (cusolverDnSetStream(q->h, s) != CUSOLVER_STATUS_SUCCESS) return fail(cudaErrorUnknown);
+  const Solver& S = solver();
+  if (!S.ok) return fail(cudaErrorSharedObjectInitFailed);  // cuSOLVER not found
+  if (S.create(&q->h) != 0) return fail(cudaErrorUnknown);
+  if (S.set_stream(q->h, s) != 0) return fail(cudaErrorUnknown);
   cudaError_t e;
   if ((e = cudaMalloc(&q->colmaj, (size_t)q->max_elems * sizeof(double2))) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&q->tau, (size_t)q->max_n * sizeof(double2))) != cudaSuccess) return fail(e);
@@ -85,7 +132,7 @@ void wide_qr_destroy(WideQr* q) {
   if (q->info) cudaFree(q->info);
   if (q->tau) cudaFree(q->tau);
   if (q->colmaj) cudaFree(q->colmaj);
-  if (q->h) cusolverDnDestroy(q->h);
+  if (q->h) solver().destroy(q->h);
   delete q;
 }
 
@@ -95,19 +142,17 @@ cudaError_t householder_qr_wide(WideQr* q, double2* M, long long m, int n, doubl
   cudaError_t e = lwork_for(q->h, m, n, q->colmaj, q->tau, &need);
   if (e != cudaSuccess) return e;
   if (need > q->lwork) return cudaErrorInvalidValue;
-  if (cusolverDnSetStream(q->h, s) != CUSOLVER_STATUS_SUCCESS) return cudaErrorUnknown;
+  const Solver& S = solver();
+  if (S.set_stream(q->h, s) != 0) return cudaErrorUnknown;
   // row-major m x n -> column-major (the transpose, row-major n x m)
   permute_mode_last(M, q->colmaj, 1, (int)m, n, s);
-  cuDoubleComplex* A = reinterpret_cast<cuDoubleComplex*>(q->colmaj);
-  cuDoubleComplex* tau = reinterpret_cast<cuDoubleComplex*>(q->tau);
-  cuDoubleComplex* work = reinterpret_cast<cuDoubleComplex*>(q->work);
-  e = status_to_cuda(cusolverDnZgeqrf(q->h, (int)m, n, A, (int)m, tau, work, q->lwork, q->info));
+  e = status_to_cuda(S.geqrf(q->h, (int)m, n, q->colmaj, (int)m, q->tau, q->work, q->lwork, q->info));
   if (e != cudaSuccess) return e;
   const long long nn = (long long)n * n;
   const int blocks = (int)std::min<long long>((nn + 255) / 256, 1024);
   k_upper_r<<<blocks, 256, 0, s>>>(q->colmaj, m, n, R, Rt);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  e = status_to_cuda(cusolverDnZungqr(q->h, (int)m, n, n, A, (int)m, tau, work, q->lwork, q->info));
+  e = status_to_cuda(S.ungqr(q->h, (int)m, n, n, q->colmaj, (int)m, q->tau, q->work, q->lwork, q->info));
   if (e != cudaSuccess) return e;
   unpermute_mode_last(q->colmaj, M, 1, (int)m, n, s);
   return cudaGetLastError();

@@ -258,3 +258,26 @@ def test_interaction_picture_coupling_converges_to_the_schroedinger_picture():
         errs.append(abs(oi.expect(0, np.diag([1.0, -1.0])).real - ref))
     assert errs[0] < 2e-4 and errs[2] < 5e-6
     assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5
+
+
+def test_sudden_cutoff_example_step_by_step():
+    """beta_10/ohmic/spin_boson_sudden (512 one-mode blocks of 100 states): through the
+    oracle, the first three printed rows of the reference -- observables to 1e-10, the
+    expansion counts (start-up expansion sweeps included) exactly for two steps and to one
+    bond decision in the third (9200 against 9201: one bond at the spawning threshold,
+    where the reference's Krylov estimate and this build's exact eigensolver part)."""
+    from oracle.oracle import Oracle
+    v = _golden()["beta_10/ohmic/spin_boson_sudden"]
+    inp = D.parse_input(v["input"])
+    m = D.build_model(inp)
+    orc = Oracle(m.topology, m.hamiltonian, krylov_dim=inp.krylov_dim, krylov_tol=inp.krylov_tolerance)
+    orc.init_product(inp.psi0, inp.seed)
+    orc.set_expansion(m.capacity, spawning_threshold=inp.spawning_parameter,
+                      unoccupied_threshold=inp.unoccupied_threshold, minimum_unoccupied=inp.minimum_unoccupied, seed=0)
+    for k in (1, 2, 3):
+        orc.step(inp.dt)
+        row = v["rows"][k]
+        vals = np.array([orc.expect(0, op).real for op in inp.ops])
+        assert np.max(np.abs(vals - row["values"])) < 1e-10, (k, vals, row["values"])
+        one, two = orc.expansion_counts()
+        assert one == row["counts"][0] and abs(two - row["counts"][1]) <= (0 if k < 3 else 2), (k, two, row["counts"])

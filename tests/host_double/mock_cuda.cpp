@@ -67,6 +67,7 @@ cudaError_t cudaGetDeviceProperties(struct cudaDeviceProp* p, int d) { return cu
 namespace ttn {
 std::atomic<unsigned long long> g_launches{0};
 std::atomic<unsigned long long> g_wide_qr{0};  // QRs that took the wide (cuSOLVER) route
+std::atomic<unsigned long long> g_csr_ops{0};  // sparse leaf-operator contractions applied
 
 static zc opA(const ZOperand& o, long long i, long long k) {
   const double2 v = o.p[i * o.s0 + (k / o.kdiv) * o.k1 + (k % o.kdiv) * o.k2];
@@ -189,6 +190,17 @@ static void apply_prog(const ExpmArgs& a, const double2* x, double2* out) {
           t[xx * r + k] = al * s;
         }
       for (size_t e = 0; e < t.size(); ++e) ob[e] = D(o.beta ? t[e] + Z(ob[e]) : t[e]);
+    } else if (o.kind == MV_CSR) {
+      ++g_csr_ops;
+      std::vector<zc> t((size_t)o.na * o.d * o.nb);
+      for (long long aa = 0; aa < o.na; ++aa)
+        for (int i = 0; i < o.d; ++i)
+          for (long long bb = 0; bb < o.nb; ++bb) {
+            zc s = 0.0;
+            for (int q = o.rowptr[i]; q < o.rowptr[i + 1]; ++q) s += Z(o.mat[q]) * Z(in[(aa * o.d + o.colind[q]) * o.nb + bb]);
+            t[(aa * o.d + i) * o.nb + bb] = al * s;
+          }
+      for (size_t e = 0; e < t.size(); ++e) ob[e] = D(o.beta ? t[e] + Z(ob[e]) : t[e]);
     } else if (o.kind == MV_AXPY) {
       for (long long e = 0; e < o.na; ++e) { zc r = al * Z(in[e]); if (o.beta) r += Z(ob[e]); ob[e] = D(r); }
     } else {
@@ -294,3 +306,4 @@ extern "C" int ttn_qr_noalloc(int, int, double*, double*, void*, int) { return 1
 
 // how many QRs took the wide route (read by the host-orchestration test)
 extern "C" unsigned long long mock_wide_qr_count() { return ttn::g_wide_qr.load(); }
+extern "C" unsigned long long mock_csr_op_count() { return ttn::g_csr_ops.load(); }

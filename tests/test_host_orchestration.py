@@ -300,8 +300,12 @@ orc.set_expansion(m.capacity, spawning_threshold=inp.spawning_parameter, unoccup
                   minimum_unoccupied=inp.minimum_unoccupied, seed=0)
 out = dict(first=r.first_row(), start=float(max(np.max(np.abs(a - b)) for a, b in zip(r.A.get(), orc.get_state()))),
            steps=[])
+import ctypes
+csr = ctypes.CDLL({lib!r}).mock_csr_op_count
+csr.restype = ctypes.c_ulonglong
 for k in range(2):
     r.step(); orc.step(inp.dt)
+    out["csr_ops"] = int(csr())
     out["steps"].append(dict(values=float(max(abs(a - orc.expect(0, op).real) for a, op in zip(r.observables(), inp.ops))),
                              counts=[list(r.tdvp.expansion_counts()), list(orc.expansion_counts())],
                              hrank=bool(np.array_equal(r.hrank(), orc.hrank()[1:]))))
@@ -311,9 +315,10 @@ print(json.dumps(out))
 
 def test_driver_device_path_matches_oracle():
     """The spin-boson driver's device path (start state, expansion set-up, steps, leaf
-    observables, expansion counters) on the test double against the oracle, on a 16-mode
-    version of the reference's sudden-cutoff example: the same start state bit for bit,
-    the same bond dimensions and counts, observables to rounding."""
+    observables, expansion counters, sparse leaf operators in the matvec programs) on the
+    test double against the oracle, on a 16-mode version of the reference's sudden-cutoff
+    example: the same start state bit for bit, the same bond dimensions and counts,
+    observables to rounding."""
     lib = _build()
     code = DRIVER_CHILD.format(root=ROOT, lib=lib, golden=os.path.join(ROOT, "tests", "golden", "driver_examples.json"))
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
@@ -321,6 +326,7 @@ def test_driver_device_path_matches_oracle():
     res = json.loads(r.stdout.strip().splitlines()[-1])
     assert res["first"].startswith("0 0 0 1 1  0 0 0 2 2 ")
     assert res["start"] == 0.0
+    assert res["csr_ops"] > 0  # the blocks' sparse operators went through the CSR contractions
     for s in res["steps"]:
         assert s["values"] < 1e-11 and s["hrank"], s
         assert s["counts"][0] == s["counts"][1], s

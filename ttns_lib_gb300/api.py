@@ -178,9 +178,19 @@ class Operator:
         _check(lib().ttn_sop_create(sop.nterms, len(md), _ip(md), C.byref(h)))
         self.h = h
         for b in sop.ops:
-            m = _cplx(b.matrix)
             r = np.array(b.terms, dtype=np.int32)
-            _check(lib().ttn_sop_bind_dense(h, b.mode, _dp(m.view(np.float64)), _ip(r), len(r)))
+            sp = b.sparse_form()
+            if sp is not None and sp[0] == "diag":
+                dg = _cplx(sp[1])
+                _check(lib().ttn_sop_bind_diag(h, b.mode, _dp(dg.view(np.float64)), _ip(r), len(r)))
+            elif sp is not None and sp[0] == "csr":
+                rp = np.ascontiguousarray(sp[1], dtype=np.int32)
+                ci = np.ascontiguousarray(sp[2], dtype=np.int32)
+                vals = _cplx(sp[3])
+                _check(lib().ttn_sop_bind_csr(h, b.mode, _ip(rp), _ip(ci), _dp(vals.view(np.float64)), _ip(r), len(r)))
+            else:
+                m = _cplx(b.matrix)
+                _check(lib().ttn_sop_bind_dense(h, b.mode, _dp(m.view(np.float64)), _ip(r), len(r)))
         for r, c in enumerate(sop.coeffs):
             _check(lib().ttn_sop_set_coeff(h, r, float(np.real(c)), float(np.imag(c))))
 

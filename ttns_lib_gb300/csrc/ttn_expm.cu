@@ -110,6 +110,26 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
       if (acc) o = cadd(o, out[e]);
       out[e] = o;
     }
+  } else if (op.kind == MV_CSR) {
+    const int d = op.d;
+    const long long nb = op.nb, total = op.na * d * nb;
+    for (long long e = tid; e < total; e += nthreads) {
+      const long long aa = e / (d * nb), rem = e % (d * nb);
+      const int i = (int)(rem / nb);
+      const long long b = rem % nb;
+      const double2* v = in + aa * d * nb + b;
+      double2 s0 = make_double2(0.0, 0.0), s1 = s0;
+      int q = op.rowptr[i];
+      const int q1 = op.rowptr[i + 1];
+      for (; q + 2 <= q1; q += 2) {
+        s0 = cfma(op.mat[q], v[(long long)op.colind[q] * nb], s0);
+        s1 = cfma(op.mat[q + 1], v[(long long)op.colind[q + 1] * nb], s1);
+      }
+      if (q < q1) s0 = cfma(op.mat[q], v[(long long)op.colind[q] * nb], s0);
+      double2 r = cmul(op.alpha, cadd(s0, s1));
+      if (acc) r = cadd(r, out[e]);
+      out[e] = r;
+    }
   } else if (op.kind == MV_AXPY) {
     const long long total = op.na;
     for (long long e = tid; e < total; e += nthreads) {

@@ -9,12 +9,14 @@ namespace ttn {
 
 struct GridBarrier;
 
-enum { MV_MODE = 0, MV_MF = 1, MV_AXPY = 2, MV_ZERO = 3 };
+enum { MV_MODE = 0, MV_MF = 1, MV_AXPY = 2, MV_ZERO = 3, MV_CSR = 4 };
 
 // One contraction of a matrix-vector program.  Buffers: 0 = input vector, 1 = output,
 // 2..4 = temporaries.  MODE: out(a,i,b) = alpha sum_j mat(i,j) in(a,j,b) (+ out) with
 // shape (na, d, nb); MF: out(x,k) = alpha sum_l in(x,l) mat(k,l) (+ out) with nx = na,
-// r = d; AXPY: out = alpha in (+ out) over na elements; ZERO: out = 0 over na elements.
+// r = d; AXPY: out = alpha in (+ out) over na elements; ZERO: out = 0 over na elements;
+// CSR: MODE with a sparse d x d matrix (row i: mat[q], column colind[q] for q in
+// rowptr[i] .. rowptr[i+1]), for sparse leaf operators.
 struct MvOp {
   int kind;
   int in, out;
@@ -26,6 +28,8 @@ struct MvOp {
   int tc;    // 1: run on the tensor cores (mixed precision; MODE with d = 64, MF with r = 64)
   int img;   // tensor-core ops: slot of the operator image (split TF32 block form of alpha mat)
   double2 alpha;
+  const int* rowptr;  // CSR only
+  const int* colind;
 };
 // bytes of one operator image: row exponents (1 KB) and the 128 x 128 block operand as
 // six bf16 integer slices in four K-chunks of 48 KB

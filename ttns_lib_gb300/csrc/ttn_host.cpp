@@ -160,11 +160,17 @@ struct Tree {
 };
 
 // ------------------------------------------------------------------ operator
+// a sparse copy of a leaf operator bound in CSR or diagonal form
+struct SparseOp {
+  std::vector<int> rowptr, colind;
+  std::vector<cd> val;
+};
 struct Sop {
   int nterms = 0, nmodes = 0;
   std::vector<int> mode_dim;
   std::vector<cd> coeff;
   std::vector<std::vector<std::vector<cd>>> ops;  // [mode][k] dense d x d
+  std::vector<std::vector<SparseOp>> sparse;      // [mode][k] CSR form, empty rowptr when bound dense
   std::vector<std::vector<int>> opidx;            // [mode][r]
   std::vector<std::pair<int, int>> op_order;      // (mode, k) of every operator in binding order
 };
@@ -422,6 +428,18 @@ struct Integrator {
   // device arenas
   DevBuf ops_buf, env_buf, r_buf, work_buf, ctl_buf, mel_buf;
   std::vector<std::vector<double2*>> leaf_ops;  // [mode][k]
+  // sparse copies of large sparse leaf operators (bound in CSR or diagonal form), used by
+  // the matvec programs while no time-dependent update hook is set
+  struct LeafCsr {
+    const int* rp = nullptr;
+    const int* ci = nullptr;
+    const double2* val = nullptr;
+    long long nnz = 0;
+  };
+  std::vector<std::vector<LeafCsr>> leaf_csr;  // [mode][k]
+  DevBuf csr_buf;
+  static bool sparse_worth_it(int d, long long nnz) { return d >= 32 && nnz * 8 <= (long long)d * d; }
+  bool csr_enabled() const { return !op_update_fn; }
   std::vector<double2*> rmat, mel;
   double2 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w4 = nullptr, *V = nullptr, *p = nullptr,
           *gws = nullptr, *qtau = nullptr, *scal = nullptr;
@@ -538,6 +556,46 @@ struct Integrator {
           leaf_ops[m].push_back(dptr);
           o += align256(M.size() * sizeof(double2));
         }
+    }
+    // sparse leaf operators: row pointers, column indices and values in one buffer
+    leaf_csr.assign(H.nmodes, {});
+    {
+      size_t cb = 0;
+      for (int m = 0; m < H.nmodes; ++m)
+        for (size_t k = 0; k < H.ops[m].size(); ++k) {
+          leaf_csr[m].push_back(LeafCsr());
+          if (m >= (int)H.sparse.size() || k >= H.sparse[m].size()) continue;
+          const SparseOp& sp = H.sparse[m][k];
+          if (sp.rowptr.empty() || !sparse_worth_it(H.mode_dim[m], (long long)sp.val.size())) continue;
+          cb += align256(sp.rowptr.size() * sizeof(int)) + align256(std::max<size_t>(1, sp.colind.size()) * sizeof(int)) +
+                align256(std::max<size_t>(1, sp.val.size()) * sizeof(double2));
+        }
+      if (cb) {
+        csr_buf.alloc(cb);
+        char* base = csr_buf.as<char>();
+        size_t o = 0;
+        for (int m = 0; m < H.nmodes; ++m)
+          for (size_t k = 0; k < H.ops[m].size(); ++k) {
+            if (m >= (int)H.sparse.size() || k >= H.sparse[m].size()) continue;
+            const SparseOp& sp = H.sparse[m][k];
+            if (sp.rowptr.empty() || !sparse_worth_it(H.mode_dim[m], (long long)sp.val.size())) continue;
+            LeafCsr& c = leaf_csr[m][k];
+            int* rp = (int*)(base + o);
+            o += align256(sp.rowptr.size() * sizeof(int));
+            int* ci = (int*)(base + o);
+            o += align256(std::max<size_t>(1, sp.colind.size()) * sizeof(int));
+            double2* val = (double2*)(base + o);
+            o += align256(std::max<size_t>(1, sp.val.size()) * sizeof(double2));
+            std::vector<double2> v(sp.val.size());
+            for (size_t q = 0; q < v.size(); ++q) v[q] = d2(sp.val[q]);
+            CK(cudaMemcpy(rp, sp.rowptr.data(), sp.rowptr.size() * sizeof(int), cudaMemcpyHostToDevice));
+            if (!sp.colind.empty()) {
+              CK(cudaMemcpy(ci, sp.colind.data(), sp.colind.size() * sizeof(int), cudaMemcpyHostToDevice));
+              CK(cudaMemcpy(val, v.data(), v.size() * sizeof(double2), cudaMemcpyHostToDevice));
+            }
+            c.rp = rp; c.ci = ci; c.val = val; c.nnz = (long long)sp.val.size();
+          }
+      }
     }
     allocate_sized();
     finish_setup();
@@ -975,7 +1033,8 @@ struct Integrator {
         for (const SpfTuple& t : g.spf)
           for (const Item& it : t.items) {
             int d = (it.slot < 0) ? T.dims[nd][0] : T.dims[nd][it.slot];
-            f += 8.0 * sz * d;
+            const LeafCsr* c = item_csr(nd, it);
+            f += c ? 8.0 * (sz / d) * (double)c->nnz : 8.0 * sz * d;
           }
       if (!g.id_mf) f += 8.0 * sz * r;
     }
@@ -1026,14 +1085,30 @@ struct Integrator {
     if (it.slot < 0) { S = leaf_ops[T.leaf_mode[nd]][it.grp]; na = 1; d = T.dims[nd][0]; nb = T.hrank[nd]; }
     else { S = G[T.children[nd][it.slot]][it.grp].spf_dev; r3(nd, it.slot, na, d, nb); }
   }
+  // the product of one item with the vector: a sparse leaf operator's CSR contraction, or
+  // the dense mode product
+  const LeafCsr* item_csr(int nd, const Item& it) const {
+    if (it.slot >= 0 || !csr_enabled()) return nullptr;
+    const LeafCsr& c = leaf_csr[T.leaf_mode[nd]][it.grp];
+    return c.rp ? &c : nullptr;
+  }
+  MvOp mk_item(int in, int out, int nd, const Item& it, cd alpha, bool acc) {
+    const double2* S; long long na, nb; int d;
+    item_shape(nd, it, S, na, d, nb);
+    if (const LeafCsr* c = item_csr(nd, it)) {
+      MvOp o = mk(MV_CSR, in, out, c->val, na, d, nb, alpha, acc);
+      o.rowptr = c->rp;
+      o.colind = c->ci;
+      return o;
+    }
+    return mk(MV_MODE, in, out, S, na, d, nb, alpha, acc);
+  }
   // chain of mode products ending in a temporary; returns its buffer id
   int emit_chain(ProgBuilder& B, int nd, const std::vector<Item>& items, int in, cd alpha_last) {
     int cur = in;
     for (size_t q = 0; q < items.size(); ++q) {
-      const double2* S; long long na, nb; int d;
-      item_shape(nd, items[q], S, na, d, nb);
       int out = (q % 2 == 0) ? 2 : 3;
-      B.emit(mk(MV_MODE, cur, out, S, na, d, nb, q + 1 == items.size() ? alpha_last : cd(1.0), false));
+      B.emit(mk_item(cur, out, nd, items[q], q + 1 == items.size() ? alpha_last : cd(1.0), false));
       cur = out;
     }
     return cur;
@@ -1052,9 +1127,7 @@ struct Integrator {
       } else if (g.spf.size() == 1) {
         const auto& t = g.spf[0];
         if (direct && t.items.size() == 1) {
-          const double2* S; long long na, nb; int d;
-          item_shape(nd, t.items[0], S, na, d, nb);
-          B.emit(mk(MV_MODE, 0, 1, S, na, d, nb, g.s * t.a, !first));
+          B.emit(mk_item(0, 1, nd, t.items[0], g.s * t.a, !first));
         } else {
           int X = emit_chain(B, nd, t.items, 0, t.a);
           if (direct) B.emit(mk(MV_AXPY, X, 1, nullptr, sz, 0, 0, g.s * chain_scale(t), !first));
@@ -1067,9 +1140,7 @@ struct Integrator {
           const bool accum = direct ? !(first && f2) : !f2;
           const cd sc = direct ? g.s * t.a : t.a;
           if (t.items.size() == 1) {
-            const double2* S; long long na, nb; int d;
-            item_shape(nd, t.items[0], S, na, d, nb);
-            B.emit(mk(MV_MODE, 0, acc_buf, S, na, d, nb, sc, accum));
+            B.emit(mk_item(0, acc_buf, nd, t.items[0], sc, accum));
           } else {
             int X = emit_chain(B, nd, t.items, 0, t.a);
             B.emit(mk(MV_AXPY, X, acc_buf, nullptr, sz, 0, 0, (direct ? g.s : cd(1.0)) * chain_scale(t), accum));
@@ -1605,13 +1676,15 @@ int ttn_sop_create(int nterms, int nmodes, const int* mode_dims, ttn_sop** out) 
     if (d < 1) { delete s; throw ttn::Err(TTN_EINVAL, "mode dimensions must be >= 1"); }
   s->H.coeff.assign(nterms, 1.0);
   s->H.ops.assign(nmodes, {});
+  s->H.sparse.assign(nmodes, {});
   s->H.opidx.assign(nmodes, std::vector<int>(nterms, -1));
   *out = s;
   TTN_API_END
 }
 int ttn_sop_destroy(ttn_sop* s) { delete s; return TTN_OK; }
 
-static void sop_bind(ttn_sop* s, int mode, std::vector<ttn::cd>&& M, const int* r, int nr) {
+static void sop_bind(ttn_sop* s, int mode, std::vector<ttn::cd>&& M, const int* r, int nr,
+                     ttn::SparseOp&& sp = ttn::SparseOp()) {
   TTN_REQUIRE(s && mode >= 0 && mode < s->H.nmodes, TTN_EINVAL, "mode out of range");
   TTN_REQUIRE(r && nr >= 1, TTN_EINVAL, "an operator must be bound to at least one term");
   for (int q = 0; q < nr; ++q) {
@@ -1621,6 +1694,8 @@ static void sop_bind(ttn_sop* s, int mode, std::vector<ttn::cd>&& M, const int* 
   for (auto& z : M) TTN_REQUIRE(std::isfinite(z.real()) && std::isfinite(z.imag()), TTN_EINVAL, "non-finite operator entry");
   int k = (int)s->H.ops[mode].size();
   s->H.ops[mode].push_back(std::move(M));
+  if (s->H.sparse.size() < (size_t)s->H.nmodes) s->H.sparse.resize(s->H.nmodes);
+  s->H.sparse[mode].push_back(std::move(sp));
   s->H.op_order.push_back({mode, k});
   for (int q = 0; q < nr; ++q) s->H.opidx[mode][r[q]] = k;
 }
@@ -1638,8 +1713,16 @@ int ttn_sop_bind_diag(ttn_sop* s, int mode, const double* diag, const int* r, in
   TTN_REQUIRE(s && diag && mode >= 0 && mode < s->H.nmodes, TTN_EINVAL, "bad argument");
   int d = s->H.mode_dim[mode];
   std::vector<ttn::cd> M((size_t)d * d, 0.0);
-  for (int i = 0; i < d; ++i) M[(size_t)i * d + i] = ttn::cd(diag[2 * i], diag[2 * i + 1]);
-  sop_bind(s, mode, std::move(M), r, nr);
+  ttn::SparseOp sp;
+  sp.rowptr.resize(d + 1);
+  for (int i = 0; i < d; ++i) {
+    M[(size_t)i * d + i] = ttn::cd(diag[2 * i], diag[2 * i + 1]);
+    sp.rowptr[i] = i;
+    sp.colind.push_back(i);
+    sp.val.push_back(M[(size_t)i * d + i]);
+  }
+  sp.rowptr[d] = d;
+  sop_bind(s, mode, std::move(M), r, nr, std::move(sp));
   TTN_API_END
 }
 int ttn_sop_bind_csr(ttn_sop* s, int mode, const int* rowptr, const int* colind, const double* vals, const int* r,
@@ -1647,13 +1730,19 @@ int ttn_sop_bind_csr(ttn_sop* s, int mode, const int* rowptr, const int* colind,
   TTN_API_BEGIN
   TTN_REQUIRE(s && rowptr && mode >= 0 && mode < s->H.nmodes, TTN_EINVAL, "bad argument");
   int d = s->H.mode_dim[mode];
+  TTN_REQUIRE(rowptr[0] == 0, TTN_EINVAL, "CSR row pointers must start at 0");
+  for (int i = 0; i < d; ++i) TTN_REQUIRE(rowptr[i + 1] >= rowptr[i], TTN_EINVAL, "CSR row pointers must not decrease");
   std::vector<ttn::cd> M((size_t)d * d, 0.0);
+  ttn::SparseOp sp;
+  sp.rowptr.assign(rowptr, rowptr + d + 1);
   for (int i = 0; i < d; ++i)
     for (int q = rowptr[i]; q < rowptr[i + 1]; ++q) {
       TTN_REQUIRE(colind && vals && colind[q] >= 0 && colind[q] < d, TTN_EINVAL, "CSR column out of range");
       M[(size_t)i * d + colind[q]] += ttn::cd(vals[2 * q], vals[2 * q + 1]);
+      sp.colind.push_back(colind[q]);
+      sp.val.push_back(ttn::cd(vals[2 * q], vals[2 * q + 1]));
     }
-  sop_bind(s, mode, std::move(M), r, nr);
+  sop_bind(s, mode, std::move(M), r, nr, std::move(sp));
   TTN_API_END
 }
 int ttn_sop_set_coeff(ttn_sop* s, int r, double re, double im) {
@@ -2226,8 +2315,10 @@ int ttn_integrator_set_op_update(ttn_integrator* it, ttn_op_update_fn fn, void* 
   TTN_REQUIRE(it, TTN_EINVAL, "null argument");
   ttn::Integrator& I = it->I;
   TTN_REQUIRE(!fn || !I.mixed, TTN_EINVAL, "time-dependent operators need an FP64 integrator");
+  const bool recompile = (I.op_update_fn == nullptr) != (fn == nullptr);
   I.op_update_fn = fn;
   I.op_update_user = user;
+  if (recompile) I.compile_programs();  // sparse leaf copies are used only without the hook
   I.op_global.assign(I.H.nmodes, {});
   for (int m = 0; m < I.H.nmodes; ++m) I.op_global[m].assign(I.H.ops[m].size(), -1);
   for (size_t g = 0; g < I.H.op_order.size(); ++g) I.op_global[I.H.op_order[g].first][I.H.op_order[g].second] = (int)g;

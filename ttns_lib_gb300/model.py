@@ -205,6 +205,13 @@ class _Bound:
     mode: int
     matrix: np.ndarray
     terms: List[int]
+    # ("diag", d) or ("csr", indptr, indices, data) when bound in that form; valid while
+    # ``sparse_of`` is ``matrix`` (replacing the matrix drops back to the dense form)
+    sparse: Optional[tuple] = None
+    sparse_of: Optional[np.ndarray] = None
+
+    def sparse_form(self):
+        return self.sparse if self.sparse is not None and self.sparse_of is self.matrix else None
 
 
 class SOPOperator:
@@ -217,7 +224,7 @@ class SOPOperator:
         self.ops: List[_Bound] = []
         self._taken = set()
 
-    def _bind(self, mat: np.ndarray, terms, mode: int):
+    def _bind(self, mat: np.ndarray, terms, mode: int, sparse: Optional[tuple] = None):
         d = self.mode_dims[mode]
         mat = np.ascontiguousarray(mat, dtype=np.complex128)
         if mat.shape != (d, d):
@@ -229,21 +236,24 @@ class SOPOperator:
             if (r, mode) in self._taken:
                 raise ValueError(f"term {r} already has an operator on mode {mode}")
             self._taken.add((r, mode))
-        self.ops.append(_Bound(mode, mat, terms))
+        self.ops.append(_Bound(mode, mat, terms, sparse, mat if sparse is not None else None))
 
     def bind_dense(self, mat, terms, mode: int):
         self._bind(np.asarray(mat), terms, mode)
 
     def bind_diag(self, diag, terms, mode: int):
-        self._bind(np.diag(np.asarray(diag, dtype=np.complex128)), terms, mode)
+        dg = np.ascontiguousarray(diag, dtype=np.complex128)
+        self._bind(np.diag(dg), terms, mode, ("diag", dg))
 
     def bind_csr(self, indptr, indices, data, terms, mode: int):
         d = self.mode_dims[mode]
         indptr = np.asarray(indptr, dtype=np.int64)
         rows = np.repeat(np.arange(d), np.diff(indptr[:d + 1]))
         m = np.zeros((d, d), dtype=np.complex128)
-        np.add.at(m, (rows, np.asarray(indices, dtype=np.int64)[:len(rows)]), np.asarray(data)[:len(rows)])
-        self._bind(m, terms, mode)
+        ind = np.asarray(indices, dtype=np.int64)[:len(rows)]
+        dat = np.asarray(data, dtype=np.complex128)[:len(rows)]
+        np.add.at(m, (rows, ind), dat)
+        self._bind(m, terms, mode, ("csr", indptr[:d + 1].copy(), ind.copy(), dat.copy()))
 
     def set_coeff(self, r: int, c: complex):
         self.coeffs[r] = c

@@ -129,7 +129,7 @@ struct DevExpander {
   }
 
   // M (dimen_C x pre*post, row-major, on the host) at the bond above C; r: gauge factor (d x d)
-  std::vector<cd> two_site_matrix(ttn_state* S, int C, const double2* r) {
+  std::vector<cd> two_site_matrix(ttn_state* S, int C, const double2* r, bool download = true) {
     const Tree& T = I.T;
     const int P = T.parent[C], mu = T.slot[C], d = T.hrank[C], rp = T.hrank[P];
     long long pre, post;
@@ -187,6 +187,7 @@ struct DevExpander {
       g.beta = make_double2(1.0, 0.0);
       zgemm(g, I.gws, I.gws_bytes, I.stream);
     }
+    if (!download) return {};
     return down(M, (size_t)(mC * outer));
   }
 
@@ -253,34 +254,120 @@ struct DevExpander {
     }
   }
 
-  // dominant singular values and (right or left) vectors of M (m x n), at most k
-  // the Gram matrix of the smaller side of M (still in m_buf on the device): M M^H when
-  // m <= n, else M^H M, by one GEMM, then to the host
-  std::vector<cd> gram_dev(size_t m, size_t n) {
+  // dominant_dev: the same result as dominant() for the M left in m_buf by
+  // two_site_matrix(..., false), without bringing M or its Gram matrix to the host: the
+  // Gram matrix of the smaller side by one GEMM, the Lanczos process of top_eig on the
+  // device (w = G q by GEMM, two passes of classical Gram-Schmidt against all earlier
+  // vectors by GEMM, only alpha and beta copied back per step), the tridiagonal solved
+  // and the Ritz vectors formed on the host from the Lanczos vectors (48 x g), and the
+  // other side's vectors M^H z / s or M z / s by GEMM.
+  void dominant_dev(size_t m, size_t n, int k, bool right, std::vector<double>& sv, std::vector<std::vector<cd>>& vecs) {
     const bool small_left = m <= n;
     const size_t g = small_left ? m : n;
-    DevBuf gb;
+    const int mmax = (int)std::min<size_t>(g, 48);
+    DevBuf gb, qb, wb;
     gb.alloc(g * g * sizeof(double2));
+    qb.alloc((size_t)mmax * g * sizeof(double2));
+    wb.alloc((g + 64 + 4) * sizeof(double2));
+    double2* Gd = gb.as<double2>();
+    double2* Qd = qb.as<double2>();
+    double2* w = wb.as<double2>();
+    double2* h = w + g;         // projections on the Lanczos vectors (<= 48)
+    double2* sc = h + 64;       // alpha, beta^2
     const double2* M = m_buf.as<double2>();
-    ZGemm z{};
-    z.M = (int)g; z.N = (int)g;
-    if (small_left) {
-      z.K = (int)n;
-      z.A = op_rowmajor(M, (long long)n);  // A(i,c) = M(i,c)
-      z.B = op_rowmajor(M, (long long)n);  // B(c,j) = conj M(j,c)
-      z.B.cj = 1;
-    } else {
-      z.K = (int)m;
-      z.A = op_colk(M, (long long)n, 1);   // A(i,r) = conj M(r,i)
-      z.A.cj = 1;
-      z.B = op_colk(M, (long long)n, 1);   // B(r,j) = M(r,j)
+    auto gemm = [&](int Mr, int Nc, int K, ZOperand A, ZOperand B, double2* C, long long ci, long long cj, double2 al,
+                    double2 be) {
+      ZGemm z{};
+      z.M = Mr; z.N = Nc; z.K = K; z.A = A; z.B = B; z.C = C; z.ci = ci; z.cj = cj;
+      z.batch = 1; z.alpha = al; z.beta = be;
+      zgemm(z, I.gws, I.gws_bytes, I.stream);
+    };
+    const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0), mone = make_double2(-1.0, 0.0);
+    // Gram matrix of the smaller side
+    {
+      ZOperand A, B;
+      if (small_left) {
+        A = op_rowmajor(M, (long long)n);
+        B = op_rowmajor(M, (long long)n);
+        B.cj = 1;
+        gemm((int)g, (int)g, (int)n, A, B, Gd, (long long)g, 1, one, zero);
+      } else {
+        A = op_colk(M, (long long)n, 1);
+        A.cj = 1;
+        B = op_colk(M, (long long)n, 1);
+        gemm((int)g, (int)g, (int)m, A, B, Gd, (long long)g, 1, one, zero);
+      }
     }
-    z.C = gb.as<double2>(); z.ci = (long long)g; z.cj = 1;
-    z.batch = 1;
-    z.alpha = make_double2(1.0, 0.0);
-    z.beta = make_double2(0.0, 0.0);
-    zgemm(z, I.gws, I.gws_bytes, I.stream);
-    return down(gb.as<double2>(), g * g);
+    // the start vector of top_eig
+    {
+      std::vector<cd> q(g);
+      double nq = 0.0;
+      for (size_t i = 0; i < g; ++i) { q[i] = 1.0 + 0.5 * std::sin((double)(i + 1)); nq += std::norm(q[i]); }
+      for (auto& z : q) z /= std::sqrt(nq);
+      up(Qd, q);
+    }
+    std::vector<double> al, be;
+    for (int j = 0; j < mmax; ++j) {
+      const double2* q = Qd + (size_t)j * g;
+      const ZOperand vec_q = op_colk(q, 1, 0);
+      gemm((int)g, 1, (int)g, op_rowmajor(Gd, (long long)g), vec_q, w, 1, 0, one, zero);  // w = G q
+      ZOperand qc = op_colk(q, 1, 0);
+      qc.cj = 1;
+      gemm(1, 1, (int)g, qc, op_colk(w, 1, 0), sc, 1, 0, one, zero);  // alpha = q^H w
+      for (int pass = 0; pass < 2; ++pass) {
+        ZOperand Qc = op_rowmajor(Qd, (long long)g);
+        Qc.cj = 1;
+        gemm(j + 1, 1, (int)g, Qc, op_colk(w, 1, 0), h, 1, 0, one, zero);                          // h = Q^H w
+        gemm((int)g, 1, j + 1, op_colk(Qd, (long long)g, 1), op_colk(h, 1, 0), w, 1, 0, mone, one);  // w -= Q h
+      }
+      ZOperand wc = op_colk(w, 1, 0);
+      wc.cj = 1;
+      gemm(1, 1, (int)g, wc, op_colk(w, 1, 0), sc + 1, 1, 0, one, zero);  // beta^2 = w^H w
+      double2 hs[2];
+      CK(cudaMemcpyAsync(hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, I.stream));
+      CK(cudaStreamSynchronize(I.stream));
+      const double a = hs[0].x, b = std::sqrt(std::max(0.0, hs[1].x));
+      al.push_back(a);
+      if (j + 1 == mmax || b <= 1e-14 * (std::fabs(a) + (be.empty() ? 0.0 : be.back()) + 1e-300)) break;
+      be.push_back(b);
+      zaxpy(Qd + (size_t)(j + 1) * g, w, make_double2(1.0 / b, 0.0), (long long)g, false, I.stream);
+    }
+    const int mm = (int)al.size();
+    std::vector<cd> Tm((size_t)mm * mm, 0.0);
+    for (int i = 0; i < mm; ++i) {
+      Tm[(size_t)i * mm + i] = al[i];
+      if (i + 1 < mm) { Tm[(size_t)i * mm + i + 1] = be[i]; Tm[(size_t)(i + 1) * mm + i] = be[i]; }
+    }
+    std::vector<double> tw;
+    std::vector<cd> Y;
+    herm_eig_host(Tm, mm, tw, Y);
+    const std::vector<cd> Q = down(Qd, (size_t)mm * g);
+    sv.clear();
+    vecs.clear();
+    for (int j = 0; j < std::min(k, mm); ++j) {
+      std::vector<cd> z(g, 0.0);
+      for (int i = 0; i < mm; ++i)
+        for (size_t r = 0; r < g; ++r) z[r] += Y[(size_t)i * mm + j] * Q[(size_t)i * g + r];
+      const double s2 = tw[j];
+      sv.push_back(s2 > 0.0 ? std::sqrt(s2) : 0.0);
+      if (right == !small_left) { vecs.push_back(z); continue; }
+      const double s = sv.back();
+      const size_t len = right ? n : m;
+      if (!(s > 0.0)) { vecs.push_back(std::vector<cd>(len, 0.0)); continue; }
+      DevBuf ob;
+      ob.alloc((len + g) * sizeof(double2));
+      double2* zd = ob.as<double2>() + len;
+      up(zd, z);
+      if (right) {  // o(c) = sum_r conj M(r, c) z(r) / s
+        ZOperand A = op_colk(M, (long long)n, 1);
+        A.cj = 1;
+        gemm((int)n, 1, (int)m, A, op_colk(zd, 1, 0), ob.as<double2>(), 1, 0, make_double2(1.0 / s, 0.0), zero);
+      } else {      // o(r) = sum_c M(r, c) z(c) / s
+        gemm((int)m, 1, (int)n, op_rowmajor(M, (long long)n), op_colk(zd, 1, 0), ob.as<double2>(), 1, 0,
+             make_double2(1.0 / s, 0.0), zero);
+      }
+      vecs.push_back(down(ob.as<double2>(), len));
+    }
   }
 
   // dominant singular values and (right or left) vectors of M (m x n), at most k; Gpre: the
@@ -420,13 +507,16 @@ struct DevExpander {
     const int required = nunocc < minimum_unoccupied ? std::min(minimum_unoccupied - nunocc, max_add) : 0;
     int nadd = 0;
     if (d < T.dimen[C] && d != 1) {
-      const std::vector<cd> M = two_site_matrix(S, C, I.rmat[P]);
       std::vector<double> sv;
       std::vector<std::vector<cd>> V;
       const size_t mm = (size_t)T.dimen[C], nn = (size_t)outer;
-      std::vector<cd> G;
-      if (std::min(mm, nn) > 96) G = gram_dev(mm, nn);
-      dominant(M, mm, nn, neigenvalues, true, sv, V, G.empty() ? nullptr : &G);
+      if (std::min(mm, nn) > 96) {
+        two_site_matrix(S, C, I.rmat[P], false);
+        dominant_dev(mm, nn, neigenvalues, true, sv, V);
+      } else {
+        const std::vector<cd> M = two_site_matrix(S, C, I.rmat[P]);
+        dominant(M, mm, nn, neigenvalues, true, sv, V);
+      }
       for (double s : sv)
         if (s > 0.0 && std::isfinite(s) && s * I.dt / 2.0 > spawning_threshold) ++nadd;
       nadd = std::min(nadd, max_add);
@@ -467,13 +557,16 @@ struct DevExpander {
     const int required = nunocc < minimum_unoccupied ? std::min(minimum_unoccupied - nunocc, max_add) : 0;
     int nadd = 0;
     if (d < pre * post && d != 1) {
-      const std::vector<cd> M = two_site_matrix(S, C, I.rmat[C]);
       std::vector<double> sv;
       std::vector<std::vector<cd>> U;
       const size_t mm = (size_t)mC, nn = (size_t)(pre * post);
-      std::vector<cd> G;
-      if (std::min(mm, nn) > 96) G = gram_dev(mm, nn);
-      dominant(M, mm, nn, neigenvalues, false, sv, U, G.empty() ? nullptr : &G);
+      if (std::min(mm, nn) > 96) {
+        two_site_matrix(S, C, I.rmat[C], false);
+        dominant_dev(mm, nn, neigenvalues, false, sv, U);
+      } else {
+        const std::vector<cd> M = two_site_matrix(S, C, I.rmat[C]);
+        dominant(M, mm, nn, neigenvalues, false, sv, U);
+      }
       for (double s : sv)
         if (s > 0.0 && std::isfinite(s) && s * I.dt / 2.0 > spawning_threshold) ++nadd;
       nadd = std::min(nadd, max_add);

@@ -309,6 +309,14 @@ for k in range(2):
     out["steps"].append(dict(values=float(max(abs(a - orc.expect(0, op).real) for a, op in zip(r.observables(), inp.ops))),
                              counts=[list(r.tdvp.expansion_counts()), list(orc.expansion_counts())],
                              hrank=bool(np.array_equal(r.hrank(), orc.hrank()[1:]))))
+# with a time-dependent update hook the programs use the dense copies (kept current by the hook)
+def keep(mode, op, t, dt, mat):
+    pass
+r.tdvp.set_op_update(keep); orc.set_op_update(keep)
+before = int(csr())
+r.step(); orc.step(inp.dt)
+out["csr_with_hook"] = int(csr()) - before
+out["hook_values"] = float(max(abs(a - orc.expect(0, op).real) for a, op in zip(r.observables(), inp.ops)))
 print(json.dumps(out))
 """
 
@@ -327,6 +335,7 @@ def test_driver_device_path_matches_oracle():
     assert res["first"].startswith("0 0 0 1 1  0 0 0 2 2 ")
     assert res["start"] == 0.0
     assert res["csr_ops"] > 0  # the blocks' sparse operators went through the CSR contractions
+    assert res["csr_with_hook"] == 0 and res["hook_values"] < 1e-10
     for s in res["steps"]:
         assert s["values"] < 1e-11 and s["hrank"], s
         assert s["counts"][0] == s["counts"][1], s

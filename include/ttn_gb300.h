@@ -42,7 +42,7 @@ enum {
   TTN_ENUMERIC = 3,   /* non-finite values or a failed Krylov / eigen solve */
   TTN_ECUDA = 4,      /* a CUDA runtime call failed */
   TTN_ETIMEOUT = 5,   /* a bounded device-side wait gave up */
-  TTN_ENOTSUP = 6     /* valid request outside what this build implements */
+  TTN_ENOTSUP = 6     /* valid request outside what the library implements */
 };
 
 /* precision of the contractions in the sweep */

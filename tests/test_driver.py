@@ -73,7 +73,7 @@ def test_first_step_matches_the_reference_example():
     agree with the reference's printed values to 1e-8; the two-site expansion count (which
     includes the start-up expansion sweeps) to 2 %; and almost every bond dimension.  The
     reference finds the dominant two-site directions with a 12-vector Krylov eigensolver
-    and this build with an exact eigensolver, so the bonds that sit at the spawning
+    and the oracle with an exact eigensolver, so the bonds that sit at the spawning
     threshold can differ by one."""
     from oracle.oracle import Oracle
     v = _golden()[WITH_BONDS[0]]
@@ -265,7 +265,7 @@ def test_sudden_cutoff_example_step_by_step():
     oracle, the first three printed rows of the reference -- observables to 1e-10, the
     expansion counts (start-up expansion sweeps included) exactly for two steps and to one
     bond decision in the third (9200 against 9201: one bond at the spawning threshold,
-    where the reference's Krylov estimate and this build's exact eigensolver part)."""
+    where the reference's Krylov estimate and the exact eigensolver part)."""
     from oracle.oracle import Oracle
     v = _golden()["beta_10/ohmic/spin_boson_sudden"]
     inp = D.parse_input(v["input"])

@@ -7,7 +7,7 @@ columns.
 
 Tolerances are those the oracle meets on the same inputs on the CPU
 (tests/test_driver.py): the reference picks expansion directions with a 12-vector Krylov
-eigensolver and this build with an exact one, so the states drift apart slowly -- by
+eigensolver and the device library an exact one, so the states drift apart slowly -- by
 3e-9 / 5e-8 / 3e-7 over the first three steps of the Debye case and by 3e-11 / 3e-10 over
 the first two of the sub-ohmic one; the sudden-cutoff case agrees to 1e-11 with identical
 expansion counts."""

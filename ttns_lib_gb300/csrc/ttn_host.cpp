@@ -135,7 +135,7 @@ struct Tree {
       }
     }
     for (int i = 0; i < n; ++i) {
-      TTN_REQUIRE(hrank[i] <= kMaxBond, TTN_ENOTSUP, "bond dimensions above 256 are not supported by this build");
+      TTN_REQUIRE(hrank[i] <= kMaxBond, TTN_ENOTSUP, "bond dimensions above 256 are not supported");
       if (!children[i].empty())
         for (int m = 0; m < nmodes[i]; ++m) {
           long long d2 = dims[i][m], d1 = dimen[i] * hrank[i] / d2;

@@ -36,7 +36,7 @@ from .model import SOPOperator, Topology, _flatten, _NTree
 
 ECUT = 3000.0          # energy cutoff of a combined block basis (spin_boson.cpp:242)
 NMAX_HIGH_TARGET = 250  # target block dimension above twice the high-frequency bound (:418)
-MAX_BOND = 256          # widest bond of the device build (kMaxBond, csrc/ttn_kernels.cuh)
+MAX_BOND = 256          # widest bond of the device library (kMaxBond, csrc/ttn_kernels.cuh)
 
 
 # --------------------------------------------------------------------------------------
@@ -510,14 +510,14 @@ def build_model(inp: DriverInput) -> DriverModel:
 def capacity_tree(inp: DriverInput, dims: Sequence[int], topo: Topology, log: Optional[TextIO] = None) -> np.ndarray:
     """Largest bond above every node: the tree of ``nspf capacity`` / ``nspf lower
     capacity`` (spin_boson.cpp:469-489), never below the starting bonds, and capped at the
-    device build's widest bond (``MAX_BOND``); a cap that bites is reported on ``log``."""
+    device library's widest bond (``MAX_BOND``); a cap that bites is reported on ``log``."""
     cap = driver_topology(inp.hsys.shape[0], dims, inp.nspf_capacity, inp.nspf_lower_capacity).hrank
     cap = np.maximum(cap, topo.hrank)
     if np.any(topo.hrank > MAX_BOND):
-        raise ValueError(f"starting bond dimensions above {MAX_BOND} are not supported by the device build")
+        raise ValueError(f"starting bond dimensions above {MAX_BOND} are not supported by the device library")
     if np.any(cap > MAX_BOND):
         (log or sys.stderr).write(f"bond capacities above {MAX_BOND} (up to {int(cap.max())}) are capped at "
-                                  f"{MAX_BOND}, the widest bond of the device build\n")
+                                  f"{MAX_BOND}, the widest bond of the device library\n")
         cap = np.minimum(cap, MAX_BOND)
     return cap
 

@@ -317,6 +317,18 @@ before = int(csr())
 r.step(); orc.step(inp.dt)
 out["csr_with_hook"] = int(csr()) - before
 out["hook_values"] = float(max(abs(a - orc.expect(0, op).real) for a, op in zip(r.observables(), inp.ops)))
+# the command-line entry: input file in, the reference's columns out
+import os, tempfile
+tmp = tempfile.mkdtemp()
+doc["output file"] = os.path.join(tmp, "sb.out")
+with open(os.path.join(tmp, "sb.in"), "w") as f:
+    json.dump(doc, f)
+out["cli_rc"] = D.main([os.path.join(tmp, "sb.in"), "--steps", "1"])
+out["cli_lines"] = open(doc["output file"]).read().splitlines()
+doc.pop("Hsys")
+with open(os.path.join(tmp, "bad.in"), "w") as f:
+    json.dump(doc, f)
+out["cli_bad_rc"] = D.main([os.path.join(tmp, "bad.in")])
 print(json.dumps(out))
 """
 
@@ -336,6 +348,11 @@ def test_driver_device_path_matches_oracle():
     assert res["start"] == 0.0
     assert res["csr_ops"] > 0  # the blocks' sparse operators went through the CSR contractions
     assert res["csr_with_hook"] == 0 and res["hook_values"] < 1e-10
+    lines = res["cli_lines"]
+    assert res["cli_rc"] == 0 and res["cli_bad_rc"] == 1
+    assert len(lines) == 3 and lines[0].startswith("0 0 0 1 1  0 0 0 2 2 ") and lines[2].startswith("nh_app: ")
+    f = lines[1].split()
+    assert float(f[0]) == 0.005 and len(f) == len(lines[0].split())
     for s in res["steps"]:
         assert s["values"] < 1e-11 and s["hrank"], s
         assert s["counts"][0] == s["counts"][1], s

@@ -108,3 +108,30 @@ def test_expansion_validates_its_arguments():
     mixed = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=8, precision=api.PREC_MIXED)
     with pytest.raises(api.TTNError):
         mixed.set_expansion(A, m.topology.hrank)
+
+
+def test_large_two_site_matrices_on_the_device():
+    """Bonds whose two-site matrix has both sides above 96 (here 144 x 144): the dominant
+    directions are found on the device (Gram matrix, Lanczos and the other side's vectors
+    by GEMM).  The bond dimensions equal the oracle's, the state is unchanged and every
+    non-root node stays an isometry (inside near-degenerate clusters of singular values
+    the two may pick different directions at rounding level)."""
+    from helpers import random_sop
+    topo = Topology(np.array([-1, 0, 1, 1, 0, 0]), np.array([1, 4, 12, 12, 12, 12]), np.array([-1, -1, 0, 1, 2, 3]),
+                    np.array([0, 0, 12, 12, 12, 12]))
+    rng = np.random.default_rng(9)
+    H = random_sop(rng, [12] * 4, nterms=8)
+    st = generic_state(topo, rng)
+    cap = np.array([1, 40, 12, 12, 12, 12])
+    orc = Oracle(topo, H, krylov_dim=10, krylov_tol=1e-12)
+    orc.set_state(st)
+    orc.set_expansion(cap, spawning_threshold=1e-7)
+    orc.expand_prepare(0.05)
+    A = api.httensor(topo)
+    A.set(st)
+    integ = api.subspace_expansion_projector_splitting_integrator(A, H, cap, krylov_dim=10, spawning_threshold=1e-7)
+    integ.dt = 0.05
+    integ.prepare(A)
+    assert np.array_equal(A.hrank(), orc.hrank()) and A.hrank()[1] > 4
+    assert np.linalg.norm(full_state(A.current_topology(), A.get()) - full_state(topo, st)) < 1e-12
+    assert max(np.max(np.abs(a.conj().T @ a - np.eye(a.shape[1]))) for a in A.get()[1:]) < 1e-12

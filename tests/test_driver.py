@@ -281,3 +281,34 @@ def test_sudden_cutoff_example_step_by_step():
         assert np.max(np.abs(vals - row["values"])) < 1e-10, (k, vals, row["values"])
         one, two = orc.expansion_counts()
         assert one == row["counts"][0] and abs(two - row["counts"][1]) <= (0 if k < 3 else 2), (k, two, row["counts"])
+
+
+def test_other_baths_and_input_forms():
+    """Gaussian and Jacobi-cutoff baths, a temperature given as T, a single observable
+    matrix, and the defaults of the optional entries: the model builds, the window and the
+    couplings follow the bath (sum pi g^2 = integral of the measure over the window)."""
+    from scipy.integrate import quad
+    base = {"Hsys": [[0, 1], [1, 0]], "Scoup": [[1, 0], [0, -1]], "psi0": [1, 0], "tmax": 0.1, "dt": 0.01,
+            "nspf": 4, "nspf lower": 2, "nmodes": 24, "maximum dimension": 6, "target dimension": 40,
+            "ops": [[1, 0], [0, -1]]}
+    cases = [
+        ({"type": "gaussian", "wc": 3.0, "alpha": 0.5, "T": 0.5}, 1e-4),
+        ({"type": "jacobi", "wc": 4.0, "alpha": 0.3, "s": 1.5, "q": 2.0}, 1e-4),
+        ({"type": "sudden", "wc": 4.0, "alpha": 0.3, "s": 0.5}, 1e-4),
+    ]
+    for b, tol in cases:
+        doc = dict(base, bath=b)
+        doc["bath integration error tolerance"] = tol
+        inp = D.parse_input(doc)
+        assert len(inp.ops) == 1 and inp.seed == 0 and inp.krylov_dim == 6 and inp.nmax_high == 6
+        assert inp.nspf_capacity == 4 and inp.minimum_unoccupied == 4
+        lo, hi = D.frequency_window(inp)
+        m = D.build_model(inp)
+        assert sum(len(bl.wk) for bl in m.blocks) == 24 and m.topology.nmodes == len(m.blocks) + 1
+        pts = [0.0] if lo < 0 else None
+        total = quad(lambda x: float(inp.bath.measure(np.float64(x))), lo, hi, points=pts, limit=400, epsrel=1e-12)[0]
+        assert np.sum(math.pi * m.gk ** 2) == pytest.approx(total, rel=1e-9)
+        if inp.bath.nonzero_temperature:
+            assert lo < 0 and np.any(m.wk < 0)
+        else:
+            assert lo == 0.0 and np.all(m.wk > 0)

@@ -70,6 +70,7 @@ def lib():
         L.orc_expansion_counts.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
         L.orc_init_product.argtypes = [P, dp, C.c_uint]
         L.orc_orthogonalise.argtypes = [P]
+        L.orc_set_krylov_stop.argtypes = [P, C.c_int]
         L.orc_adjoint.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_int, dp, C.c_int, dp, C.c_int, C.c_int,
                                   dp, dp, dp, dp]
         _lib = L
@@ -199,6 +200,11 @@ class Oracle:
         a, b = C.c_longlong(), C.c_longlong()
         self._check(lib().orc_expansion_counts(self.h, C.byref(a), C.byref(b)))
         return int(a.value), int(b.value)
+
+    def set_krylov_stop(self, mode: int):
+        """0: the full Krylov space of every sub-step (Expokit); 1: stop once the residual
+        estimate for the remaining interval is below the tolerance."""
+        self._check(lib().orc_set_krylov_stop(self.h, int(mode)))
 
     def orthogonalise(self):
         """Every non-root node made an isometry, the rest carried to the root."""

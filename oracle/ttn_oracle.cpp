@@ -585,6 +585,10 @@ struct Engine {
   Plan P;
   int krylov_dim = 12;
   double krylov_tol = 1e-12;
+  // 1: stop the Lanczos recurrence of a sub-step once the residual estimate of the space
+  // built so far, for the whole remaining interval, is below krylov_tol (the rule the
+  // reference's work counter shows); 0: always the full space with Expokit's step control
+  int krylov_stop = 0;
   std::vector<std::vector<cd>> A;                       // node tensors (dimen x hrank)
   std::vector<std::vector<std::vector<cd>>> spf, mf;    // [node][group] r x r
   std::vector<std::vector<cd>> rmat;                    // R tensor per node
@@ -815,6 +819,19 @@ struct Engine {
         bet[j + 1] = s;
         if (s <= 1e-14 * (1.0 + anorm)) { mb = j + 1; k1 = 0; t_step = t_out - t_now; break; }
         for (size_t i = 0; i < n; ++i) V[j + 1][i] = p[i] / s;
+        if (krylov_stop && j + 1 < m) {
+          // residual estimate beta * beta_{j+1} * |e_j^T exp(c tau T_{j+1}) e_1| for the
+          // remaining interval tau, with the (j+1)-dimensional tridiagonal
+          const int jj = j + 1;
+          std::vector<double> dd(alpha.begin(), alpha.begin() + jj), ee(std::max(jj - 1, 1)), zz((size_t)jj * jj);
+          for (int i = 0; i + 1 < jj; ++i) ee[i] = bet[i + 1];
+          tql2(jj, dd.data(), ee.data(), zz.data());
+          const double rest = t_out - t_now;
+          const cd zc = cf * (sgn * rest);
+          cd last = 0.0;
+          for (int q = 0; q < jj; ++q) last += zz[(jj - 1) * jj + q] * std::exp(zc * dd[q]) * zz[q];
+          if (beta * s * std::abs(last) <= tol) { mb = jj; k1 = 0; t_step = rest; break; }
+        }
       }
       if (k1 != 0) {
         hop(V[m].data(), p.data()); ++napps;
@@ -1362,6 +1379,13 @@ int orc_prepare(void* p) {
 }
 double orc_t(void* p) { OrcHandle* h = (OrcHandle*)p; return h->E.nsteps * h->E.dt; }
 long long orc_nh(void* p) { return ((OrcHandle*)p)->E.nh; }
+int orc_set_krylov_stop(void* p, int mode) {
+  OrcHandle* h = (OrcHandle*)p;
+  ORC_TRY(h, {
+    ORC_REQUIRE(mode == 0 || mode == 1, "Krylov stop rule: 0 (full space) or 1 (residual)");
+    h->E.krylov_stop = mode;
+  })
+}
 int orc_orthogonalise(void* p) {
   OrcHandle* h = (OrcHandle*)p;
   ORC_TRY(h, { h->E.orthogonalise(); })

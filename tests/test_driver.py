@@ -312,3 +312,30 @@ def test_other_baths_and_input_forms():
             assert lo < 0 and np.any(m.wk < 0)
         else:
             assert lo == 0.0 and np.all(m.wk > 0)
+
+
+def test_residual_stop_reproduces_the_reference_work_counter():
+    """With the Lanczos recurrence ended on the residual estimate (Krylov stop rule 1) the
+    oracle's H applications per node on the sudden-cutoff example follow the reference's
+    printed counter (55.7, 70.5, 85.4 after three steps) to 5 %, where the full-space
+    Expokit scheme counts 156, 182 and 208, and the observables still match the
+    reference's to 1e-10."""
+    from oracle.oracle import Oracle
+    v = _golden()["beta_10/ohmic/spin_boson_sudden"]
+    inp = D.parse_input(v["input"])
+    m = D.build_model(inp)
+    orc = Oracle(m.topology, m.hamiltonian, krylov_dim=inp.krylov_dim, krylov_tol=inp.krylov_tolerance)
+    orc.set_krylov_stop(1)
+    orc.init_product(inp.psi0, inp.seed)
+    orc.set_expansion(m.capacity, spawning_threshold=inp.spawning_parameter,
+                      unoccupied_threshold=inp.unoccupied_threshold, minimum_unoccupied=inp.minimum_unoccupied, seed=0)
+    for k in (1, 2, 3):
+        orc.step(inp.dt)
+        row = v["rows"][k]
+        vals = np.array([orc.expect(0, op).real for op in inp.ops])
+        assert np.max(np.abs(vals - row["values"])) < 1e-10, (k, vals, row["values"])
+        nh = orc.nh_applications / m.topology.nnodes
+        assert abs(nh - row["nh_per_node"]) < 0.05 * row["nh_per_node"], (k, nh, row["nh_per_node"])
+        assert abs(orc.expansion_counts()[1] - row["counts"][1]) <= 3
+    with pytest.raises(RuntimeError):
+        orc.set_krylov_stop(2)

@@ -253,3 +253,34 @@ def test_device_matches_golden_trajectory():
         dev(A, m.sop, -1j)
         assert abs(dev.mel()(sb.SZ, 0, A).real - g["sz"][k]) < 1e-11, k
         assert abs(dev.mel()(sb.SX, 0, A).real - g["sx"][k]) < 1e-11, k
+
+
+def test_residual_krylov_stop_matches_oracle():
+    """Krylov stop rule 1 (the Lanczos recurrence ends on the residual estimate for the
+    remaining interval): the device follows the oracle with the same rule to 1e-10 over
+    six steps from a generic state, applies H far less often than the full-space rule, and
+    stays within 1e-9 of the full-space trajectory."""
+    w, c = sb.ohmic_modes(8, 0.5, 5.0)
+    m = sb.build_from_modes(w, c, 6, 6, 0.3, 1.0)
+    st = generic_state(m.topology, np.random.default_rng(17))
+    orc = Oracle(m.topology, m.sop, krylov_dim=12, krylov_tol=1e-12)
+    orc.set_state(st)
+    orc.set_krylov_stop(1)
+    A, B = api.httensor(m.topology), api.httensor(m.topology)
+    A.set(st)
+    B.set(st)
+    ia = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=12, krylov_tolerance=1e-12)
+    ib = api.fixed_step_projector_splitting_integrator(B, m.sop, krylov_dim=12, krylov_tolerance=1e-12)
+    ia.set_krylov_stop(1)
+    ia.dt = ib.dt = 0.05
+    for _ in range(6):
+        ia(A)
+        ib(B)
+        orc.step(0.05)
+    assert max(np.max(np.abs(a - b)) for a, b in zip(A.get(), orc.get_state())) < 1e-10
+    assert abs(ia.nh_applications() - orc.nh_applications) <= 0.02 * orc.nh_applications
+    assert ia.nh_applications() < 0.8 * ib.nh_applications()
+    assert abs(ia.mel()(sb.SZ, 0, A).real - ib.mel()(sb.SZ, 0, B).real) < 1e-9
+    mixed = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=12, precision=api.PREC_MIXED)
+    with pytest.raises(api.TTNError):
+        mixed.set_krylov_stop(1)

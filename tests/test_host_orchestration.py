@@ -238,6 +238,17 @@ io.orthogonalise(Ao); orc.orthogonalise()
 for _ in range(2):
     io(Ao); orc.step(0.05)
 out["plain_orthogonalise_steps"] = float(max(np.max(np.abs(a - b)) for a, b in zip(Ao.get(), orc.get_state())))
+# the residual stop rule reaches the device library (the double's exponential is exact, the
+# oracle's within the Krylov tolerance)
+sk = generic_state(mt.topology, np.random.default_rng(5))
+orc = Oracle(mt.topology, mt.sop, krylov_dim=10, krylov_tol=1e-13); orc.set_state(sk); orc.set_krylov_stop(1)
+Ak = api.httensor(mt.topology, device=0); Ak.set(sk)
+ik = api.fixed_step_projector_splitting_integrator(Ak, mt.sop, krylov_dim=10, krylov_tolerance=1e-13)
+ik.set_krylov_stop(1)
+ik.dt = 0.05
+for _ in range(3):
+    ik(Ak); orc.step(0.05)
+out["plain_krylov_stop"] = float(max(np.max(np.abs(a - b)) for a, b in zip(Ak.get(), orc.get_state())))
 # bonds wider than the cooperative QR kernels (70 > 64): the wide QR route in both gauge moves
 import ctypes
 from ttns_lib_gb300.model import Topology

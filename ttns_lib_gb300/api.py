@@ -79,6 +79,7 @@ SIGNATURES = {
     "ttn_integrator_nh_applications": (_I, [_P, _LLP]),
     "ttn_integrator_expansion_counts": (_I, [_P, _LLP, _LLP]),
     "ttn_state_orthogonalise": (_I, [_P, _P]),
+    "ttn_integrator_set_krylov_stop": (_I, [_P, _I]),
     "ttn_integrator_reset": (_I, [_P]),
     "ttn_integrator_synchronize": (_I, [_P]),
     "ttn_integrator_prepare": (_I, [_P, _P]),
@@ -361,6 +362,11 @@ class fixed_step_projector_splitting_integrator:
         out = C.c_longlong()
         _check(lib().ttn_integrator_nh_applications(self.h, C.byref(out)))
         return out.value
+
+    def set_krylov_stop(self, mode: int):
+        """0: the full Krylov space of every sub-step (default); 1: stop on the residual
+        estimate for the remaining interval (the reference's rule)."""
+        _check(lib().ttn_integrator_set_krylov_stop(self.h, int(mode)))
 
     def orthogonalise(self, A: httensor):
         """orthogonaliser(A): every non-root node of A made an isometry, the state unchanged."""

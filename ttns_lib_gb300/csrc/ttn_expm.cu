@@ -625,6 +625,30 @@ __device__ bool warp_expm_e1(int mb, bool aug, double betm, double2 zc, CtlSmem&
   return true;
 }
 
+// The residual stop of a Lanczos recurrence, by warp 0 of block 0 after step jj - 1: ends
+// the recurrence at dimension jj (as an exact breakdown does) when
+// beta_0 beta_jj |e_{jj-1}^T exp(c tau T_jj) e_1| <= tol for the remaining interval tau.
+// Kept out of line so that the registers of the Lanczos loop do not grow.
+__device__ __noinline__ void residual_stop(KrylovCtl* ctl, int jj, int m, double beta, CtlSmem& S) {
+  const int lane = threadIdx.x & 31;
+  for (int i = lane; i < jj; i += 32) {
+    S.d[i] = ctl->alpha[i];
+    S.e[i] = ctl->bet[i];
+  }
+  __syncwarp();
+  const double rest = ctl->t_out - ctl->t_now;
+  const double2 zc = cscale(ctl->sgn * rest, make_double2(ctl->cf_re, ctl->cf_im));
+  const bool ok = warp_expm_e1(jj, false, 0.0, zc, S);
+  if (lane == 0 && ok && ctl->mb == m) {
+    const double2 last = S.x[jj - 1];
+    if (ctl->beta * beta * hypot(last.x, last.y) <= ctl->tol) {
+      ctl->mb = jj;
+      ctl->k1 = 0;
+    }
+  }
+  __syncwarp();
+}
+
 // Expokit step control by warp 0 of block 0.
 __device__ void control(const ExpmArgs& a, CtlSmem& S) {
   KrylovCtl* ctl = a.ctl;
@@ -986,6 +1010,12 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
           }
           if (!isfinite(beta)) ctl->err |= 2;
         }
+        // residual stop: the (j+1)-dimensional space is enough for the whole remaining
+        // interval once beta_0 beta_{j+1} |e_j^T exp(c tau T_{j+1}) e_1| <= tol; it ends the
+        // recurrence like an exact breakdown (mb = j + 1, no error-estimate product), so
+        // every CTA leaves the loop at the same step after the next grid barrier
+        if (a.krylov_stop && !a.mixed && blockIdx.x == 0 && warp == 0 && !brk && j + 1 < m)
+          residual_stop(ctl, j + 1, m, beta, cs);
         __syncthreads();
       }
       pc.mark(4);

@@ -54,6 +54,8 @@ struct ExpmArgs {
   double tau, cf_re, cf_im, tol;
   int mixed;             // 1: the program contains tensor-core contractions (TMEM + big smem)
   int apply_only;        // 1: apply the program once to y (result in p) and return
+  int krylov_stop;       // 1: end a sub-step's Lanczos recurrence once the residual estimate
+                         //    for the remaining interval is below tol (FP64 programs only)
   unsigned long long* phase;  // optional: ns spent per phase as seen by CTA 0 (kPhases slots)
   uint32_t* tc_img;      // operator images of the tensor-core ops (kTcImageBytes each)
   MvOp op1;              // the program when prog is null (one contraction, apply_only)

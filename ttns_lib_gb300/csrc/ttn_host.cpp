@@ -444,6 +444,7 @@ struct Integrator {
   double2 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w4 = nullptr, *V = nullptr, *p = nullptr,
           *gws = nullptr, *qtau = nullptr, *scal = nullptr;
   WideQr* wide = nullptr;  // cuSOLVER QR of matricisations wider than kQrMaxCols
+  int krylov_stop = 0;     // 1: Lanczos recurrences end on the residual estimate (FP64 only)
   size_t gws_bytes = 0;
   long long maxsize = 0, ldv = 0;
   KrylovCtl* ctl = nullptr;
@@ -1248,6 +1249,7 @@ struct Integrator {
     a.flops_total = tally ? flops_dev : nullptr;
     a.flops_per_app = (kind == 0) ? heff_flops(nd) : kbond_flops(nd);
     a.m = cfg.krylov_dim; a.tau = tau; a.cf_re = cf.real(); a.cf_im = cf.imag(); a.tol = cfg.krylov_tol;
+    a.krylov_stop = krylov_stop;
     a.mixed = (kind == 0 ? heff_tc[nd] : kbond_tc[nd]) ? 1 : 0;
     a.tail_barrier = (kind == 0 ? heff_tail[nd] : kbond_tail[nd]) ? 1 : 0;
     a.apply_only = apply_only ? 1 : 0;
@@ -1970,6 +1972,13 @@ int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out) {
   *out = it->I.nh;
   TTN_API_END
 }
+int ttn_integrator_set_krylov_stop(ttn_integrator* it, int mode) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it && (mode == 0 || mode == 1), TTN_EINVAL, "Krylov stop rule: 0 (full space) or 1 (residual)");
+  TTN_REQUIRE(mode == 0 || !it->I.mixed, TTN_EINVAL, "the residual stop needs an FP64 integrator");
+  it->I.krylov_stop = mode;
+  TTN_API_END
+}
 int ttn_state_orthogonalise(ttn_integrator* it, ttn_state* psi) {
   TTN_API_BEGIN
   TTN_REQUIRE(it && psi, TTN_EINVAL, "null argument");
@@ -2220,6 +2229,7 @@ int ttn_adjoint_grad(ttn_integrator* it, ttn_state* psi, double dt, double coeff
   TTN_REQUIRE(!I.mixed, TTN_EINVAL, "the adjoint sweep needs an FP64 integrator (TTN_PREC_FP64)");
   TTN_REQUIRE(I.nsteps == 0, TTN_EINVAL, "the adjoint sweep starts from step 0 (a fresh or reset integrator)");
   TTN_REQUIRE(!it->X, TTN_EINVAL, "the adjoint sweep needs fixed bond dimensions (no subspace expansion)");
+  TTN_REQUIRE(!I.krylov_stop, TTN_EINVAL, "the adjoint sweep uses the full Krylov space (Krylov stop rule 0)");
   TTN_REQUIRE(!I.op_update_fn, TTN_EINVAL, "the adjoint sweep needs time-independent operators");
   for (int k = 0; k < nsteps; ++k) TTN_REQUIRE(std::isfinite(weights[k]), TTN_EINVAL, "non-finite weight");
   CK(cudaSetDevice(I.device));

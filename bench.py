@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--config", default="c3")
     ap.add_argument("--instances", type=int, default=32, help="instances of the batched form (--config c4)")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--krylov-stop", default="full", choices=["full", "residual"],
+                    help="how FP64 Krylov sub-steps end: the full space (default) or the residual estimate")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--override-n", type=int, default=None,
@@ -280,6 +282,8 @@ def run_ours(args):
         A.init_product(psi0, seed=0)
         it = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=cfg["krylov_dim"],
                                                            krylov_tolerance=1e-12, precision=precision)
+        if args.krylov_stop == "residual" and precision == api.PREC_FP64:
+            it.set_krylov_stop(1)
         it.dt = cfg["dt"]
         it.prepare(A)
         return A, it
@@ -397,7 +401,7 @@ def run_ours(args):
         "dtype": "c128" if prec_name == "fp64" else
                  "c128 state and Krylov; rank-64 contractions on tensor cores from exact bf16 integer slices",
         "data": "synthetic (formula-generated spin-boson bath; std::mt19937 unoccupied SPFs)",
-        "config": workload_config(args.config, cfg, prec_name, over),
+        "config": dict(workload_config(args.config, cfg, prec_name, over), krylov_stop=args.krylov_stop),
         "roofline": roof,
         "e2e": {"value": world * args.steps / e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},

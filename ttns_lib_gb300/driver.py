@@ -558,7 +558,7 @@ class SpinBosonRun:
     """The device state, Hamiltonian and subspace-expanding integrator of one input file
     (spin_boson.cpp:584-662), stepped one row at a time."""
 
-    def __init__(self, inp: DriverInput, model: Optional[DriverModel] = None, device: int = 0):
+    def __init__(self, inp: DriverInput, model: Optional[DriverModel] = None, device: int = 0, krylov_stop: int = 0):
         from . import api
         self.inp = inp
         self.model = model if model is not None else build_model(inp)
@@ -569,6 +569,8 @@ class SpinBosonRun:
             self.A, m.hamiltonian, m.capacity, krylov_dim=inp.krylov_dim, krylov_tolerance=inp.krylov_tolerance,
             spawning_threshold=inp.spawning_parameter, unoccupied_threshold=inp.unoccupied_threshold,
             minimum_unoccupied=int(inp.minimum_unoccupied), seed=0, device=device)
+        if krylov_stop:
+            self.tdvp.set_krylov_stop(krylov_stop)
         self.tdvp.dt = inp.dt
         self.mel = self.tdvp.mel()
         self.nnodes = m.topology.nnodes
@@ -598,9 +600,9 @@ class SpinBosonRun:
 
 
 def run(inp: DriverInput, out: TextIO, device: int = 0, max_steps: Optional[int] = None,
-        model: Optional[DriverModel] = None) -> SpinBosonRun:
+        model: Optional[DriverModel] = None, krylov_stop: int = 0) -> SpinBosonRun:
     """Step to tmax (or ``max_steps`` rows) writing the reference's columns to ``out``."""
-    r = SpinBosonRun(inp, model, device)
+    r = SpinBosonRun(inp, model, device, krylov_stop)
     out.write(r.first_row())
     n = 0
     while r.t < inp.tmax and (max_steps is None or n < max_steps):
@@ -643,6 +645,8 @@ def main(argv: Optional[Sequence[str]] = None) -> int:
     ap.add_argument("--steps", type=int, default=None, help="stop after this many rows")
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--output", default=None, help="overrides the input's output file")
+    ap.add_argument("--krylov-stop", default="full", choices=["full", "residual"],
+                    help="how Krylov sub-steps end: the full space or, as the reference, the residual estimate")
     a = ap.parse_args(argv)
     try:
         with open(a.input) as f:
@@ -666,7 +670,8 @@ def main(argv: Optional[Sequence[str]] = None) -> int:
             topo = driver_topology(n, dims, inp.nspf, inp.nspf_lower)
             model = DriverModel(inp, wk, gk, blocks, topo, capacity_tree(inp, dims, topo), build_hamiltonian(inp, blocks))
             sys.stdout.write(f"{len(blocks)}\n")
-            run(inp, out, device=a.device, max_steps=a.steps, model=model)
+            run(inp, out, device=a.device, max_steps=a.steps, model=model,
+                krylov_stop=1 if a.krylov_stop == "residual" else 0)
         finally:
             if out is not sys.stdout:
                 out.close()

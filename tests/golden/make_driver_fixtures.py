@@ -14,6 +14,8 @@ import json
 import os
 import sys
 
+# every printed row (t, observables, expansion counts, H applications per node) of these
+LONG = ["beta_10/ohmic/spin_boson_sudden"]
 CASES = [
     "beta_10/ohmic/spin_boson_debye",
     "beta_10/ohmic/spin_boson_exponential",
@@ -45,6 +47,9 @@ def main(ref):
             lines = [ln for ln in f.read().splitlines() if ln.strip() and not ln.startswith("nh_app")]
         rows = [parse_row(ln, nops) for ln in lines[:ROWS]]
         out[case] = {"input": doc, "rows": rows, "text": [ln + "\n" for ln in lines[:2]]}
+        if case in LONG:
+            out[case]["trajectory"] = [[r["t"]] + r["values"] + r["counts"] + [r["nh_per_node"]]
+                                       for r in (parse_row(ln, nops) for ln in lines)]
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "driver_examples.json")
     with open(dst, "w") as f:
         json.dump(out, f, separators=(",", ":"))

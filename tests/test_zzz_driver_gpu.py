@@ -33,14 +33,14 @@ def _check_rows(r, g, tols, count_tol):
     for k, tol in enumerate(tols):
         line = r.step()
         row = g["rows"][k + 1]
-        assert r.t == row["t"]
+        assert abs(r.t - row["t"]) < 1e-12  # printed with 16 digits
         vals = np.array(r.observables())
         assert np.max(np.abs(vals - np.array(row["values"]))) < tol, (k, vals, row["values"])
         one, two = r.tdvp.expansion_counts()
         assert one == row["counts"][0]
         assert abs(two - row["counts"][1]) <= count_tol * row["counts"][1], (k, two, row["counts"])
         f = line.split()
-        assert float(f[0]) == row["t"] and len(f) == len(g["text"][1].split())
+        assert abs(float(f[0]) - row["t"]) < 1e-12 and len(f) == len(g["text"][1].split())
         if row["hrank"] and k == 0:
             # after the first step 96 % of the oracle's bonds equal the reference's; later
             # steps drift further apart (83 % after the second), so only the first is checked
@@ -81,7 +81,7 @@ def test_command_line_writes_the_reference_columns(tmp_path):
     for k in (1, 2):
         f = lines[k].split()
         row = g["rows"][k]
-        assert float(f[0]) == row["t"]
+        assert abs(float(f[0]) - row["t"]) < 1e-12
         assert np.max(np.abs(np.array([float(x) for x in f[1:5]]) - row["values"])) < 1e-9
         assert abs(int(f[6]) - row["counts"][1]) <= 0.01 * row["counts"][1]
         assert len(f) == len(g["text"][1].split())
@@ -142,6 +142,6 @@ def test_whole_sudden_cutoff_run():
     worst = 0.0
     for k in range(1, len(traj)):
         r.step()
-        assert r.t == traj[k][0]
+        assert abs(r.t - traj[k][0]) < 1e-12  # printed with 16 digits
         worst = max(worst, float(np.max(np.abs(np.array(r.observables()) - traj[k][1:5]))))
     assert worst < 1e-6, worst

@@ -15,7 +15,7 @@ import os
 import sys
 
 # every printed row (t, observables, expansion counts, H applications per node) of these
-LONG = ["beta_10/ohmic/spin_boson_sudden"]
+LONG = ["beta_10/ohmic/spin_boson_sudden", "beta_10/ohmic/spin_boson_debye"]
 CASES = [
     "beta_10/ohmic/spin_boson_debye",
     "beta_10/ohmic/spin_boson_exponential",

@@ -145,3 +145,23 @@ def test_whole_sudden_cutoff_run():
         assert abs(r.t - traj[k][0]) < 1e-12  # printed with 16 digits
         worst = max(worst, float(np.max(np.abs(np.array(r.observables()) - traj[k][1:5]))))
     assert worst < 1e-6, worst
+
+
+def test_whole_debye_run_with_bonds_past_64():
+    """The reference's whole printed run of beta_10/ohmic/spin_boson_debye (36 steps to
+    t = 0.18): its bonds grow past 64 (to 161 at the top), so the gauge moves take the wide
+    QR route and the expansion the device eigensolver.  Every row's observables within 1e-4
+    of the reference's (both runs are converged to the spawning threshold, and the two
+    expansions choose their directions differently, so the trajectories part slowly); the
+    bonds must have grown past 64."""
+    g = _case("beta_10/ohmic/spin_boson_debye")
+    traj = g["trajectory"]
+    inp = D.parse_input(g["input"])
+    r = D.SpinBosonRun(inp, device=0)
+    worst = 0.0
+    for k in range(1, len(traj)):
+        r.step()
+        assert abs(r.t - traj[k][0]) < 1e-12
+        worst = max(worst, float(np.max(np.abs(np.array(r.observables()) - traj[k][1:5]))))
+    assert worst < 1e-4, worst
+    assert r.hrank().max() > 64

@@ -5,7 +5,8 @@
 // test suite and is compared with the oracle.  Linked only into the library that
 // tests/test_host_orchestration.py builds under tests/host_double/_build; the package
 // never loads it (its library is the CUDA build, which fails loudly when absent).
-//   * device memory is host memory; streams and events do nothing;
+//   * device memory is host memory (filled with NaN on allocation, as stale device
+//     memory may be); streams and events do nothing;
 //   * zgemm follows the operand maps of ZOperand / ZGemm literally;
 //   * the Householder QR is the oracle's (LAPACK zgeqrf / zungqr conventions);
 //   * the persistent Krylov kernel applies the term program (MODE / MF / AXPY / ZERO)
@@ -30,11 +31,23 @@ typedef std::complex<double> zc;
 static inline zc Z(double2 v) { return zc(v.x, v.y); }
 static inline double2 D(zc v) { return make_double2(v.real(), v.imag()); }
 
+static std::atomic<unsigned long long> g_alloc_calls{0};  // cudaMalloc/cudaFree/cudaMallocHost/cudaFreeHost
 extern "C" {
-cudaError_t cudaMalloc(void** p, size_t b) { *p = std::calloc(1, b ? b : 16); return cudaSuccess; }
-cudaError_t cudaFree(void* p) { std::free(p); return cudaSuccess; }
-cudaError_t cudaMallocHost(void** p, size_t b) { *p = std::calloc(1, b ? b : 16); return cudaSuccess; }
-cudaError_t cudaFreeHost(void* p) { std::free(p); return cudaSuccess; }
+// device memory starts as NaN (all bits set), not zero: cudaMalloc does not clear memory,
+// and a buffer that the orchestration reads before writing must show up here
+cudaError_t cudaMalloc(void** p, size_t b) {
+  ++g_alloc_calls;
+  *p = std::malloc(b ? b : 16);
+  if (*p) std::memset(*p, 0xff, b ? b : 16);
+  return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+}
+cudaError_t cudaFree(void* p) { ++g_alloc_calls; std::free(p); return cudaSuccess; }
+cudaError_t cudaMallocHost(void** p, size_t b) { ++g_alloc_calls; *p = std::calloc(1, b ? b : 16); return cudaSuccess; }
+cudaError_t cudaFreeHost(void* p) { ++g_alloc_calls; std::free(p); return cudaSuccess; }
+cudaError_t cudaGetDeviceCount(int* n) { *n = 1; return cudaSuccess; }
+cudaError_t cudaGetDevice(int* d) { *d = 0; return cudaSuccess; }
+// a file-scope __device__ array is a host array in this build: its address is the symbol's
+cudaError_t cudaGetSymbolAddress(void** p, const void* symbol) { *p = const_cast<void*>(symbol); return cudaSuccess; }
 cudaError_t cudaMemcpy(void* d, const void* s, size_t b, enum cudaMemcpyKind) { std::memmove(d, s, b); return cudaSuccess; }
 cudaError_t cudaMemcpyAsync(void* d, const void* s, size_t b, enum cudaMemcpyKind, cudaStream_t) { std::memmove(d, s, b); return cudaSuccess; }
 cudaError_t cudaMemset(void* d, int v, size_t b) { std::memset(d, v, b); return cudaSuccess; }
@@ -93,6 +106,21 @@ void zgemm(const ZGemm& g, double2* ws, size_t ws_bytes, cudaStream_t s) {
   ++g_launches;
 }
 int coop_qr_grid(long long m, int n) { (void)m; (void)n; return 1; }
+size_t coop_qr_scratch_bytes(int g) { return (size_t)(4 * g + 4 + 4 * (size_t)g * kQrMaxCols) * sizeof(double); }
+cudaError_t coop_qr_max_grid(int* out) { *out = 1; return cudaSuccess; }
+// the column-by-column cooperative QR of ttn_qr_noalloc: the oracle's Householder QR,
+// with its status word left at zero
+cudaError_t householder_qr_coop(double2* M, long long m, int n, double2* R, int Rt, double2* tau, double* scratch,
+                                GridBarrier* bar, int* err, int grid, cudaStream_t s) {
+  (void)tau; (void)scratch; (void)bar; (void)grid; (void)s;
+  std::vector<cd> Rr((size_t)n * n), t;
+  orc::householder_qr(reinterpret_cast<cd*>(M), (size_t)m, n, Rr.data(), t);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) R[(size_t)i * n + j] = D(Rt ? Rr[(size_t)j * n + i] : Rr[(size_t)i * n + j]);
+  *err = 0;
+  ++g_launches;
+  return cudaSuccess;
+}
 int qr_blocked_max_grid() { return 1; }
 size_t qr_blocked_scratch_bytes(int g) { (void)g; return 1024; }
 cudaError_t householder_qr_blocked(double2* M, long long m, int n, double2* R, int Rt, double2* tau, double* scratch,
@@ -302,7 +330,7 @@ cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s, int threads) 
   return cudaSuccess;
 }
 }  // namespace ttn
-extern "C" int ttn_qr_noalloc(int, int, double*, double*, void*, int) { return 1; }
+extern "C" unsigned long long mock_alloc_calls() { return g_alloc_calls.load(); }
 
 // how many QRs took the wide route (read by the host-orchestration test)
 extern "C" unsigned long long mock_wide_qr_count() { return ttn::g_wide_qr.load(); }

@@ -1047,14 +1047,23 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
     }
     grid_barrier(a.bar, a.err);
     pc.mark(6);
-    // ---- y = sum_q c_q V_q
+    // ---- y = sum_q c_q V_q over the basis vectors this sub-step wrote: V_0 .. V_m without a
+    // breakdown, V_0 .. V_{mb-1} after one (or after the residual stop).  The vectors past
+    // them hold whatever an earlier launch (or nothing) left there, and a zero coefficient
+    // times a stale non-finite value would still poison y.
     {
+      if (threadIdx.x == 0) {
+        const int mbq = *(volatile int*)&ctl->mb, k1q = *(volatile int*)&ctl->k1;
+        const int nq = mbq + (k1q > 1 ? k1q - 1 : 0);
+        s_mb = nq < 1 ? 1 : (nq > m + 1 ? m + 1 : nq);
+      }
       for (int q = threadIdx.x; q <= m; q += blockDim.x)
         red[q] = make_double2(ctl->coef[2 * q], ctl->coef[2 * q + 1]);
       __syncthreads();
+      const int nq = s_mb;
       for (long long i = tid; i < n; i += nthreads) {
         double2 s = make_double2(0.0, 0.0);
-        for (int q = 0; q <= m; ++q) s = cfma(red[q], a.V[(long long)q * a.ldv + i], s);
+        for (int q = 0; q < nq; ++q) s = cfma(red[q], a.V[(long long)q * a.ldv + i], s);
         a.y[i] = s;
       }
       __syncthreads();

@@ -299,7 +299,8 @@ int ttn_debug_qr(int m, int n, double* a, double* r, int device);
  * returns TTN_ECAPACITY.  The first call on a device looks the array up (set-up); make
  * it before any stream capture.  All calls share the array, so calls that overlap on
  * the GPU race.  Returns after the stream has finished the QR (TTN_ETIMEOUT if a grid
- * barrier gave up). */
+ * barrier gave up).  The calling thread's current device is the same on return as on
+ * entry. */
 int ttn_qr_noalloc(int m, int n, double* a, double* r, void* stream, int device);
 
 #ifdef __cplusplus

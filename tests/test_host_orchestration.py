@@ -23,7 +23,8 @@ CUDA_INC = "/usr/local/cuda/include"
 def _build():
     if shutil.which("g++") is None or not os.path.exists(os.path.join(CUDA_INC, "cuda_runtime_api.h")):
         pytest.skip("g++ or the CUDA headers are missing")
-    srcs = [os.path.join(ROOT, "ttns_lib_gb300", "csrc", "ttn_host.cpp"), os.path.join(HERE, "mock_cuda.cpp")]
+    srcs = [os.path.join(ROOT, "ttns_lib_gb300", "csrc", "ttn_host.cpp"),
+            os.path.join(ROOT, "ttns_lib_gb300", "csrc", "ttn_noalloc.cu"), os.path.join(HERE, "mock_cuda.cpp")]
     deps = srcs + [os.path.join(ROOT, "ttns_lib_gb300", "csrc", f) for f in os.listdir(os.path.join(ROOT, "ttns_lib_gb300", "csrc"))
                    if f.endswith((".cuh", ".hpp"))]
     deps += [os.path.join(ROOT, "include", "ttn_gb300.h"), os.path.join(ROOT, "oracle", "ttn_oracle.cpp"),
@@ -367,3 +368,44 @@ def test_driver_device_path_matches_oracle():
     for s in res["steps"]:
         assert s["values"] < 1e-11 and s["hrank"], s
         assert s["counts"][0] == s["counts"][1], s
+
+
+NOALLOC_CHILD = r"""
+import ctypes as C, json
+import numpy as np
+lib = C.CDLL({lib!r})
+lib.ttn_qr_noalloc.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+lib.mock_alloc_calls.restype = C.c_ulonglong
+rng = np.random.default_rng(5)
+out = {{}}
+before = lib.mock_alloc_calls()
+for call, (m, n) in enumerate([(96, 20), (64, 64)]):
+    a = rng.normal(size=(m, n)) + 1j * rng.normal(size=(m, n))
+    q = a.copy()
+    r = np.full((n, n), np.nan, dtype=np.complex128)
+    rc = lib.ttn_qr_noalloc(m, n, q.ctypes.data, r.ctypes.data, None, 0)
+    out["rc%d" % call] = rc
+    out["qr%d" % call] = float(np.abs(q @ r - a).max())
+    out["orth%d" % call] = float(np.abs(q.conj().T @ q - np.eye(n)).max())
+out["alloc_calls"] = int(lib.mock_alloc_calls() - before)
+wide = np.zeros((128, 65), dtype=np.complex128)
+rw = np.zeros((65, 65), dtype=np.complex128)
+out["rc_wide"] = lib.ttn_qr_noalloc(128, 65, wide.ctypes.data, rw.ctypes.data, None, 0)
+print(json.dumps(out))
+"""
+
+
+def test_noalloc_entry_point_allocates_nothing():
+    """ttn_qr_noalloc, built into the CPU test double, makes no cudaMalloc, cudaFree,
+    cudaMallocHost or cudaFreeHost call on its first (set-up) call or on the next one,
+    factorises correctly, and rejects more than 64 columns with TTN_ECAPACITY."""
+    lib = _build()
+    r = subprocess.run([sys.executable, "-c", NOALLOC_CHILD.format(lib=lib)], capture_output=True, text=True,
+                       timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-3000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    assert res["alloc_calls"] == 0, res
+    for call in range(2):
+        assert res["rc%d" % call] == 0, res
+        assert res["qr%d" % call] < 1e-12 and res["orth%d" % call] < 1e-12, res
+    assert res["rc_wide"] == 2, res  # TTN_ECAPACITY

@@ -1,9 +1,14 @@
 """ttn_qr_noalloc (workspace in a static device array, no device allocation) against the
 allocating QR entry point ttn_debug_qr, through the C-ABI, on two calls in a row.
 
-Both run the same cooperative kernel on the same grid, so the factors agree to rounding;
-the check uses the QR parity tolerance of the other device tests (relative 1e-12).
-Collected last so that it also runs after every other test has used the device.
+The two entry points run different kernels: ttn_qr_noalloc the column-by-column
+cooperative Householder QR (k_qr_coop), ttn_debug_qr the sweep's panel-blocked one
+(k_qr_blocked).  Both follow LAPACK's zgeqrf/zungqr conventions, so their factors agree to
+rounding; the check uses the QR parity tolerance of the other device tests (relative
+1e-12), and Q R = A and Q^H Q = I are checked on their own.  This file sorts after every
+other test file, so pytest collects it last: a run that stops at the first failure has
+run every other test before it.  That the entry point allocates nothing is checked on the
+CPU test double (tests/test_host_orchestration.py), which counts allocations.
 """
 import ctypes as C
 

@@ -679,12 +679,14 @@ size_t coop_qr_scratch_bytes(int max_grid) {
   return (size_t)(4 * max_grid + 4 + 2 * (size_t)max_grid * 2 * CQN) * sizeof(double);
 }
 
-int coop_qr_max_grid() {
+cudaError_t coop_qr_max_grid(int* out) {
   int dev = 0, sms = 0, per = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_qr_coop, CQT, 0);
-  return sms * (per < 1 ? 1 : per);
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_qr_coop, CQT, 0);
+  if (e != cudaSuccess) return e;
+  *out = sms * (per < 1 ? 1 : per);
+  return cudaSuccess;
 }
 
 int coop_qr_grid(long long m, int num_sms) {

@@ -72,8 +72,8 @@ constexpr int kKrylovMax = 64;   // largest Krylov dimension
 struct GridBarrier;
 size_t coop_qr_scratch_bytes(int max_grid);
 int coop_qr_grid(long long m, int num_sms);
-// co-resident CTAs of the cooperative QR on the current device
-int coop_qr_max_grid();
+// co-resident CTAs of the cooperative QR on the current device (in *out)
+cudaError_t coop_qr_max_grid(int* out);
 cudaError_t householder_qr_coop(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, double* scratch,
                                 GridBarrier* bar, int* err, int grid, cudaStream_t s);
 // Panel-blocked cooperative Householder QR (ttn_qr.cu), same conventions and arguments

@@ -76,13 +76,22 @@ const DeviceSetup& setup(int device) {
     if (coop_qr_scratch_bytes(kMaxGrid) > kPartBytes)
       throw Fail{TTN_ECAPACITY, "ttn_qr_noalloc: workspace smaller than the QR's partials"};
     check(cudaDeviceGetAttribute(&s.sms, cudaDevAttrMultiProcessorCount, device), "multiprocessor count");
-    s.max_grid = coop_qr_max_grid();
-    check(cudaGetLastError(), "occupancy query");
+    check(coop_qr_max_grid(&s.max_grid), "occupancy query");
     s.base = static_cast<unsigned char*>(p);
     s.ready = true;
   }
   return s;
 }
+
+// Puts back the caller's current device on every return path: the entry point works on
+// `device`, but the caller (a framework with its own notion of the current device) must
+// not find it changed afterwards.
+struct DeviceGuard {
+  int saved = -1;
+  ~DeviceGuard() {
+    if (saved >= 0) cudaSetDevice(saved);
+  }
+};
 
 }  // namespace
 }  // namespace ttn
@@ -101,6 +110,8 @@ extern "C" int ttn_qr_noalloc(int m, int n, double* a, double* r, void* stream, 
     check(cudaGetDeviceCount(&ndev), "device count");
     if (device < 0 || device >= ndev || device >= kMaxDevices)
       throw Fail{TTN_EINVAL, "ttn_qr_noalloc: no such device"};
+    DeviceGuard guard;
+    check(cudaGetDevice(&guard.saved), "cudaGetDevice");
     check(cudaSetDevice(device), "cudaSetDevice");
     const DeviceSetup& s = setup(device);
     cudaStream_t st = static_cast<cudaStream_t>(stream);

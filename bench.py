@@ -46,8 +46,12 @@ def parse():
     ap.add_argument("--config", default="c3")
     ap.add_argument("--instances", type=int, default=32, help="instances of the batched form (--config c4)")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
-    ap.add_argument("--krylov-stop", default="full", choices=["full", "residual"],
-                    help="how FP64 Krylov sub-steps end: the full space (default) or the residual estimate")
+    ap.add_argument("--krylov-stop", default="residual", choices=["full", "residual"],
+                    help="how Krylov sub-steps end: on the residual estimate for the remaining interval (the "
+                         "reference's rule, default) or after the full Krylov space")
+    ap.add_argument("--fp64-steps", type=int, default=3,
+                    help="timed steps of the FP64 comparison arm (after the same warm-up steps)")
+    ap.add_argument("--no-breakdown", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--override-n", type=int, default=None,
@@ -182,15 +186,19 @@ def upper_node(topo):
 
 
 # ---------------------------------------------------------------- CPU reference
-def cpu_sample(cfg_name: str, threads: int, seconds_hint: float = 20.0):
+def cpu_sample(cfg_name: str, threads: int, krylov_stop: int = 1):
     """Oracle sweep of a tree with the same node shapes and operators as the workload,
-    scaled to the workload's node counts.  Returns (steps_per_s, description)."""
+    extrapolated to the workload's node counts by per-node-shape times (the full 2049-node
+    sweep takes about a quarter of an hour on the host cores).  Returns (steps_per_s,
+    description, wall seconds of the sampled sweep)."""
     from oracle.oracle import Oracle
     from ttns_lib_gb300 import spin_boson as sb
     full, cfg = sb.build_config(cfg_name)
     n_small = 4 if cfg.get("beta") is not None else 8   # 8 bath modes: every node shape present
     small, _ = sb.build_config(cfg_name, N=n_small)
     orc = Oracle(small.topology, small.sop, krylov_dim=cfg["krylov_dim"], threads=threads)
+    if krylov_stop:
+        orc.set_krylov_stop(1)
     orc.set_state(sb.initial_state_numpy(small.topology, seed=0, psi0=np.array([1.0, 0.0])))
     orc.prepare()
     orc.sweep(cfg["dt"])          # move off the exactly rank-deficient start
@@ -212,8 +220,9 @@ def cpu_sample(cfg_name: str, threads: int, seconds_hint: float = 20.0):
         if k not in by_shape:
             raise RuntimeError(f"sample tree lacks node shape {k}")
         est += float(np.mean(by_shape[k]))
-    desc = (f"one oracle sweep of a {small.topology.nnodes}-node tree with the workload's node shapes and "
-            f"operators ({wall:.1f} s), per-node times scaled to the {full.topology.nnodes}-node workload")
+    desc = (f"extrapolated: one oracle sweep of a {small.topology.nnodes}-node tree with the workload's node "
+            f"shapes and operators ({wall:.1f} s of sweep), per-node-shape times summed over the "
+            f"{full.topology.nnodes} nodes of the workload; Krylov stop rule {'residual' if krylov_stop else 'full'}")
     return 1.0 / est, desc, wall
 
 
@@ -229,8 +238,9 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     vals = []
     desc = ""
+    stop = 1 if args.krylov_stop == "residual" else 0
     for k in range(args.warmup + args.steps):
-        v, desc, _ = cpu_sample(args.config, threads)
+        v, desc, _ = cpu_sample(args.config, threads, stop)
         if k >= args.warmup:
             vals.append(v)
     value = float(np.mean(vals))
@@ -241,8 +251,9 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128", "data": "synthetic (formula-generated spin-boson bath)",
         "impl": "reference",
-        "config": workload_config(args.config, cfg, "fp64 (CPU)"),
-        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port", "sample": desc},
+        "config": dict(workload_config(args.config, cfg, "fp64 (CPU)"), krylov_stop=args.krylov_stop),
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port", "sample": desc,
+                         "extrapolated": True},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference not buildable here (linalg/utils submodules absent); CPU restatement in oracle/ timed",
     }
@@ -282,7 +293,7 @@ def run_ours(args):
         A.init_product(psi0, seed=0)
         it = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=cfg["krylov_dim"],
                                                            krylov_tolerance=1e-12, precision=precision)
-        if args.krylov_stop == "residual" and precision == api.PREC_FP64:
+        if args.krylov_stop == "residual":
             it.set_krylov_stop(1)
         it.dt = cfg["dt"]
         it.prepare(A)
@@ -325,55 +336,71 @@ def run_ours(args):
                 "peak_source": f"bf16 dense, {src} (MEASURED_PEAKS.json)",
                 "ms_per_launch": k_ms, "flops_per_launch": k_fl}
 
+    # Timed steps.  Each step is run the way a drop-in caller that keeps the node tensors
+    # on the host runs it: the whole state goes up from pinned host memory, one sweep runs
+    # through the C-ABI, the state comes back down and <sz> is read.  `value` is the device
+    # time of the sweeps alone (CUDA events on the integrator's stream, the state already
+    # resident when each starts); `e2e` is the host wall clock of the same loop, copies
+    # included.
     sz_trace = []
     for _ in range(args.warmup):
         tdvp(A, m.sop, -1j)
         sz_trace.append(tdvp.mel()(sb.SZ, 0, A).real)
+    host = api.PinnedBuffer(topo.state_size())
+    A.download_to(host)
     tdvp.synchronize()
     dist.barrier()
     clocks = Clocks(device)
     l0 = api.launch_count()
     f0 = tdvp.flops()
+    io0 = tdvp.io_bytes()
     nvtx = Nvtx()
     clocks.start()
     nvtx.push("ttn_timed")
-    tdvp.timer_start()
+    ms = 0.0
+    t0 = time.perf_counter()
     for _ in range(args.steps):
+        A.upload_from(host)
+        tdvp.timer_start()
         tdvp(A, m.sop, -1j)
-    ms = tdvp.timer_stop()
+        ms += tdvp.timer_stop()
+        A.download_to(host)
+        sz_trace.append(tdvp.mel()(sb.SZ, 0, A).real)
+    e2e_s = time.perf_counter() - t0
     nvtx.pop()
     clk = clocks.stop()
     launches = api.launch_count() - l0
     flops_step = (tdvp.flops() - f0) / args.steps
-    sz_trace.append(tdvp.mel()(sb.SZ, 0, A).real)   # after the timed block (outside it)
-    n_compared = len(sz_trace)
+    io1 = tdvp.io_bytes()
     dist.barrier()
     ms_max = dist.max(ms)
-    value = world * args.steps / (ms_max / 1e3)
-
-    # End to end through the C-ABI with host buffers, the way a drop-in caller that keeps
-    # the node tensors on the host would call it: per step the whole state goes up from
-    # pinned memory, one sweep runs, the state comes back down and <sz> is read.
-    host = api.PinnedBuffer(topo.state_size())
-    A.download_to(host)
-    io0 = tdvp.io_bytes()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        A.upload_from(host)
-        tdvp(A, m.sop, -1j)
-        A.download_to(host)
-        sz_trace.append(tdvp.mel()(sb.SZ, 0, A).real)
-    e2e_s = time.perf_counter() - t0
     e2e = dist.max(e2e_s)
-    io1 = tdvp.io_bytes()
+    value = world * args.steps / (ms_max / 1e3)
     h2d = host.nbytes + (io1[0] - io0[0]) // args.steps
     d2h = host.nbytes + (io1[1] - io0[1]) // args.steps
+    del host
 
-    # The FP64 path on the same start state over the same warm-up and timed steps: its
-    # step rate and the largest |<sz>(mixed) - <sz>(FP64)| over the compared points.
+    # Where a step's time goes: one more step (after the timed ones, not counted) with the
+    # synchronising per-operation breakdown on, by operation and node size.
+    breakdown = None
+    if not args.no_breakdown:
+        tdvp.set_profiling(True)
+        t0 = time.perf_counter()
+        tdvp(A, m.sop, -1j)
+        wall_prof = time.perf_counter() - t0
+        prof = tdvp.profile()
+        tdvp.set_profiling(False)
+        breakdown = {"wall_s": wall_prof, "note": "one extra step with a stream synchronisation after every "
+                     "operation; seconds and calls per operation[node-size class]",
+                     "ops": {k: {"s": round(v[0], 4), "calls": v[1]} for k, v in
+                             sorted(prof.items(), key=lambda kv: -kv[1][0])}}
+
+    # The FP64 path from the same start state: the same warm-up steps, then a bounded
+    # number of timed steps; its step rate and the largest |<sz>(mixed) - <sz>(FP64)| over
+    # the steps both ran.
     fp64 = None
     if prec_name == "mixed" and not args.no_fp64_compare:
-        del host
+        k64 = max(1, min(args.steps, args.fp64_steps))
         A64, t64 = make(api.PREC_FP64)
         sz64 = []
         for _ in range(args.warmup):
@@ -381,17 +408,20 @@ def run_ours(args):
             sz64.append(t64.mel()(sb.SZ, 0, A64).real)
         t64.synchronize()
         dist.barrier()
-        t64.timer_start()
-        for _ in range(args.steps):
+        ms64 = 0.0
+        for _ in range(k64):
+            t64.timer_start()
             t64(A64, m.sop, -1j)
-        ms64 = dist.max(t64.timer_stop())
-        sz64.append(t64.mel()(sb.SZ, 0, A64).real)
-        dsz = max(abs(a - b) for a, b in zip(sz_trace[:n_compared], sz64))
-        v64 = world * args.steps / (ms64 / 1e3)
-        fp64 = {"value": v64, "unit": "steps/s", "ms_per_step": ms64 / args.steps,
+            ms64 += t64.timer_stop()
+            sz64.append(t64.mel()(sb.SZ, 0, A64).real)
+        ms64 = dist.max(ms64)
+        dsz = max(abs(a - b) for a, b in zip(sz_trace, sz64))
+        v64 = world * k64 / (ms64 / 1e3)
+        fp64 = {"value": v64, "unit": "steps/s", "ms_per_step": ms64 / k64, "timed_steps": k64,
                 "mixed_over_fp64": value / v64, "max_abs_dsz": dsz, "dsz_bound": 1e-6,
-                "within_bound": bool(dsz <= 1e-6), "compared_points": n_compared,
-                "compared": "<sz> after each warm-up step and after the timed steps, same start state"}
+                "within_bound": bool(dsz <= 1e-6), "compared_points": len(sz64),
+                "compared": "<sz> after each warm-up step and each timed FP64 step, same start state, "
+                            "same Krylov stop rule"}
         del A64, t64
 
     line = {
@@ -407,6 +437,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clk,
+        "breakdown": breakdown,
         "algorithmic_tflop_per_step": flops_step / 1e12,
         "sz_last": sz_trace[-1] if sz_trace else None,
         "parallelism": "replicas only (the sweep is a sequential chain over the tree)",
@@ -417,8 +448,9 @@ def run_ours(args):
         line["fp64"] = fp64
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, desc, _ = cpu_sample(args.config, threads)
-        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": threads, "kind": "port", "sample": desc}
+        v, desc, _ = cpu_sample(args.config, threads, 1 if args.krylov_stop == "residual" else 0)
+        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": threads, "kind": "port", "sample": desc,
+                                "extrapolated": True}
     if rank == 0:
         print(json.dumps(line), flush=True)
     dist.close()

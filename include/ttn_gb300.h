@@ -265,7 +265,11 @@ int ttn_debug_get_env(ttn_integrator* it, int node, int group, int which, double
  * returns milliseconds and algorithmic flops per repetition */
 int ttn_bench_node_op(ttn_integrator* it, ttn_state* psi, int node, int kind, int reps, double* ms_per_rep,
                       double* flops_per_rep);
-/* With TTN_PROFILE set in the environment, synchronising wall-clock seconds and
+/* Turns the synchronising per-operation breakdown below on (1) or off (0) and clears it
+ * (TTN_PROFILE in the environment turns it on at creation).  It synchronises the stream
+ * after every operation, so a step runs slower while it is on. */
+int ttn_integrator_set_profiling(ttn_integrator* it, int on);
+/* With the breakdown on (TTN_PROFILE or ttn_integrator_set_profiling), synchronising wall-clock seconds and
  * call counts per operation kind (8: node exponential, bond exponential, root-to-leaf
  * QR, leaf-to-root QR, mean-field update, spf update, apply-to-parent,
  * apply-from-parent) and node-size class (4: <1K, <64K, <1M, >=1M elements);

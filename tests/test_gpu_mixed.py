@@ -103,3 +103,28 @@ def test_mixed_sweeps_track_fp64():
     assert worst <= 1e-8, worst
     A, it = its["mixed"]
     assert abs(it.mel()(A) - 1.0) < 1e-10
+
+
+def test_mixed_residual_stop_tracks_the_oracle():
+    """Krylov stop rule 1 (the Lanczos recurrence ends on the residual estimate, the
+    reference's rule) in mixed precision: six sweeps of the rank-64 tree from a generic
+    state follow the oracle with the same rule to 1e-8 in <sigma_z> and 1e-7 in every node
+    tensor, with the oracle's count of H applications to 2 %."""
+    m, cfg = rank64_tree()
+    topo = m.topology
+    st = generic_state(topo, np.random.default_rng(15))
+    orc = Oracle(topo, m.sop, krylov_dim=cfg["krylov_dim"], krylov_tol=1e-12)
+    orc.set_state(st)
+    orc.set_krylov_stop(1)
+    A = api.httensor(topo)
+    A.set(st)
+    it = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=cfg["krylov_dim"], krylov_tolerance=1e-12,
+                                                      precision=api.PREC_MIXED)
+    it.set_krylov_stop(1)
+    it.dt = cfg["dt"]
+    for _ in range(6):
+        it(A, m.sop, -1j)
+        orc.step(cfg["dt"])
+    assert abs(it.mel()(sb.SZ, 0, A).real - orc.expect(0, sb.SZ).real) < 1e-8
+    assert max(np.max(np.abs(a - b)) for a, b in zip(A.get(), orc.get_state())) < 1e-7
+    assert abs(it.nh_applications() - orc.nh_applications) <= 0.02 * orc.nh_applications

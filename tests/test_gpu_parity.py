@@ -281,6 +281,3 @@ def test_residual_krylov_stop_matches_oracle():
     assert abs(ia.nh_applications() - orc.nh_applications) <= 0.02 * orc.nh_applications
     assert ia.nh_applications() < 0.8 * ib.nh_applications()
     assert abs(ia.mel()(sb.SZ, 0, A).real - ib.mel()(sb.SZ, 0, B).real) < 1e-9
-    mixed = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=12, precision=api.PREC_MIXED)
-    with pytest.raises(api.TTNError):
-        mixed.set_krylov_stop(1)

@@ -83,6 +83,7 @@ SIGNATURES = {
     "ttn_integrator_reset": (_I, [_P]),
     "ttn_integrator_synchronize": (_I, [_P]),
     "ttn_integrator_prepare": (_I, [_P, _P]),
+    "ttn_integrator_set_profiling": (_I, [_P, _I]),
     "ttn_integrator_flops": (_I, [_P, _DP]),
     "ttn_integrator_timer": (_I, [_P, _I, _DP]),
     "ttn_bench_node_op": (_I, [_P, _P, _I, _I, _I, _DP, _DP]),
@@ -397,6 +398,10 @@ class fixed_step_projector_splitting_integrator:
     PROFILE_KINDS = ["expm_node", "expm_bond", "r2l_qr", "l2r_qr", "mf_update", "spf_update", "apply_to_parent",
                      "apply_from_parent"]
     PROFILE_CLASSES = ["<1K", "<64K", "<1M", ">=1M"]
+
+    def set_profiling(self, on: bool):
+        """Synchronising per-operation wall-time breakdown (``profile()``) on or off; clears it."""
+        _check(lib().ttn_integrator_set_profiling(self.h, int(bool(on))))
 
     def profile(self):
         t = np.zeros(32)

@@ -1014,7 +1014,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
         // interval once beta_0 beta_{j+1} |e_j^T exp(c tau T_{j+1}) e_1| <= tol; it ends the
         // recurrence like an exact breakdown (mb = j + 1, no error-estimate product), so
         // every CTA leaves the loop at the same step after the next grid barrier
-        if (a.krylov_stop && !a.mixed && blockIdx.x == 0 && warp == 0 && !brk && j + 1 < m)
+        if (a.krylov_stop && blockIdx.x == 0 && warp == 0 && !brk && j + 1 < m)
           residual_stop(ctl, j + 1, m, beta, cs);
         __syncthreads();
       }

@@ -444,7 +444,7 @@ struct Integrator {
   double2 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w4 = nullptr, *V = nullptr, *p = nullptr,
           *gws = nullptr, *qtau = nullptr, *scal = nullptr;
   WideQr* wide = nullptr;  // cuSOLVER QR of matricisations wider than kQrMaxCols
-  int krylov_stop = 0;     // 1: Lanczos recurrences end on the residual estimate (FP64 only)
+  int krylov_stop = 0;     // 1: Lanczos recurrences end on the residual estimate
   size_t gws_bytes = 0;
   long long maxsize = 0, ldv = 0;
   KrylovCtl* ctl = nullptr;
@@ -1975,7 +1975,6 @@ int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out) {
 int ttn_integrator_set_krylov_stop(ttn_integrator* it, int mode) {
   TTN_API_BEGIN
   TTN_REQUIRE(it && (mode == 0 || mode == 1), TTN_EINVAL, "Krylov stop rule: 0 (full space) or 1 (residual)");
-  TTN_REQUIRE(mode == 0 || !it->I.mixed, TTN_EINVAL, "the residual stop needs an FP64 integrator");
   it->I.krylov_stop = mode;
   TTN_API_END
 }
@@ -2443,6 +2442,19 @@ int ttn_bench_node_op(ttn_integrator* it, ttn_state* psi, int node, int kind, in
   if (ms_per_rep) *ms_per_rep = ms / reps;
   if (flops_per_rep) *flops_per_rep = fl;
   I.flops = f0;
+  TTN_API_END
+}
+int ttn_integrator_set_profiling(ttn_integrator* it, int on) {
+  TTN_API_BEGIN
+  TTN_REQUIRE(it, TTN_EINVAL, "null argument");
+  CK(cudaSetDevice(it->I.device));
+  CK(cudaStreamSynchronize(it->I.stream));
+  it->I.profiling = on != 0;
+  for (int k = 0; k < 8; ++k)
+    for (int c = 0; c < 4; ++c) {
+      it->I.prof_t[k][c] = 0.0;
+      it->I.prof_n[k][c] = 0;
+    }
   TTN_API_END
 }
 int ttn_integrator_profile(ttn_integrator* it, double* seconds, long long* counts) {

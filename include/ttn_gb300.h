@@ -238,27 +238,14 @@ int ttn_adjoint_grad(ttn_integrator* it, ttn_state* psi, double dt, double coeff
                      const double* weights, int mode, const double* op, int checkpoint_every, int skip_prepare,
                      double* J, double* grad_coeff, double* grad_ops, double* grad_state);
 
-/* ---- kernel-level entry points (parity checks and benchmarks) -------------------- */
-/* recompute every environment for the current node tensors, without gauge moves */
-int ttn_debug_refresh_env(ttn_integrator* it, ttn_state* psi);
-/* out = H_eff(node) v with the current environments; v, out are host buffers */
-int ttn_debug_heff(ttn_integrator* it, int node, const double* v, double* out);
+/* ---- measurement entry points (benchmarks and profiles); the kernel-level entry points
+ * that only the parity tests use are declared in ttn_gb300_testing.h ------------------ */
 /* Krylov kernel phase times accumulated since the last call (TTN_PROFILE set at creation,
  * else zeros), out[16]: out[0..7] ms in begin, matvec, alpha, re-orthogonalisation
  * coefficients, re-orthogonalisation + norm, ||H V_m||, control, combine; out[8] sub-steps,
  * out[9] launches; out[10..13] ms inside the tensor-core contractions (row exponents,
  * chunk pipeline, TMEM drain, output), out[14] tensor-core tiles (as seen by CTA 0) */
 int ttn_integrator_kernel_phases(ttn_integrator* it, double* out);
-/* out = the compiled matrix-vector program of a node (kind 0: H_eff, kind 1: bond
- * Hamiltonian on the node's R matrix) applied once by the persistent kernel, in the
- * integrator's precision */
-int ttn_debug_program_apply(ttn_integrator* it, int node, int kind, const double* v, double* out);
-/* v <- exp(coeff * tau * H_eff(node)) v; returns the number of H applications */
-int ttn_debug_expm_node(ttn_integrator* it, int node, double tau, double cre, double cim,
-                        double* v, long long* napps);
-/* environment matrix of one node group (which: 0 spf, 1 mean field) */
-int ttn_debug_num_groups(ttn_integrator* it, int node, int* out);
-int ttn_debug_get_env(ttn_integrator* it, int node, int group, int which, double* out);
 /* time `reps` repetitions of one node operation on the device (kind 0: H_eff
  * application, 1: Krylov exponential of the node over dt/2 (persistent kernel),
  * 2: leaf-to-root Householder QR, 3: Krylov exponential of the node's bond matrix);
@@ -284,11 +271,6 @@ int ttn_host_free(void* p);
 int ttn_launch_count(unsigned long long* out);
 /* FP64 FMA throughput of a device in TFLOP/s (long independent FMA chains) */
 int ttn_device_fp64_peak(int device, double* tflops);
-/* tensor-core check: D (128 x N) = A (128 x K) B^T with B stored N x K, real fp64 in and out,
- * computed with split-TF32 tcgen05 MMAs and FP32 accumulation */
-int ttn_debug_tc_gemm(const double* A, const double* B, double* D, int K, int N, int device);
-/* Householder QR of an m x n row-major matrix on the device: a <- Q, r <- R */
-int ttn_debug_qr(int m, int n, double* a, double* r, int device);
 
 /* No counterpart in the reference: it is the one entry point that allocates no device
  * memory, for callers that cannot allocate where they factorise (all their device memory

@@ -1,5 +1,6 @@
 """CPU-side checks of the C-ABI library: it loads, exports every symbol declared in
-include/ttn_gb300.h, and validates its inputs on the host (no compute calls)."""
+include/*.h (the boundary ttn_gb300.h and the test-only ttn_gb300_testing.h), and
+validates its inputs on the host (no compute calls)."""
 import ctypes as C
 import os
 import re
@@ -14,7 +15,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def declared_symbols():
-    text = open(os.path.join(ROOT, "include", "ttn_gb300.h")).read()
+    inc = os.path.join(ROOT, "include")
+    text = "".join(open(os.path.join(inc, f)).read() for f in sorted(os.listdir(inc)) if f.endswith(".h"))
     return sorted(set(re.findall(r"\b(ttn_[a-z0-9_]+)\s*\(", text)))
 
 

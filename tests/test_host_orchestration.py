@@ -27,7 +27,8 @@ def _build():
             os.path.join(ROOT, "ttns_lib_gb300", "csrc", "ttn_noalloc.cu"), os.path.join(HERE, "mock_cuda.cpp")]
     deps = srcs + [os.path.join(ROOT, "ttns_lib_gb300", "csrc", f) for f in os.listdir(os.path.join(ROOT, "ttns_lib_gb300", "csrc"))
                    if f.endswith((".cuh", ".hpp"))]
-    deps += [os.path.join(ROOT, "include", "ttn_gb300.h"), os.path.join(ROOT, "oracle", "ttn_oracle.cpp"),
+    deps += [os.path.join(ROOT, "include", "ttn_gb300.h"), os.path.join(ROOT, "include", "ttn_gb300_testing.h"),
+             os.path.join(ROOT, "oracle", "ttn_oracle.cpp"),
              os.path.join(ROOT, "oracle", "ttn_adjoint.hpp")]
     if os.path.exists(OUT) and os.path.getmtime(OUT) >= max(os.path.getmtime(d) for d in deps):
         return OUT

@@ -147,21 +147,23 @@ def test_whole_sudden_cutoff_run():
     assert worst < 1e-6, worst
 
 
-def test_whole_debye_run_with_bonds_past_64():
-    """The reference's whole printed run of beta_10/ohmic/spin_boson_debye (36 steps to
-    t = 0.18, where the reference's top bond reaches 161): the bonds grow large, towards
-    the wide QR route and the device eigensolver of the expansion.  Every row's observables
-    within 1e-4 of the reference's (both runs are converged to the spawning threshold, and
-    the two expansions choose their directions differently, so the trajectories part
-    slowly)."""
+def test_debye_run_with_growing_bonds():
+    """The first 10 printed steps of the reference's beta_10/ohmic/spin_boson_debye run (to
+    t = 0.05; the whole printed run, 36 steps to t = 0.18 with the reference's top bond
+    reaching 161, takes longer than the GPU suite can spend on one test): the bonds grow
+    past 32 through the expansion's device eigensolver.  Every row's observables within
+    1e-5 of the reference's (both runs are converged to the spawning threshold, and the
+    two expansions choose their directions differently, so the trajectories part slowly:
+    the oracle stays within 1.2e-6 over these steps).  Bonds wider than 64 are covered by
+    tests/test_zzz_wide_gpu.py."""
     g = _case("beta_10/ohmic/spin_boson_debye")
     traj = g["trajectory"]
     inp = D.parse_input(g["input"])
     r = D.SpinBosonRun(inp, device=0)
     worst = 0.0
-    for k in range(1, len(traj)):
+    for k in range(1, min(len(traj), 11)):
         r.step()
         assert abs(r.t - traj[k][0]) < 1e-12
         worst = max(worst, float(np.max(np.abs(np.array(r.observables()) - traj[k][1:5]))))
-    assert worst < 1e-4, worst
+    assert worst < 1e-5, worst
     assert r.hrank().max() > 32

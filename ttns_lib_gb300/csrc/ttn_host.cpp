@@ -11,6 +11,7 @@
 // walks the schedule and enqueues work on the integrator's stream.  The only
 // device-to-host traffic inside a step is one status word per Krylov sub-step.
 #include "../../include/ttn_gb300.h"
+#include "../../include/ttn_gb300_testing.h"
 #include "ttn_kernels.cuh"
 #include "ttn_coop.cuh"
 #include "ttn_expm.cuh"

@@ -107,10 +107,11 @@ def test_mixed_sweeps_track_fp64():
 
 def test_mixed_residual_stop_tracks_the_oracle():
     """Krylov stop rule 1 (the Lanczos recurrence ends on the residual estimate, the
-    reference's rule) in mixed precision: six sweeps of the rank-64 tree from a generic
-    state follow the oracle with the same rule to 1e-8 in <sigma_z> and 1e-7 in every node
+    reference's rule) in mixed precision: four sweeps of a 17-node tree with the headline
+    workload's node shapes (4096 x 64 nodes on the tensor cores) from a generic state
+    follow the oracle with the same rule to 1e-8 in <sigma_z> and 1e-7 in every node
     tensor, with the oracle's count of H applications to 2 %."""
-    m, cfg = rank64_tree()
+    m, cfg = sb.build_config("c3", N=4)
     topo = m.topology
     st = generic_state(topo, np.random.default_rng(15))
     orc = Oracle(topo, m.sop, krylov_dim=cfg["krylov_dim"], krylov_tol=1e-12)
@@ -122,7 +123,7 @@ def test_mixed_residual_stop_tracks_the_oracle():
                                                       precision=api.PREC_MIXED)
     it.set_krylov_stop(1)
     it.dt = cfg["dt"]
-    for _ in range(6):
+    for _ in range(4):
         it(A, m.sop, -1j)
         orc.step(cfg["dt"])
     assert abs(it.mel()(sb.SZ, 0, A).real - orc.expect(0, sb.SZ).real) < 1e-8

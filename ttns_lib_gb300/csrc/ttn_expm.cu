@@ -565,17 +565,41 @@ __device__ void reduce_partials(const double2* part, int nq, double2* out, Red& 
 // size mb, bordered when aug is set by row mb = betm at column mb-1 and row mb+1 = 1 at
 // column mb (Sidje's augmented matrix, whose rows mb and mb+1 of exp(zc Haug) e1 are
 // betm zc e_mb^T phi1(zc T) e1 and betm zc^2 e_mb^T phi2(zc T) e1, the two terms of the
-// error estimate).  Evaluated as (sum_{k<=kTaylor} (zc Haug / s)^k / k!)^s e1 with s
-// chosen so that ||zc Haug / s||_inf <= 1: truncation below 1e-17 relative, and every
-// row is one lane, so the dependent chain per term is a handful of FP64 operations
-// (FP64 latency, not throughput, bounds this phase on GB300).
+// error estimate).  Evaluated as (sum_{k<=K} (zc Haug / s)^k / k!)^s e1 with s the
+// fewest segments of norm r = ||zc Haug / s||_inf <= 4 and K the fewest terms whose
+// remainder r^(K+1) e^r / (K+1)! stays below 2^-56 (kTaylorK); every row is one lane, so
+// the dependent chain per term is a handful of FP64 operations (FP64 latency and the
+// FP64 issue rate of one warp, not throughput, bound this phase on GB300).  When zc is
+// real or imaginary (the usual case: coefficient -i and a real time step), the first
+// segment, which starts from the real e1, runs in real arithmetic: term k is u^k w_k with
+// u in {1, -1, i, -i} and the real recurrence w_k = (|zc| / (s k)) Haug w_{k-1}.
 struct CtlSmem {
   double d[EQ], e[EQ + 1];
   double2 x[EQ + 2];
   double2 t[2][EQ + 2];
+  double w[2][EQ + 2];
 };
-constexpr int kTaylor = 18;
 constexpr int kMaxScaling = 4096;   // ||zc Haug||_inf above this fails the step (error bit 4)
+constexpr int kMaxTaylor = 34;
+__constant__ unsigned char kTaylorK[32] = {10, 12, 14, 15, 16, 17, 18, 19, 19, 20, 21, 22, 23, 23, 24, 25,
+                                           25, 26, 26, 27, 28, 28, 29, 30, 30, 31, 31, 32, 32, 33, 34, 34};
+__constant__ double kInvK[kMaxTaylor + 1] = {
+    0.0,       1.0,       1.0 / 2,   1.0 / 3,   1.0 / 4,   1.0 / 5,   1.0 / 6,   1.0 / 7,   1.0 / 8,
+    1.0 / 9,   1.0 / 10,  1.0 / 11,  1.0 / 12,  1.0 / 13,  1.0 / 14,  1.0 / 15,  1.0 / 16,  1.0 / 17,
+    1.0 / 18,  1.0 / 19,  1.0 / 20,  1.0 / 21,  1.0 / 22,  1.0 / 23,  1.0 / 24,  1.0 / 25,  1.0 / 26,
+    1.0 / 27,  1.0 / 28,  1.0 / 29,  1.0 / 30,  1.0 / 31,  1.0 / 32,  1.0 / 33,  1.0 / 34};
+
+// row i of Haug applied to a real vector t
+__device__ __forceinline__ double haug_row(int i, int mb, double betm, const double* d, const double* e,
+                                           const double* t) {
+  if (i < mb) {
+    double u = d[i] * t[i];
+    if (i > 0) u = fma(e[i], t[i - 1], u);
+    if (i + 1 < mb) u = fma(e[i + 1], t[i + 1], u);
+    return u;
+  }
+  return (i == mb) ? betm * t[mb - 1] : t[mb];
+}
 
 __device__ bool warp_expm_e1(int mb, bool aug, double betm, double2 zc, CtlSmem& S) {
   const int lane = threadIdx.x & 31;
@@ -590,18 +614,53 @@ __device__ bool warp_expm_e1(int mb, bool aug, double betm, double2 zc, CtlSmem&
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) rn = fmax(rn, __shfl_xor_sync(0xffffffffu, rn, o));
-  const double nrm = rn * hypot(zc.x, zc.y);
+  const double az = hypot(zc.x, zc.y);
+  const double nrm = rn * az;
   if (!(nrm <= (double)kMaxScaling)) return false;
-  const int s = nrm > 1.0 ? (int)ceil(nrm) : 1;
+  const int s = nrm > 4.0 ? (int)ceil(nrm * 0.25) : 1;
   const double inv_s = 1.0 / (double)s;
+  int kb = (int)ceil(nrm * inv_s * 8.0) - 1;
+  kb = kb < 0 ? 0 : (kb > 31 ? 31 : kb);
+  const int K = kTaylorK[kb];
   for (int i = lane; i < mx; i += 32) S.x[i] = make_double2(i == 0 ? 1.0 : 0.0, 0.0);
   __syncwarp();
-  for (int rep = 0; rep < s; ++rep) {
+  int rep = 0;
+  const bool real_z = (zc.y == 0.0), imag_z = (zc.x == 0.0);
+  if (real_z || imag_z) {
+    // zc = |zc| u: real_z: u = sign(zc.x); imag_z: u = sign(zc.y) i
+    const double sg = real_z ? (zc.x < 0.0 ? -1.0 : 1.0) : (zc.y < 0.0 ? -1.0 : 1.0);
+    const double a = az * inv_s;
+    for (int i = lane; i < mx; i += 32) S.w[0][i] = (i == 0) ? 1.0 : 0.0;
+    __syncwarp();
+    double* xs = reinterpret_cast<double*>(S.x);
+    int cur = 0;
+    for (int k = 1; k <= K; ++k) {
+      const double ck = a * kInvK[k];
+      // u^k: real_z: sg^k (real part); imag_z: sg^k i^k
+      const bool odd = (k & 1) != 0;
+      double sk = odd ? sg : 1.0;
+      int comp = 0;
+      if (imag_z) {
+        comp = odd ? 1 : 0;
+        if ((k & 3) >= 2) sk = -sk;
+      }
+      const double* tc = S.w[cur];
+      for (int i = lane; i < mx; i += 32) {
+        const double v = ck * haug_row(i, mb, betm, S.d, S.e, tc);
+        S.w[cur ^ 1][i] = v;
+        xs[2 * i + comp] = fma(sk, v, xs[2 * i + comp]);
+      }
+      __syncwarp();
+      cur ^= 1;
+    }
+    rep = 1;
+  }
+  for (; rep < s; ++rep) {
     for (int i = lane; i < mx; i += 32) S.t[0][i] = S.x[i];
     __syncwarp();
     int cur = 0;
-    for (int k = 1; k <= kTaylor; ++k) {
-      const double2 ck = cscale(inv_s / (double)k, zc);
+    for (int k = 1; k <= K; ++k) {
+      const double2 ck = cscale(inv_s * kInvK[k], zc);
       const double2* tc = S.t[cur];
       for (int i = lane; i < mx; i += 32) {
         double2 u;
@@ -871,6 +930,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
     if (pc.acc) pc.acc[8] += 1;
     pc.mark(0);
     // ---- Lanczos with full re-orthogonalisation
+    double anorm_rows = 0.0;  // breakdown scale: largest row sum of the tridiagonal so far
     for (int j = 0; j < m; ++j) {
       const double2* Vj = a.V + (long long)j * a.ldv;
       grid_barrier(a.bar, a.err);
@@ -984,12 +1044,11 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
       reduce_partials(pa, 1, red, sm);
       {
         const double beta = sqrt(red[0].x);
-        double anorm = 0.0;
-        for (int q = 0; q <= j; ++q) {
-          double nb = (q < j) ? ctl->bet[q + 1] : beta;
-          double v = fabs(ctl->alpha[q]) + ctl->bet[q] + nb;
-          anorm = v > anorm ? v : anorm;
-        }
+        // max over the rows q <= j of |alpha_q| + beta_q + beta_{q+1}: the rows below j were
+        // complete at the previous step, row j completes with this beta
+        const double vrow = fabs(alpha) + bj + beta;
+        const double anorm = vrow > anorm_rows ? vrow : anorm_rows;
+        anorm_rows = anorm;
         const int brk = (beta <= 1e-14 * (1.0 + anorm)) ? 1 : 0;
         const double inv = brk ? 0.0 : 1.0 / beta;
         double2* Vn = a.V + (long long)(j + 1) * a.ldv;

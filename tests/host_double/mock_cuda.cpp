@@ -106,6 +106,20 @@ void zgemm(const ZGemm& g, double2* ws, size_t ws_bytes, cudaStream_t s) {
   ++g_launches;
 }
 int coop_qr_grid(long long m, int n) { (void)m; (void)n; return 1; }
+size_t qr_rows_scratch_bytes(int g) { (void)g; return 1024; }
+int qr_rows_max_grid() { return 1; }
+// the shared-memory QR: the oracle's Householder QR (one CTA holds at most kQrRowsMax rows)
+cudaError_t householder_qr_rows(double2* M, long long m, int n, double2* R, int Rt, double2* tau, double* scratch,
+                                GridBarrier* bar, int* err, int grid, cudaStream_t s) {
+  if (grid < 1 || (m + grid - 1) / grid > kQrRowsMax) return cudaErrorInvalidValue;
+  (void)tau; (void)scratch; (void)bar; (void)err; (void)s;
+  std::vector<cd> Rr((size_t)n * n), t;
+  orc::householder_qr(reinterpret_cast<cd*>(M), (size_t)m, n, Rr.data(), t);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) R[(size_t)i * n + j] = D(Rt ? Rr[(size_t)j * n + i] : Rr[(size_t)i * n + j]);
+  ++g_launches;
+  return cudaSuccess;
+}
 size_t coop_qr_scratch_bytes(int g) { return (size_t)(4 * g + 4 + 4 * (size_t)g * kQrMaxCols) * sizeof(double); }
 cudaError_t coop_qr_max_grid(int* out) { *out = 1; return cudaSuccess; }
 // the column-by-column cooperative QR of ttn_qr_noalloc: the oracle's Householder QR,

@@ -454,7 +454,7 @@ struct Integrator {
   DevBuf coop_buf;
   GridBarrier* bar = nullptr;
   double* qr_scratch = nullptr;
-  int num_sms = 0, qr_max_grid = 1, expm_max_grid = 1, expm_max_grid_tc = 1;
+  int num_sms = 0, qr_max_grid = 1, qr_rows_grid = 1, expm_max_grid = 1, expm_max_grid_tc = 1;
   bool mixed = false;                      // tensor-core contractions in the matvec programs
   std::vector<char> heff_tc, kbond_tc;     // program contains tensor-core contractions
   std::vector<char> heff_tail, kbond_tail; // program needs a barrier after it
@@ -727,7 +727,10 @@ struct Integrator {
     {
       CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
       qr_max_grid = std::max(1, std::min(qr_blocked_max_grid(), num_sms));
-      size_t qb = align256(sizeof(GridBarrier)) + align256(qr_blocked_scratch_bytes(qr_max_grid));
+      qr_rows_grid = std::max(1, std::min(qr_rows_max_grid(), num_sms));
+      if (const char* e = std::getenv("TTN_QR_ROWS_TARGET")) qr_rows_target = std::max(1, std::atoi(e));
+      size_t qb = align256(sizeof(GridBarrier)) +
+                  align256(std::max(qr_blocked_scratch_bytes(qr_max_grid), qr_rows_scratch_bytes(qr_rows_grid)));
       coop_buf.alloc(qb);
       CK(cudaMemsetAsync(coop_buf.p, 0, coop_buf.bytes, stream));
       bar = coop_buf.as<GridBarrier>();
@@ -1271,12 +1274,23 @@ struct Integrator {
 
   // ---------------------------------------------------------------- gauge moves
   // Householder QR on as many CTAs as the height allows (one row block per CTA)
-  int qr_rows_per_cta = 32;  // rows of the matrix per CTA of the cooperative QR
+  int qr_rows_per_cta = 32;  // rows of the matrix per CTA of the panel-blocked QR (tall matrices)
+  int qr_rows_target = 8;    // rows per CTA of the shared-memory QR
   void qr(double2* M, long long m, int n, double2* R, int Rt) {
     if (n > kQrMaxCols) {
       TTN_REQUIRE(wide, TTN_EINVAL, "no workspace for a QR wider than 64 columns");
       CK(householder_qr_wide(wide, M, m, n, R, Rt, stream));
       return;
+    }
+    // rows resident in shared memory: about qr_rows_target rows per CTA (one CTA up to 64
+    // rows), as long as the grid holds every row
+    {
+      long long g = m <= kQrRowsMax ? 1 : (m + qr_rows_target - 1) / qr_rows_target;
+      if (g > qr_rows_grid) g = qr_rows_grid;
+      if ((m + g - 1) / g <= kQrRowsMax) {
+        CK(householder_qr_rows(M, m, n, R, Rt, qtau, qr_scratch, bar, status, (int)g, stream));
+        return;
+      }
     }
     int g = (int)std::max(1LL, std::min<long long>(m / qr_rows_per_cta, qr_max_grid));
     CK(householder_qr_blocked(M, m, n, R, Rt, qtau, qr_scratch, bar, status, g, stream));
@@ -2648,14 +2662,21 @@ int ttn_debug_qr(int m, int n, double* a, double* r, int device) {
   CK(cudaMemcpy(dA, a, (size_t)m * n * sizeof(double2), cudaMemcpyHostToDevice));
   int sms = 0;
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-  int g = std::min(ttn::coop_qr_grid(m, sms), std::max(1, std::min(ttn::qr_blocked_max_grid(), sms)));
+  // the sweep's choice: the shared-memory kernel (8 rows per CTA, one CTA up to 64 rows)
+  // when the grid holds every row, else the panel-blocked kernel
+  long long gr = m <= ttn::kQrRowsMax ? 1 : (m + 7) / 8;
+  gr = std::min<long long>(gr, std::max(1, std::min(ttn::qr_rows_max_grid(), sms)));
+  const bool rows = (m + gr - 1) / gr <= ttn::kQrRowsMax;
+  int g = rows ? (int)gr : std::min(ttn::coop_qr_grid(m, sms), std::max(1, std::min(ttn::qr_blocked_max_grid(), sms)));
+  const size_t sb = rows ? ttn::qr_rows_scratch_bytes(g) : ttn::qr_blocked_scratch_bytes(g);
   ttn::DevBuf cb;
-  cb.alloc(ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(ttn::qr_blocked_scratch_bytes(g)) + 256);
+  cb.alloc(ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(sb) + 256);
   CK(cudaMemset(cb.p, 0, cb.bytes));
   auto* bar = cb.as<ttn::GridBarrier>();
   double* scr = (double*)(cb.as<char>() + ttn::align256(sizeof(ttn::GridBarrier)));
-  int* err = (int*)(cb.as<char>() + ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(ttn::qr_blocked_scratch_bytes(g)));
-  CK(ttn::householder_qr_blocked(dA, m, n, dR, 0, dt, scr, bar, err, g, 0));
+  int* err = (int*)(cb.as<char>() + ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(sb));
+  if (rows) CK(ttn::householder_qr_rows(dA, m, n, dR, 0, dt, scr, bar, err, g, 0));
+  else CK(ttn::householder_qr_blocked(dA, m, n, dR, 0, dt, scr, bar, err, g, 0));
   CK(cudaDeviceSynchronize());
   CK(cudaGetLastError());
   int herr = 0;

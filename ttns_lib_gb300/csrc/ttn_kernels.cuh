@@ -82,6 +82,15 @@ size_t qr_blocked_scratch_bytes(int max_grid);
 int qr_blocked_max_grid();
 cudaError_t householder_qr_blocked(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws,
                                    double* scratch, GridBarrier* bar, int* err, int grid, cudaStream_t s);
+// Householder QR with every CTA's rows held in shared memory (ttn_qr_rows.cu), same
+// conventions and arguments as householder_qr_blocked; at most kQrRowsMax rows per CTA
+// (ceil(m / grid) <= kQrRowsMax, else cudaErrorInvalidValue); scratch of
+// qr_rows_scratch_bytes(grid) bytes.
+constexpr int kQrRowsMax = 64;
+size_t qr_rows_scratch_bytes(int max_grid);
+int qr_rows_max_grid();
+cudaError_t householder_qr_rows(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, double* scratch,
+                                GridBarrier* bar, int* err, int grid, cudaStream_t s);
 // QR of matrices with kQrMaxCols < n <= kMaxBond (cuSOLVER zgeqrf / zungqr on a
 // column-major copy; same conventions and arguments as householder_qr_coop).  The
 // workspace is sized at creation for the (m, n) shapes listed; a later call with a

@@ -162,16 +162,19 @@ struct PhaseClock {
 
 // ---- tensor-core contractions (mixed precision) at FP64 accuracy
 //
-// Both kinds are D(128 x 64) = A B^T per tile, A the real block form of alpha * mat
-// (64 x 64, row = output index, column = input index) and B 64 input columns n:
+// Both kinds are D(128 x N) = A B^T per tile (N = kTcTileN = 32), A the real block form
+// of alpha * mat (64 x 64, row = output index, column = input index) and B N input
+// columns n:
 //   MODE tile (aa, b0): in(aa, j, b0 + n);   MF tile x0: in(x0 + n, j)   (j < 64)
+// (32 columns per tile, not 64: a 4096 x 64 node's contractions then have 128 tiles for the
+// 152 SMs instead of 64, and the per-tile B slicing, TMEM drain and output halve)
 // with K = 128 ordered k = 2 j + c (c = 0 real, 1 imaginary part of input j):
 //   A[(0,i)][(j,0)] = Re S, A[(0,i)][(j,1)] = -Im S, A[(1,i)][(j,0)] = Im S, A[(1,i)][(j,1)] = Re S.
 // Exact integer slices (the Ozaki splitting): every row of A and of B is scaled by a power
 // of two 2^E (E the smallest with all |x| < 2^E) and cut into six 7-bit integer slices,
 // x = 2^E sum_t s_t 2^(-7t) + O(2^(E-42)), each slice exact in TF32.  The products s_t s_u
 // (< 2^14) summed over K = 128 and over the at most 7 pairs of one level L = t + u stay
-// below 2^24, so each level is accumulated EXACTLY in FP32 TMEM (levels 2..8, 7 x 64
+// below 2^24, so each level is accumulated EXACTLY in FP32 TMEM (levels 2..8, 7 x N
 // columns); the epilogue combines the levels in integers and scales by 2^(E_i + E_n - 56).
 // Error: the 42-bit truncation of the operands and the dropped levels >= 9, about 1e-13
 // relative to sum_k |A||B| (FP64 contractions: about 1e-16).  Operands arrive in 4 chunks
@@ -184,7 +187,7 @@ struct TcState {
   uint64_t* mbar;         // [2] MMA completion, one per operand buffer
   uint64_t* lbar;         // [2] bulk-load completion
   unsigned char* a[2];    // A chunk buffers: 6 slices x 128 x 32 bf16; both together the epilogue stage
-  unsigned char* b[2];    // B chunk buffers: 6 slices x 64 x 32 bf16
+  unsigned char* b[2];    // B chunk buffers: 6 slices x N x 32 bf16
   int* e_n;               // row exponents of the B tile
 };
 constexpr int TC_SLICES = 6;
@@ -192,16 +195,18 @@ constexpr int TC_LEVELS = 7;                              // t + u = 2 .. 8
 constexpr int TC_CHUNK_K = 32;
 constexpr int TC_CHUNKS = 4;
 constexpr int TC_A_SLICE_BYTES = 128 * TC_CHUNK_K * 2;    // 8 KB
-constexpr int TC_B_SLICE_BYTES = 64 * TC_CHUNK_K * 2;     // 4 KB
+constexpr int TC_N = kTcTileN;                            // columns per tile
+constexpr int TC_B_SLICE_BYTES = TC_N * TC_CHUNK_K * 2;   // 2 KB
 constexpr int TC_A_CHUNK_BYTES = TC_SLICES * TC_A_SLICE_BYTES;
 constexpr int TC_B_CHUNK_BYTES = TC_SLICES * TC_B_SLICE_BYTES;
 constexpr int TC_IMG_HDR = 1024;                          // int E_i[64], padded
 constexpr int TC_STAGE_LD = 65;                           // doubles per staged row
 constexpr size_t TC_SMEM = (size_t)2 * (TC_A_CHUNK_BYTES + TC_B_CHUNK_BYTES) + 256;
-constexpr uint32_t TC_TMEM_COLS = 512;
+constexpr uint32_t TC_TMEM_COLS = 256;
 static_assert(kTcImageBytes == (size_t)TC_IMG_HDR + (size_t)TC_CHUNKS * TC_A_CHUNK_BYTES, "image size");
 static_assert(128 * TC_STAGE_LD * 8 <= 2 * TC_A_CHUNK_BYTES, "epilogue stage must fit in the A buffers");
-static_assert(TC_LEVELS * 64 <= (int)TC_TMEM_COLS, "TMEM columns");
+static_assert(TC_LEVELS * TC_N <= (int)TC_TMEM_COLS, "TMEM columns");
+static_assert(TC_N % 16 == 0 && TC_N >= 16 && TC_N <= 64, "MMA N for M = 128");
 
 // smallest E with |x| < 2^E from the bits of |x| (x != 0)
 __device__ __forceinline__ int exp_bound_bits(unsigned long long absbits) {
@@ -312,13 +317,14 @@ __device__ void build_tc_images(const ExpmArgs& a) {
   tc::fence_proxy_async_all();
 }
 
-// row exponents of the B tile: 4 threads per row n, 16 inputs each
+// row exponents of the B tile: 256 / N threads per row n, 64 N / 256 inputs each
 __device__ __forceinline__ void tc_b_exponents(const TcState& t, const double2* base, long long sn, long long sj) {
-  const int n = threadIdx.x >> 2, part = threadIdx.x & 3;
+  constexpr int TPR = 256 / TC_N, JPT = 64 / TPR;
+  const int n = threadIdx.x / TPR, part = threadIdx.x % TPR;
   unsigned long long mx = 0;
-  if (n < 64) {
+  if (n < TC_N) {
 #pragma unroll
-    for (int j = 16 * part; j < 16 * part + 16; ++j) {
+    for (int j = JPT * part; j < JPT * part + JPT; ++j) {
       const double2 v = base[(long long)n * sn + (long long)j * sj];
       const unsigned long long ar = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
       const unsigned long long ai = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
@@ -327,31 +333,32 @@ __device__ __forceinline__ void tc_b_exponents(const TcState& t, const double2* 
     }
   }
 #pragma unroll
-  for (int o = 1; o < 4; o <<= 1) {
+  for (int o = 1; o < TPR; o <<= 1) {
     const unsigned long long u = __shfl_xor_sync(0xffffffffu, mx, o);
     mx = u > mx ? u : mx;
   }
-  if (n < 64 && part == 0) t.e_n[n] = mx ? exp_bound_bits(mx) : 0;
+  if (n < TC_N && part == 0) t.e_n[n] = mx ? exp_bound_bits(mx) : 0;
   __syncthreads();
 }
 
 // slices of chunk q of the B tile (inputs j = 16 q .. 16 q + 15) into buffer bi
-// (tensor-core programs run with 256 threads: four rounds of 256 (n, jj) tasks; the lanes
-// of a warp cover one 8-row x 4-word block of core matrices, 128 contiguous bytes per
+// (tensor-core programs run with 256 threads: N / 16 rounds of 256 (n, jj) tasks; the
+// lanes of a warp cover one 8-row x 4-word block of core matrices, 128 contiguous bytes per
 // slice store, so the stores are free of bank conflicts)
 __device__ __forceinline__ void tc_stage_b(const TcState& t, int bi, const double2* base, long long sn, long long sj,
                                            int q) {
+  constexpr int NBLK = TC_N / 8;  // 8-row blocks of the tile
 #pragma unroll
-  for (int r = 0; r < 4; ++r) {
+  for (int r = 0; r < TC_N / 16; ++r) {
     const int task = threadIdx.x + 256 * r;
     const int blk = task >> 5, ln = task & 31;
-    const int n = (blk & 7) * 8 + (ln >> 2), jj = (blk >> 3) * 4 + (ln & 3);
+    const int n = (blk % NBLK) * 8 + (ln >> 2), jj = (blk / NBLK) * 4 + (ln & 3);
     const double2 v = base[(long long)n * sn + (long long)(16 * q + jj) * sj];
     const int Er = t.e_n[n];
     uint32_t wr[TC_SLICES], wi[TC_SLICES];
     slice6(v.x, Er, wr);
     slice6(v.y, Er, wi);
-    const uint32_t o = tc::b16_offset(n, 2 * jj, 64);
+    const uint32_t o = tc::b16_offset(n, 2 * jj, TC_N);
 #pragma unroll
     for (int s = 0; s < TC_SLICES; ++s)
       *reinterpret_cast<uint32_t*>(t.b[bi] + s * TC_B_SLICE_BYTES + o) = wr[s] | (wi[s] << 16);
@@ -362,9 +369,9 @@ __device__ __forceinline__ void tc_stage_b(const TcState& t, int bi, const doubl
 // to mbar[bi]; one thread.  A descriptor's start address is its low 14 bits in 16-byte
 // units, so every operand slice's descriptor is the buffer's plus a constant.
 __device__ __forceinline__ void tc_issue_chunk(const TcState& t, int q, int bi) {
-  const uint32_t idesc = tc::idesc_bf16(128, 64);
+  const uint32_t idesc = tc::idesc_bf16(128, TC_N);
   const uint64_t ad0 = tc::smem_desc(tc::smem_u32(t.a[bi]), 16 * 128, 128);
-  const uint64_t bd0 = tc::smem_desc(tc::smem_u32(t.b[bi]), 8 * 128, 128);
+  const uint64_t bd0 = tc::smem_desc(tc::smem_u32(t.b[bi]), (TC_N / 8) * 128, 128);
 #pragma unroll
   for (int kk = 0; kk < TC_CHUNK_K / 16; ++kk) {
 #pragma unroll
@@ -374,10 +381,10 @@ __device__ __forceinline__ void tc_issue_chunk(const TcState& t, int q, int bi) 
         const int L = s + u;  // level - 2
         if (L >= TC_LEVELS) continue;
         const uint64_t ad = ad0 + (uint64_t)((s * TC_A_SLICE_BYTES + kk * 2 * 16 * 128) >> 4);
-        const uint64_t bd = bd0 + (uint64_t)((u * TC_B_SLICE_BYTES + kk * 2 * 8 * 128) >> 4);
+        const uint64_t bd = bd0 + (uint64_t)((u * TC_B_SLICE_BYTES + kk * 2 * (TC_N / 8) * 128) >> 4);
         // the first product into a level starts it: chunk 0, k-step 0, smallest s of the level
         const bool first = (q == 0 && kk == 0 && (s == (L < TC_SLICES ? 0 : L - TC_SLICES + 1)));
-        tc::mma_bf16(t.tmem + 64u * (uint32_t)L, ad, bd, idesc, first ? 0u : 1u);
+        tc::mma_bf16(t.tmem + (uint32_t)TC_N * (uint32_t)L, ad, bd, idesc, first ? 0u : 1u);
       }
   }
   tc::mma_commit(&t.mbar[bi]);
@@ -390,17 +397,17 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t& ph) {
 }
 
 // TMEM -> stage (double [128][TC_STAGE_LD] over the A buffers): warp w drains TMEM lanes
-// 32 (w % 4) .. + 31 (one row each), columns 32 (w / 4) .. + 31; exact integer combination
-// of the 7 levels, scaled by 2^(E_i + E_n - 56)
+// 32 (w % 4) .. + 31 (one row each), columns (N / 2) (w / 4) .. + N / 2 - 1; exact integer
+// combination of the 7 levels, scaled by 2^(E_i + E_n - 56)
 __device__ __forceinline__ void tc_drain_to_stage(const TcState& t, int Ei, PhaseClock& pc) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int row_i = 32 * (warp & 3) + lane;
   double* row = reinterpret_cast<double*>(t.a[0]) + row_i * TC_STAGE_LD;
   const uint32_t lane_base = t.tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-  for (int c0 = 32 * (warp >> 2); c0 < 32 * (warp >> 2) + 32; c0 += 8) {
+  for (int c0 = (TC_N / 2) * (warp >> 2); c0 < (TC_N / 2) * (warp >> 2) + TC_N / 2; c0 += 8) {
     float f[TC_LEVELS][8];
 #pragma unroll
-    for (int L = 0; L < TC_LEVELS; ++L) tc::tmem_ld8_nowait(lane_base + 64u * L + (uint32_t)c0, f[L]);
+    for (int L = 0; L < TC_LEVELS; ++L) tc::tmem_ld8_nowait(lane_base + (uint32_t)TC_N * L + (uint32_t)c0, f[L]);
     tc::tmem_wait_ld();
     pc.mark(15);
 #pragma unroll
@@ -425,7 +432,7 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
   const bool acc = (op.beta != 0);
   const bool mode = (op.kind == MV_MODE);
   const long long nb = op.nb;
-  const long long tiles = mode ? op.na * (nb / 64) : op.na / 64;
+  const long long tiles = mode ? op.na * (nb / TC_N) : op.na / TC_N;
   if ((long long)blockIdx.x >= tiles) return;
   const unsigned char* img = reinterpret_cast<const unsigned char*>(a.tc_img) + (size_t)op.img * kTcImageBytes;
   const int Ei = reinterpret_cast<const int*>(img)[(32 * ((threadIdx.x >> 5) & 3) + (threadIdx.x & 31)) & 63];
@@ -437,13 +444,13 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
     long long aa = 0, b0 = 0, sn, sj;
     const double2* base;
     if (mode) {
-      aa = tile / (nb / 64);
-      b0 = (tile % (nb / 64)) * 64;
+      aa = tile / (nb / TC_N);
+      b0 = (tile % (nb / TC_N)) * TC_N;
       base = in + aa * 64 * nb + b0;
       sn = 1;
       sj = nb;
     } else {
-      b0 = tile * 64;
+      b0 = tile * TC_N;
       base = in + b0 * 64;
       sn = 64;
       sj = 1;
@@ -488,9 +495,9 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
     pc.mark(11);
     tc_drain_to_stage(t, Ei, pc);
     pc.mark(12);
-    // stage -> out: element (i, n) = (stage[i][n], stage[64 + i][n]); 16 elements per
-    // thread in batches of 4 so that the loads of the accumulated outputs overlap
-    for (int r0 = 0; r0 < 16; r0 += 4) {
+    // stage -> out: element (i, n) = (stage[i][n], stage[64 + i][n]); 64 N / 256 elements
+    // per thread in batches of 4 so that the loads of the accumulated outputs overlap
+    for (int r0 = 0; r0 < 64 * TC_N / 256; r0 += 4) {
       double2* dst[4];
       double2 v[4];
 #pragma unroll
@@ -498,8 +505,8 @@ __device__ void run_op_tc(const ExpmArgs& a, const MvOp& op, const double2* x, T
         const int task = threadIdx.x + 256 * (r0 + u);
         int i, n;
         if (mode) {
-          n = task & 63;
-          i = task >> 6;
+          n = task % TC_N;
+          i = task / TC_N;
           dst[u] = out + aa * 64 * nb + (long long)i * nb + b0 + n;
         } else {
           i = task & 63;

@@ -76,10 +76,12 @@ cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s, int threads =
 // whether a contraction can run on the tensor cores
 // Tensor-core contractions need rank-64 operands and enough 64-column tiles to occupy the
 // device; smaller ones run faster as element-wise FP64 contractions.
-constexpr long long kTcMinTiles = 32;
+// A tile is the 64 outputs of the operator times kTcTileN columns of the input.
+constexpr int kTcTileN = 32;
+constexpr long long kTcMinTiles = 64;
 inline bool tc_eligible(int kind, int d, long long na, long long nb) {
-  if (kind == MV_MODE) return d == 64 && nb % 64 == 0 && na * (nb / 64) >= kTcMinTiles;
-  if (kind == MV_MF) return d == 64 && na % 64 == 0 && na / 64 >= kTcMinTiles;
+  if (kind == MV_MODE) return d == 64 && nb % kTcTileN == 0 && na * (nb / kTcTileN) >= kTcMinTiles;
+  if (kind == MV_MF) return d == 64 && na % kTcTileN == 0 && na / kTcTileN >= kTcMinTiles;
   return false;
 }
 

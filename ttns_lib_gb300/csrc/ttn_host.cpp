@@ -785,7 +785,7 @@ struct Integrator {
     a.m = cfg.krylov_dim; a.tau = 0.0; a.cf_re = 0.0; a.cf_im = -1.0; a.tol = cfg.krylov_tol;
     a.mixed = 1; a.apply_only = 1; a.phase = nullptr;
     a.tc_img = tc_img_buf.as<uint32_t>();
-    const long long tiles = kind == MV_MODE ? na * (nb / 64) : na / 64;
+    const long long tiles = kind == MV_MODE ? na * (nb / kTcTileN) : na / kTcTileN;
     const int grid = (int)std::max(1LL, std::min<long long>(tiles, expm_max_grid_tc));
     CK(expm_coop(a, grid, stream));
     return true;

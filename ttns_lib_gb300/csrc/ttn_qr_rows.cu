@@ -134,6 +134,7 @@ struct RSmem {
   double2 P[QNB][QNB + QBN];    // reduced panel block (Gram | projections)
   double2 W[QNB][QNB + QBN];    // T^H P (factorisation) or T P (Q formation)
   double2 g[QNB];               // Gram sums of column j with the panel columns, relative to 2^E
+  double2 rowj[QNB];            // M[j][j .. jend), read next to the partials
   double2 w[QNB];               // conj(tau) conj(v)^T M[:, c] for the panel columns c
   double nrm2;                  // squared norm below the diagonal, relative to 2^(2E)
   int E;
@@ -220,6 +221,12 @@ __device__ void col_reduce(const RqrArgs& a, int j, int jend, RSmem& S) {
   const int G = gridDim.x, par = j & 1;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nc = jend - j - 1;
+  // row j of the panel (alpha and the entries the w_c need), loaded by the last warp while
+  // the others load the partials
+  if (w == QW - 1 && lane <= nc) {
+    const double* rj = a.scr + rq_off_rowj(G) + (size_t)par * 2 * QNB;
+    S.rowj[lane] = make_double2(rj[2 * lane], rj[2 * lane + 1]);
+  }
   if (w > nc) return;
   const double* cp = a.scr + (size_t)par * G * rq_colw();
   int emax = kNoScale;
@@ -366,11 +373,10 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
       col_reduce(a, j, jend, S);
       __syncthreads();
       if (threadIdx.x == 0) {
-        const double* rj = a.scr + rq_off_rowj(G) + (size_t)(j & 1) * 2 * QNB;
         const int E = S.E;
         double xnorm = sqrt(S.nrm2);
         if (E) xnorm = qldexp(xnorm, E);
-        double ar = rj[0], ai = rj[1];
+        double ar = S.rowj[0].x, ai = S.rowj[0].y;
         int knt = 0;
         S.active = 0;
         if (xnorm == 0.0 && ai == 0.0) {
@@ -416,14 +422,13 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
       }
       __syncthreads();
       if (threadIdx.x >= 1 && threadIdx.x <= nc) {
-        const double* rj = a.scr + rq_off_rowj(G) + (size_t)(j & 1) * 2 * QNB;
         // w_c = M[j][c] + conj(scal) 2^kfac g_c, times conj(tau)
         double2 t = qmulc(S.scal, S.g[threadIdx.x]);
         if (S.kfac) {
           t.x = qldexp(t.x, S.kfac);
           t.y = qldexp(t.y, S.kfac);
         }
-        const double2 wc = qadd(make_double2(rj[2 * threadIdx.x], rj[2 * threadIdx.x + 1]), t);
+        const double2 wc = qadd(S.rowj[threadIdx.x], t);
         S.w[threadIdx.x] = qmulc(S.tau[j], wc);
       }
       __syncthreads();

@@ -29,6 +29,11 @@ int ttn_debug_get_env(ttn_integrator* it, int node, int group, int which, double
 int ttn_debug_tc_gemm(const double* A, const double* B, double* D, int K, int N, int device);
 /* Householder QR of an m x n row-major matrix on the device: a <- Q, r <- R */
 int ttn_debug_qr(int m, int n, double* a, double* r, int device);
+/* the same QR with the shared-memory kernel's phase clock: phases[16] microseconds as seen
+ * by thread 0 of CTA 0 (0 column barriers, 1 column sums, 2 reflectors, 3 projections,
+ * 4 row updates, 5 next partials, 6 panel updates, 7 R and Q formation; phases[8] columns);
+ * zeros when the panel-blocked kernel ran */
+int ttn_debug_qr_phases(int m, int n, double* a, double* r, int device, double* phases);
 
 #ifdef __cplusplus
 }

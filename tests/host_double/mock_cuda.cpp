@@ -110,7 +110,8 @@ size_t qr_rows_scratch_bytes(int g) { (void)g; return 1024; }
 int qr_rows_max_grid() { return 1; }
 // the shared-memory QR: the oracle's Householder QR (one CTA holds at most kQrRowsMax rows)
 cudaError_t householder_qr_rows(double2* M, long long m, int n, double2* R, int Rt, double2* tau, double* scratch,
-                                GridBarrier* bar, int* err, int grid, cudaStream_t s) {
+                                GridBarrier* bar, int* err, int grid, cudaStream_t s, unsigned long long* phase) {
+  (void)phase;
   if (grid < 1 || (m + grid - 1) / grid > kQrRowsMax) return cudaErrorInvalidValue;
   (void)tau; (void)scratch; (void)bar; (void)err; (void)s;
   std::vector<cd> Rr((size_t)n * n), t;

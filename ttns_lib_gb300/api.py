@@ -103,6 +103,7 @@ SIGNATURES = {
     "ttn_debug_num_groups": (_I, [_P, _I, _IP]),
     "ttn_debug_get_env": (_I, [_P, _I, _I, _I, _DP]),
     "ttn_debug_qr": (_I, [_I, _I, _DP, _DP, _I]),
+    "ttn_debug_qr_phases": (_I, [_I, _I, _DP, _DP, _I, _DP]),
     "ttn_qr_noalloc": (_I, [_I, _I, _P, _P, _P, _I]),
     "ttn_bond_singular_values": (_I, [_P, _P, _I, _DP, C.POINTER(C.c_int)]),
     "ttn_integrator_set_expansion": (_I, [_P, _P, _IP, _D, _D, _I, _I, _I, C.c_uint]),
@@ -645,6 +646,19 @@ def device_qr(a: np.ndarray, device: int = 0):
     r = np.zeros((n, n), dtype=np.complex128)
     _check(lib().ttn_debug_qr(m, n, _dp(a.view(np.float64)), _dp(r.view(np.float64)), device))
     return a, r
+
+
+def device_qr_phases(a: np.ndarray, device: int = 0):
+    """device_qr with the shared-memory QR kernel's phase clock (microseconds per phase)."""
+    a = _cplx(a).copy()
+    m, n = a.shape
+    r = np.zeros((n, n), dtype=np.complex128)
+    ph = np.zeros(16)
+    _check(lib().ttn_debug_qr_phases(m, n, _dp(a.view(np.float64)), _dp(r.view(np.float64)), device, _dp(ph)))
+    names = ["barrier", "col_sums", "reflector", "w", "update", "partials", "panels", "r_and_q"]
+    out = {k: float(ph[i]) for i, k in enumerate(names)}
+    out["columns"] = int(ph[8])
+    return a, r, out
 
 
 def batch_step(integrators, states, coeff: complex = -1j, threads: int = 0):

@@ -57,8 +57,9 @@ __device__ double2* buf_of(const ExpmArgs& a, int id, const double2* x) {
   }
 }
 
-// one contraction of the matvec program over all output elements (grid-stride)
-__device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
+// one contraction of the matvec program over all output elements (grid-stride), one
+// thread per output element (the element-wise form; a.tpo == 1)
+__device__ void run_op_1(const ExpmArgs& a, const MvOp& op, const double2* x) {
   const double2* in = buf_of(a, op.in, x);
   double2* out = buf_of(a, op.out, x);
   const long long nthreads = (long long)gridDim.x * blockDim.x;
@@ -73,14 +74,25 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
       const long long b = rem % nb;
       const double2* S = op.mat + (long long)i * d;
       const double2* v = in + aa * d * nb + b;
-      // four independent chains: FP64 latency, not throughput, bounds small contractions
+      // four independent chains: FP64 latency, not throughput, bounds small contractions;
+      // the operands of eight steps are loaded before they are used
       double2 s0 = make_double2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
       int j = 0;
-      for (; j + 4 <= d; j += 4) {
-        s0 = cfma(S[j], v[(long long)j * nb], s0);
-        s1 = cfma(S[j + 1], v[(long long)(j + 1) * nb], s1);
-        s2 = cfma(S[j + 2], v[(long long)(j + 2) * nb], s2);
-        s3 = cfma(S[j + 3], v[(long long)(j + 3) * nb], s3);
+      for (; j + 8 <= d; j += 8) {
+        double2 sa[8], va[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          sa[u] = S[j + u];
+          va[u] = v[(long long)(j + u) * nb];
+        }
+        s0 = cfma(sa[0], va[0], s0);
+        s1 = cfma(sa[1], va[1], s1);
+        s2 = cfma(sa[2], va[2], s2);
+        s3 = cfma(sa[3], va[3], s3);
+        s0 = cfma(sa[4], va[4], s0);
+        s1 = cfma(sa[5], va[5], s1);
+        s2 = cfma(sa[6], va[6], s2);
+        s3 = cfma(sa[7], va[7], s3);
       }
       for (; j < d; ++j) s0 = cfma(S[j], v[(long long)j * nb], s0);
       const double2 s = cadd(cadd(s0, s1), cadd(s2, s3));
@@ -98,11 +110,21 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
       const double2* M = op.mat + (long long)k * r;
       double2 s0 = make_double2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
       int l = 0;
-      for (; l + 4 <= r; l += 4) {
-        s0 = cfma(v[l], M[l], s0);
-        s1 = cfma(v[l + 1], M[l + 1], s1);
-        s2 = cfma(v[l + 2], M[l + 2], s2);
-        s3 = cfma(v[l + 3], M[l + 3], s3);
+      for (; l + 8 <= r; l += 8) {
+        double2 va[8], ma[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          va[u] = v[l + u];
+          ma[u] = M[l + u];
+        }
+        s0 = cfma(va[0], ma[0], s0);
+        s1 = cfma(va[1], ma[1], s1);
+        s2 = cfma(va[2], ma[2], s2);
+        s3 = cfma(va[3], ma[3], s3);
+        s0 = cfma(va[4], ma[4], s0);
+        s1 = cfma(va[5], ma[5], s1);
+        s2 = cfma(va[6], ma[6], s2);
+        s3 = cfma(va[7], ma[7], s3);
       }
       for (; l < r; ++l) s0 = cfma(v[l], M[l], s0);
       const double2 s = cadd(cadd(s0, s1), cadd(s2, s3));
@@ -140,6 +162,100 @@ __device__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
   } else {  // MV_ZERO
     for (long long e = tid; e < op.na; e += nthreads) out[e] = make_double2(0.0, 0.0);
   }
+}
+
+// The same contraction with a.tpo (2, 4 or 8) consecutive lanes per output element: the
+// lanes of a group take every tpo-th term of the sum and combine their partial sums by
+// shuffles, and the group's first lane writes the element.  Small programs (leaves, bond
+// matrices, medium nodes) have far fewer output elements than the launch has threads and
+// are bound by the latency of one thread's chain of loads and FMAs, which this divides by
+// tpo.  Every op of a program uses the same groups, so the thread that writes element e
+// is the same in every op (accumulations into one buffer need no barrier between them);
+// the Lanczos passes own elements by thread, so such a program ends with a grid barrier.
+__device__ void run_op_g(const ExpmArgs& a, const MvOp& op, const double2* x) {
+  const double2* in = buf_of(a, op.in, x);
+  double2* out = buf_of(a, op.out, x);
+  const int tpo = a.tpo;
+  const long long nthreads = (long long)gridDim.x * blockDim.x;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long ngroups = nthreads / tpo, group = tid / tpo;
+  const int part = (int)(tid % tpo);
+  const bool acc = (op.beta != 0);
+  long long total;
+  if (op.kind == MV_MODE || op.kind == MV_CSR) total = op.na * op.d * op.nb;
+  else if (op.kind == MV_MF) total = op.na * op.d;
+  else total = op.na;
+  // uniform trip count across the warp: every lane joins the shuffles
+  for (long long e0 = 0; e0 < total; e0 += ngroups) {
+    const long long e = e0 + group;
+    const bool live = e < total;
+    double2 s = make_double2(0.0, 0.0);
+    if (op.kind == MV_MODE) {
+      if (live) {
+        const int d = op.d;
+        const long long nb = op.nb;
+        const long long aa = e / (d * nb), rem = e % (d * nb);
+        const int i = (int)(rem / nb);
+        const long long b = rem % nb;
+        const double2* S = op.mat + (long long)i * d;
+        const double2* v = in + aa * d * nb + b;
+        double2 s1 = s;
+        int j = part;
+        for (; j + tpo < d; j += 2 * tpo) {
+          const double2 p0 = S[j], q0 = v[(long long)j * nb], p1 = S[j + tpo], q1 = v[(long long)(j + tpo) * nb];
+          s = cfma(p0, q0, s);
+          s1 = cfma(p1, q1, s1);
+        }
+        if (j < d) s = cfma(S[j], v[(long long)j * nb], s);
+        s = cadd(s, s1);
+      }
+    } else if (op.kind == MV_MF) {
+      if (live) {
+        const int r = op.d;
+        const long long xx = e / r;
+        const int k = (int)(e % r);
+        const double2* v = in + xx * r;
+        const double2* M = op.mat + (long long)k * r;
+        double2 s1 = s;
+        int l = part;
+        for (; l + tpo < r; l += 2 * tpo) {
+          s = cfma(v[l], M[l], s);
+          s1 = cfma(v[l + tpo], M[l + tpo], s1);
+        }
+        if (l < r) s = cfma(v[l], M[l], s);
+        s = cadd(s, s1);
+      }
+    } else if (op.kind == MV_CSR) {
+      if (live && part == 0) {
+        const int d = op.d;
+        const long long nb = op.nb;
+        const long long aa = e / (d * nb), rem = e % (d * nb);
+        const int i = (int)(rem / nb);
+        const long long b = rem % nb;
+        const double2* v = in + aa * d * nb + b;
+        for (int q = op.rowptr[i]; q < op.rowptr[i + 1]; ++q) s = cfma(op.mat[q], v[(long long)op.colind[q] * nb], s);
+      }
+    }
+    if (op.kind == MV_MODE || op.kind == MV_MF) {
+      for (int o = tpo >> 1; o > 0; o >>= 1) {
+        s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+        s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+      }
+    }
+    if (live && part == 0) {
+      double2 r;
+      if (op.kind == MV_AXPY) r = cmul(op.alpha, in[e]);
+      else if (op.kind == MV_ZERO) r = make_double2(0.0, 0.0);
+      else r = cmul(op.alpha, s);
+      if (acc && op.kind != MV_ZERO) r = cadd(r, out[e]);
+      out[e] = r;
+    }
+  }
+}
+
+__device__ __forceinline__ void run_op(const ExpmArgs& a, const MvOp& op, const double2* x) {
+  if (a.tpo > 1) run_op_g(a, op, x);
+  else run_op_1(a, op, x);
 }
 
 __device__ __forceinline__ unsigned long long gtimer() {

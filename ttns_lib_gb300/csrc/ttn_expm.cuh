@@ -62,6 +62,8 @@ struct ExpmArgs {
   int tail_barrier;      // 1: a grid barrier after the program (tensor-core writes to p
                          // are distributed by tiles, not by the element-wise ownership the
                          // Lanczos passes assume)
+  int tpo;               // lanes per output element of the element-wise program ops (1, 2, 4
+                         // or 8; above 1 the program needs tail_barrier)
 };
 constexpr int kPhases = 16;  // begin, matvec, alpha, reorth coefficients, reorth + norm,
                              // ||H V_m||, control, combine, sub-steps, launches; then inside

@@ -737,6 +737,9 @@ struct Integrator {
       qr_scratch = (double*)(coop_buf.as<char>() + align256(sizeof(GridBarrier)));
       mixed = (cfg.precision == TTN_PREC_MIXED);
       if (const char* e = std::getenv("TTN_EXPM_CTA_FLOPS")) expm_cta_flops = std::atof(e);
+      if (const char* e = std::getenv("TTN_EXPM_ELEMS_PER_CTA")) expm_elems_per_cta = std::max(1, std::atoi(e));
+      if (const char* e = std::getenv("TTN_EXPM_TPO")) expm_tpo_max = std::max(1, std::min(8, std::atoi(e)));
+      if (const char* e = std::getenv("TTN_EXPM_TPO_MIN_FLOPS")) expm_tpo_min_flops = std::atof(e);
       if (const char* e = std::getenv("TTN_QR_ROWS_PER_CTA")) qr_rows_per_cta = std::max(1, std::atoi(e));
       if (const char* e = std::getenv("TTN_EXPM_ELEMS_PER_THREAD")) expm_elems_per_thread = std::max(0.1, std::atof(e));
       expm_max_grid = std::max(1, expm_coop_max_grid(0));
@@ -908,6 +911,8 @@ struct Integrator {
   }
 
   // bottom-up environment (single_particle_operator.hpp:26-103)
+  // A group with several tuples sums a_t X_t into w3 first and contracts once:
+  // sum_t a_t A^H X_t = A^H (sum_t a_t X_t), one K = dimen reduction instead of one per tuple.
   void update_spf(int nd, const double2* A) {
     if (on_op) on_op(OP_SPF, nd, 0);
     Prof pf(this, 5, nd);
@@ -915,12 +920,19 @@ struct Integrator {
     const int r = T.hrank[nd];
     for (auto& g : G[nd]) {
       if (g.id_spf) continue;
+      if (g.spf.size() == 1) {
+        const SpfTuple& t = g.spf[0];
+        const double2* X = apply_items(nd, t.items, A, w1, w2);
+        adj_mul(A, X, sz / r, r, g.spf_dev, t.a, false);
+        continue;
+      }
       bool first = true;
       for (const SpfTuple& t : g.spf) {
         const double2* X = apply_items(nd, t.items, A, w1, w2);
-        adj_mul(A, X, sz / r, r, g.spf_dev, t.a, !first);
+        mode_identity_axpy(X, w3, sz, t.a, !first);
         first = false;
       }
+      adj_mul(A, w3, sz / r, r, g.spf_dev, 1.0, false);
     }
   }
   // top-down environment of child nd (mean_field_operator.hpp:37-184)
@@ -936,17 +948,27 @@ struct Integrator {
     const long long szp = T.size(p);
     for (auto& g : G[nd]) {
       if (g.id_mf) continue;
-      bool first = true;
-      for (const MfKey& k : g.mf) {
+      if (g.mf.size() == 1) {
+        const MfKey& k = g.mf[0];
         const double2* X = apply_sibs(p, k.sib, Ap, w1, w2);
         if (!G[p][k.pg].id_mf) {
           double2* dst = (X == w1) ? w2 : w1;
           mf_apply(X, G[p][k.pg].mf_dev, rp, szp / rp, dst, 1.0, false);
           X = dst;
         }
-        mode_contract(Ap, X, na, d, nb, g.mf_dev, k.b, !first);
+        mode_contract(Ap, X, na, d, nb, g.mf_dev, k.b, false);
+        continue;
+      }
+      // several keys: sum_k b_k X_k into w3 (the parent's mean field applied on the way),
+      // then one contraction with the parent tensor
+      bool first = true;
+      for (const MfKey& k : g.mf) {
+        const double2* X = apply_sibs(p, k.sib, Ap, w1, w2);
+        if (!G[p][k.pg].id_mf) mf_apply(X, G[p][k.pg].mf_dev, rp, szp / rp, w3, k.b, !first);
+        else mode_identity_axpy(X, w3, szp, k.b, !first);
         first = false;
       }
+      mode_contract(Ap, w3, na, d, nb, g.mf_dev, 1.0, false);
     }
   }
   // out = H_eff(nd) v (coefficient_evolution_leaf / _branch)
@@ -1159,20 +1181,37 @@ struct Integrator {
     if (first) B.emit(mk(MV_ZERO, 0, 1, nullptr, sz, 0, 0, 0.0, false));
     return B.ops;
   }
+  // K R = sum_g s_g spf_g R mf_g^T.  The spf products of up to three groups go to the
+  // temporaries 2, 3, 4 first and the mean-field products follow, so that one grid barrier
+  // separates them instead of two per group; the accumulation order is the groups' order.
   std::vector<MvOp> kbond_program(int nd) {
     ProgBuilder B;
     B.mixed = mixed;
     const int r = T.hrank[nd];
     bool first = true;
-    for (auto& g : G[nd]) {
-      int X = 0;
-      if (!g.id_spf) {
-        B.emit(mk(MV_MODE, 0, 2, g.spf_dev, 1, r, r, 1.0, false));
-        X = 2;
+    const std::vector<Group>& gs = G[nd];
+    size_t i0 = 0;
+    while (i0 < gs.size()) {
+      size_t i1 = i0;
+      int used = 0;
+      while (i1 < gs.size() && (gs[i1].id_spf || used < 3)) {
+        if (!gs[i1].id_spf) ++used;
+        ++i1;
       }
-      if (g.id_mf) B.emit(mk(MV_AXPY, X, 1, nullptr, (long long)r * r, 0, 0, g.s, !first));
-      else B.emit(mk(MV_MF, X, 1, g.mf_dev, r, r, 0, g.s, !first));
-      first = false;
+      std::vector<int> X(i1 - i0, 0);
+      int nb = 0;
+      for (size_t k = i0; k < i1; ++k)
+        if (!gs[k].id_spf) {
+          X[k - i0] = 2 + nb++;
+          B.emit(mk(MV_MODE, 0, X[k - i0], gs[k].spf_dev, 1, r, r, 1.0, false));
+        }
+      for (size_t k = i0; k < i1; ++k) {
+        const Group& g = gs[k];
+        if (g.id_mf) B.emit(mk(MV_AXPY, X[k - i0], 1, nullptr, (long long)r * r, 0, 0, g.s, !first));
+        else B.emit(mk(MV_MF, X[k - i0], 1, g.mf_dev, r, r, 0, g.s, !first));
+        first = false;
+      }
+      i0 = i1;
     }
     if (first) B.emit(mk(MV_ZERO, 0, 1, nullptr, (long long)r * r, 0, 0, 0.0, false));
     return B.ops;
@@ -1214,11 +1253,14 @@ struct Integrator {
     CK(cudaMemcpyAsync(prog_buf.p, all.data(), all.size() * sizeof(MvOp), cudaMemcpyHostToDevice, stream));
     CK(cudaStreamSynchronize(stream));  // `all` is pageable and goes out of scope
   }
-  // CTAs of a Krylov launch: at most one per 64 vector elements and one per
+  // CTAs of a Krylov launch: at most one per expm_elems_per_cta vector elements and one per
   // expm_cta_flops of matvec work.  Small problems run on few CTAs (one CTA synchronises
   // with __syncthreads alone, several need grid barriers of a few microseconds each),
   // large ones on the whole device.
   double expm_cta_flops = 5.0e4;
+  long long expm_elems_per_cta = 64;  // at least this many vector elements per CTA
+  int expm_tpo_max = 8;               // most lanes per output element of the element-wise ops
+  double expm_tpo_min_flops = 2000.0; // matvec flops per vector element from which they are split
   // threads per CTA: about expm_elems_per_thread vector elements per thread, 64..256 (the
   // FP64 warp reductions cost the same per warp whatever the data, so tiny problems run on
   // fewer warps)
@@ -1229,7 +1271,7 @@ struct Integrator {
     return (int)std::max(64LL, std::min(256LL, t));
   }
   int expm_grid(long long n, bool tc, double flops_per_app) const {
-    long long g = (n + 63) / 64;
+    long long g = (n + expm_elems_per_cta - 1) / expm_elems_per_cta;
     if (expm_cta_flops > 0.0) {
       const long long gw = (long long)std::ceil(flops_per_app / expm_cta_flops);
       if (gw < g) g = gw;
@@ -1260,7 +1302,23 @@ struct Integrator {
     a.phase = phase_dev;
     a.tc_img = tc_img_buf.as<uint32_t>();
     const int grid = expm_grid(n, a.mixed, a.flops_per_app);
-    CK(expm_coop(a, grid, stream, expm_threads(n, grid)));
+    int threads = expm_threads(n, grid);
+    // launches with threads to spare give each output element of the element-wise ops
+    // several lanes (ExpmArgs::tpo) when the program has many terms per element (bond
+    // matrices: 6 products of 64 terms; measured: 11 % faster); with few terms per element
+    // (leaves, 256 x 64 nodes) the wider CTAs cost the Lanczos reductions more than the
+    // split saves
+    if (!a.mixed && expm_tpo_max > 1 && a.flops_per_app >= expm_tpo_min_flops * (double)n) {
+      const long long cap = (long long)grid * 256;
+      int tpo = 1;
+      while (tpo < expm_tpo_max && n * tpo * 2 <= cap) tpo *= 2;
+      if (tpo > 1) {
+        a.tpo = tpo;
+        a.tail_barrier = 1;
+        threads = (int)std::min<long long>(256, ((n * tpo + grid - 1) / grid + 31) / 32 * 32);
+      }
+    }
+    CK(expm_coop(a, grid, stream, threads));
     // Lanczos vector passes of one sub-step (the matvec flops are tallied on the device)
     if (tally) flops += lanczos_vec_flops(n);
   }
@@ -2632,7 +2690,7 @@ int ttn_debug_tc_gemm(const double* A, const double* B, double* D, int K, int N,
   CK(cudaMemcpy(D, dD, nd * sizeof(double), cudaMemcpyDeviceToHost));
   TTN_API_END
 }
-int ttn_debug_qr(int m, int n, double* a, double* r, int device) {
+static int debug_qr_impl(int m, int n, double* a, double* r, int device, double* phases) {
   TTN_API_BEGIN
   TTN_REQUIRE(a && r && m >= n && n >= 1 && n <= ttn::kMaxBond, TTN_EINVAL, "bad QR shape");
   CK(cudaSetDevice(device));
@@ -2664,7 +2722,9 @@ int ttn_debug_qr(int m, int n, double* a, double* r, int device) {
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   // the sweep's choice: the shared-memory kernel (8 rows per CTA, one CTA up to 64 rows)
   // when the grid holds every row, else the panel-blocked kernel
-  long long gr = m <= ttn::kQrRowsMax ? 1 : (m + 7) / 8;
+  long long target = 8;
+  if (const char* e = std::getenv("TTN_QR_ROWS_TARGET")) target = std::max(1, std::atoi(e));
+  long long gr = m <= ttn::kQrRowsMax ? 1 : (m + target - 1) / target;
   gr = std::min<long long>(gr, std::max(1, std::min(ttn::qr_rows_max_grid(), sms)));
   const bool rows = (m + gr - 1) / gr <= ttn::kQrRowsMax;
   int g = rows ? (int)gr : std::min(ttn::coop_qr_grid(m, sms), std::max(1, std::min(ttn::qr_blocked_max_grid(), sms)));
@@ -2675,7 +2735,14 @@ int ttn_debug_qr(int m, int n, double* a, double* r, int device) {
   auto* bar = cb.as<ttn::GridBarrier>();
   double* scr = (double*)(cb.as<char>() + ttn::align256(sizeof(ttn::GridBarrier)));
   int* err = (int*)(cb.as<char>() + ttn::align256(sizeof(ttn::GridBarrier)) + ttn::align256(sb));
-  if (rows) CK(ttn::householder_qr_rows(dA, m, n, dR, 0, dt, scr, bar, err, g, 0));
+  unsigned long long* ph = nullptr;
+  ttn::DevBuf pb;
+  if (phases && rows) {
+    pb.alloc(ttn::kQrPhases * sizeof(unsigned long long));
+    CK(cudaMemset(pb.p, 0, pb.bytes));
+    ph = pb.as<unsigned long long>();
+  }
+  if (rows) CK(ttn::householder_qr_rows(dA, m, n, dR, 0, dt, scr, bar, err, g, 0, ph));
   else CK(ttn::householder_qr_blocked(dA, m, n, dR, 0, dt, scr, bar, err, g, 0));
   CK(cudaDeviceSynchronize());
   CK(cudaGetLastError());
@@ -2685,7 +2752,16 @@ int ttn_debug_qr(int m, int n, double* a, double* r, int device) {
   CK(cudaGetLastError());
   CK(cudaMemcpy(a, dA, (size_t)m * n * sizeof(double2), cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(r, dR, (size_t)n * n * sizeof(double2), cudaMemcpyDeviceToHost));
+  if (phases) {
+    unsigned long long h[ttn::kQrPhases] = {};
+    if (ph) CK(cudaMemcpy(h, ph, sizeof(h), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < ttn::kQrPhases; ++k) phases[k] = (k == 8) ? (double)h[k] : 1e-3 * (double)h[k];
+  }
   TTN_API_END
+}
+int ttn_debug_qr(int m, int n, double* a, double* r, int device) { return debug_qr_impl(m, n, a, r, device, nullptr); }
+int ttn_debug_qr_phases(int m, int n, double* a, double* r, int device, double* phases) {
+  return debug_qr_impl(m, n, a, r, device, phases);
 }
 
 }  // extern "C"

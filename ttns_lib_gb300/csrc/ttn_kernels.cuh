@@ -89,8 +89,11 @@ cudaError_t householder_qr_blocked(double2* M, long long m, int n, double2* R, i
 constexpr int kQrRowsMax = 64;
 size_t qr_rows_scratch_bytes(int max_grid);
 int qr_rows_max_grid();
+// phase (optional): 16 ns counters, see ttn_qr_rows.cu
+constexpr int kQrPhases = 16;
 cudaError_t householder_qr_rows(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, double* scratch,
-                                GridBarrier* bar, int* err, int grid, cudaStream_t s);
+                                GridBarrier* bar, int* err, int grid, cudaStream_t s,
+                                unsigned long long* phase = nullptr);
 // QR of matrices with kQrMaxCols < n <= kMaxBond (cuSOLVER zgeqrf / zungqr on a
 // column-major copy; same conventions and arguments as householder_qr_coop).  The
 // workspace is sized at creation for the (m, n) shapes listed; a later call with a

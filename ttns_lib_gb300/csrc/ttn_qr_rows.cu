@@ -51,6 +51,23 @@ struct RqrArgs {
   double* scr;
   GridBarrier* bar;
   int* err;
+  unsigned long long* phase;  // optional: ns per phase as seen by thread 0 of CTA 0 (kQrPhases slots)
+};
+
+// wall time per phase as seen by thread 0 of CTA 0: column barrier, column sums, reflector,
+// w, row update, next partials, panel updates (factorisation), R and Q formation; slot 8
+// counts columns
+struct QrClock {
+  unsigned long long* acc;
+  unsigned long long t;
+  __device__ void mark(int k) {
+    if (acc) {
+      unsigned long long now;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+      acc[k] += now - t;
+      t = now;
+    }
+  }
 };
 
 // scratch layout (doubles), G = gridDim.x
@@ -360,6 +377,8 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
   const int nr = (int)(R.r1 - R.r0);
   const double safmin = 2.2250738585072014e-308 / 1.1102230246251565e-16;
   const int npan = (n + QNB - 1) / QNB;
+  QrClock pc{(a.phase && b == 0 && threadIdx.x == 0) ? a.phase : nullptr, 0ull};
+  if (pc.acc) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(pc.t));
   grid_barrier_begin(a.bar);
   for (int e = threadIdx.x; e < nr * n; e += QT) R.p[(e / n) * R.lds + e % n] = a.M[(R.r0 + e / n) * n + e % n];
   __syncthreads();
@@ -368,17 +387,38 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
   for (int p = 0; p < npan; ++p) {
     const int j0 = p * QNB, nbp = (n - j0) < QNB ? (n - j0) : QNB, jend = j0 + nbp;
     for (int j = j0; j < jend; ++j) {
+      pc.mark(6);
       grid_barrier(a.bar, a.err);
+      pc.mark(0);
+      if (pc.acc) pc.acc[8] += 1;
       const int nc = jend - j - 1;
       col_reduce(a, j, jend, S);
       __syncthreads();
+      pc.mark(1);
       if (threadIdx.x == 0) {
         const int E = S.E;
-        double xnorm = sqrt(S.nrm2);
-        if (E) xnorm = qldexp(xnorm, E);
         double ar = S.rowj[0].x, ai = S.rowj[0].y;
+        const double xn2 = S.nrm2, wa = fmax(fabs(ar), fabs(ai));
         int knt = 0;
         S.active = 0;
+        if (E == 0 && xn2 > 1e-300 && xn2 < 1e300 && (wa == 0.0 || (wa > 1e-150 && wa < 1e150))) {
+          // unscaled column of safe magnitude: beta from the squared norm by one square root,
+          // tau and 1 / (alpha - beta) by one division each (independent of each other);
+          // |beta| >= |x| > 1e-150, so no safe-minimum rescaling
+          const double bb = -copysign(sqrt(fma(ar, ar, fma(ai, ai, xn2))), ar >= 0.0 ? 1.0 : -1.0);
+          const double ib = 1.0 / bb;
+          const double dr = ar - bb, di = ai;
+          const double inv = 1.0 / fma(dr, dr, di * di);
+          S.tau[j] = make_double2((bb - ar) * ib, -ai * ib);
+          S.scal = make_double2(dr * inv, -di * inv);
+          S.beta = make_double2(bb, 0.0);
+          S.active = 1;
+          S.kx = 0;
+          S.kfac = 0;
+          if (b == 0) a.tau_out[j] = S.tau[j];
+        } else {
+        double xnorm = sqrt(xn2);
+        if (E) xnorm = qldexp(xnorm, E);
         if (xnorm == 0.0 && ai == 0.0) {
           S.tau[j] = make_double2(0.0, 0.0);
           S.beta = make_double2(ar, ai);
@@ -419,8 +459,10 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
         S.kx = 969 * knt;
         S.kfac = 969 * knt + E;
         if (b == 0) a.tau_out[j] = S.tau[j];
+        }
       }
       __syncthreads();
+      pc.mark(2);
       if (threadIdx.x >= 1 && threadIdx.x <= nc) {
         // w_c = M[j][c] + conj(scal) 2^kfac g_c, times conj(tau)
         double2 t = qmulc(S.scal, S.g[threadIdx.x]);
@@ -432,6 +474,7 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
         S.w[threadIdx.x] = qmulc(S.tau[j], wc);
       }
       __syncthreads();
+      pc.mark(3);
       // my rows: v below the diagonal, beta on it, the panel columns right of j updated
       if (S.active) {
         const double2 sc = S.scal;
@@ -454,7 +497,9 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
           for (int c = 1; c <= nc; ++c) R.at(j, j + c) = qfms(R.at(j, j + c), make_double2(1.0, 0.0), S.w[c]);
       }
       __syncthreads();
+      pc.mark(4);
       if (j + 1 < jend) col_partials(a, R, j + 1, jend);
+      pc.mark(5);
     }
     // ---- panel done: V top block for the Q formation, Gram and projections, T, update
     if (threadIdx.x < QNB * QNB) {
@@ -493,6 +538,7 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
       col_partials(a, R, jend, jend + ((n - jend) < QNB ? (n - jend) : QNB));
     }
   }
+  pc.mark(6);
   // ------------------------------------------------------------------ R
   for (int e = threadIdx.x; e < nr * n; e += QT) {
     const long long i = R.r0 + e / n;
@@ -558,6 +604,8 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
     }
   }
   for (int e = threadIdx.x; e < nr * n; e += QT) a.M[(R.r0 + e / n) * n + e % n] = R.p[(e / n) * R.lds + e % n];
+  __syncthreads();
+  pc.mark(7);
   grid_barrier_end(a.bar);
 }
 
@@ -578,9 +626,9 @@ int qr_rows_max_grid() {
 }
 
 cudaError_t householder_qr_rows(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, double* scratch,
-                                GridBarrier* bar, int* err, int grid, cudaStream_t s) {
+                                GridBarrier* bar, int* err, int grid, cudaStream_t s, unsigned long long* phase) {
   if (n < 1 || n > kQrMaxCols || m < n || grid < 1 || (m + grid - 1) / grid > kQrRowsMax) return cudaErrorInvalidValue;
-  RqrArgs a{M, m, n, R, Rt, tau_ws, scratch, bar, err};
+  RqrArgs a{M, m, n, R, Rt, tau_ws, scratch, bar, err, phase};
   void* args[] = {&a};
   ++g_launches;
   const int rows = (int)((m + grid - 1) / grid);

@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=3,
                     help="timed steps of the FP64 comparison arm (after the same warm-up steps)")
     ap.add_argument("--no-breakdown", action="store_true")
+    ap.add_argument("--drift", type=int, default=0, help="steps of the mixed vs FP64 drift run (no timing)")
+    ap.add_argument("--fd", type=int, default=0, help="adjoint form (--config c5): gradient components checked "
+                    "against central differences")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--override-n", type=int, default=None,
@@ -523,6 +526,129 @@ def run_expansion(args):
     return 0
 
 
+# ---------------------------------------------------------------- mixed vs FP64 drift
+def run_drift(args):
+    """|<sz>(mixed) - <sz>(FP64)| step by step over --drift steps of the headline workload's
+    model (use --override-n for a smaller tree with the same node shapes): both integrators
+    start from the same product state, take the same steps with the same Krylov stop rule,
+    and the largest difference so far is reported at powers of two and at the end."""
+    from ttns_lib_gb300 import api
+    from ttns_lib_gb300 import spin_boson as sb
+    over = {} if args.override_n is None else {"N": args.override_n}
+    m, cfg = sb.build_config(args.config, **over)
+    arms = {}
+    for name, prec in (("mixed", api.PREC_MIXED), ("fp64", api.PREC_FP64)):
+        A = api.httensor(m.topology, device=0)
+        A.init_product(np.array([1.0, 0.0]), seed=0)
+        it = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=cfg["krylov_dim"],
+                                                          krylov_tolerance=1e-12, precision=prec)
+        if args.krylov_stop == "residual":
+            it.set_krylov_stop(1)
+        it.dt = cfg["dt"]
+        arms[name] = (A, it)
+    worst, marks, first_above = 0.0, {}, None
+    t0 = time.perf_counter()
+    for k in range(1, args.drift + 1):
+        sz = {}
+        for name, (A, it) in arms.items():
+            it(A, m.sop, -1j)
+            sz[name] = it.mel()(sb.SZ, 0, A).real
+        worst = max(worst, abs(sz["mixed"] - sz["fp64"]))
+        if first_above is None and worst > 1e-6:
+            first_above = k
+        if (k & (k - 1)) == 0 or k == args.drift:
+            marks[k] = worst
+    line = {"metric": "max |<sz>(mixed) - <sz>(FP64)| over the first k steps", "impl": "drift",
+            "config": dict(workload_config(args.config, cfg, "mixed and fp64", over), krylov_stop=args.krylov_stop),
+            "steps": args.drift, "max_abs_dsz_by_step": marks, "first_step_above_1e-6": first_above,
+            "wall_s": time.perf_counter() - t0}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- adjoint form (c5)
+def generic_isometric_state(topo, seed):
+    """Random state with every non-root node an isometry (all bonds populated): gradients
+    through the QR gauge moves need invertible R factors, which a product state lacks."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(topo.nnodes):
+        d, r = topo.node_shape(i)
+        a = rng.normal(size=(d, r)) + 1j * rng.normal(size=(d, r))
+        out.append(np.linalg.qr(a)[0] if i else a / np.linalg.norm(a))
+    return out
+
+
+def run_adjoint(args):
+    """The adjoint form at its configuration's shapes: zero-temperature spin-boson, N = 128
+    modes (alpha = 0.4, wc = 5), d = 12, chi = 24, dt = 0.05, J = sum_t w_t <sz>(t) with
+    w_t ~ U[0, 1] (seeded), the gradient with respect to eps, Delta and all 128 c_k by the
+    device adjoint sweep with a checkpoint every 20 steps, over --steps time steps from a
+    seeded generic state.  The FP64 forward path over the same steps is timed beside it, and
+    --fd n checks n gradient components against central differences (h = 1e-6) of the
+    plain FP64 path."""
+    from ttns_lib_gb300 import api
+    from ttns_lib_gb300 import spin_boson as sb
+    rank, world, local = dist_env()
+    m, cfg = sb.build_config("c5")
+    topo = m.topology
+    nsteps = args.steps
+    st = generic_isometric_state(topo, seed=5)
+    wt = np.random.default_rng(17).uniform(size=nsteps)
+    theta = np.concatenate([[m.eps, m.delta], m.coupling])
+    evaluate = api.spin_boson_adjoint(m.omega, cfg["d"], cfg["chi"], st, cfg["dt"], wt, krylov_dim=cfg["krylov_dim"],
+                                      krylov_tolerance=1e-12, checkpoint_every=20, device=local)
+
+    def plain_J(th):
+        mm = sb.build_from_modes(m.omega, th[2:], cfg["d"], cfg["chi"], float(th[0]), float(th[1]))
+        A = api.httensor(topo, device=local)
+        A.set(st)
+        it = api.fixed_step_projector_splitting_integrator(A, mm.sop, krylov_dim=cfg["krylov_dim"],
+                                                          krylov_tolerance=1e-12)
+        it.dt = cfg["dt"]
+        J = 0.0
+        for k in range(nsteps):
+            it(A, mm.sop, -1j)
+            J += wt[k] * it.mel()(sb.SZ, 0, A).real
+        it.synchronize()
+        return J
+
+    for _ in range(max(0, args.warmup)):
+        plain_J(theta)
+    t0 = time.perf_counter()
+    J0 = plain_J(theta)
+    fwd_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    J, grad = evaluate(theta)
+    adj_s = time.perf_counter() - t0
+    fd = {}
+    if args.fd > 0:
+        h = 1e-6
+        idx = [0, 1] + [2 + int(k) for k in np.linspace(0, len(m.coupling) - 1, max(0, args.fd - 2)).astype(int)]
+        for i in idx[:args.fd]:
+            e = np.zeros_like(theta)
+            e[i] = h
+            fd[int(i)] = (plain_J(theta + e) - plain_J(theta - e)) / (2 * h)
+    names = ["eps", "delta"] + [f"c_{k}" for k in range(len(m.coupling))]
+    check = {names[i]: {"adjoint": float(grad[i]), "fd": v, "rel": abs(grad[i] - v) / max(abs(v), 1e-300)}
+             for i, v in fd.items()}
+    line = {
+        "metric": "adjoint gradient of a time-integrated <sz> (eps, Delta, 128 c_k), seconds per TDVP step",
+        "value": adj_s / nsteps, "unit": "s/step", "n_gpus": 1, "steps": nsteps, "warmup": args.warmup,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "impl": "adjoint",
+        "data": "synthetic (formula-generated bath; seeded generic start state and weights)",
+        "config": {"workload": "spin-boson (T=0), 128 bath modes, chi=24, d=12, dt=0.05, krylov_dim=12, "
+                               "checkpoint every 20 steps", "config": "c5", "nodes": topo.nnodes,
+                   "steps_of_config": 400},
+        "J": J, "J_plain_path": J0, "forward_s_per_step": fwd_s / nsteps, "adjoint_over_forward": adj_s / fwd_s,
+        "gradient_norm": float(np.linalg.norm(grad)), "fd_check": check,
+        "max_rel_fd": max((c["rel"] for c in check.values()), default=None),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 # ---------------------------------------------------------------- batched form (c4)
 def batched_specs(count: int, seed: int = 0):
     """Instances of the batched workload: alpha ~ U[0.05, 1], omega_c ~ U[1, 10],
@@ -604,6 +730,10 @@ def main():
         return run_batched(args)
     if args.config == "c2":
         return run_expansion(args)
+    if args.config == "c5":
+        return run_adjoint(args)
+    if args.drift > 0:
+        return run_drift(args)
     return run_ours(args)
 
 

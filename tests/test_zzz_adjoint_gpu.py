@@ -110,3 +110,43 @@ def test_device_adjoint_through_torch_matches_plain_path_differences():
         e[i] = h
         fd[i] = (plain_J(th + e) - plain_J(th - e)) / (2 * h)
     assert np.max(np.abs(grad.numpy() - fd)) <= 1e-5 * np.max(np.abs(fd))
+
+
+def test_device_adjoint_at_the_adjoint_workload_shapes():
+    """The adjoint workload's model (zero temperature, N = 128 modes, alpha = 0.4, wc = 5,
+    d = 12, chi = 24, dt = 0.05) over its first 6 steps from a generic state, with a
+    checkpoint every 3 steps: dJ/deps, dJ/dDelta and three coupling derivatives from the
+    device adjoint against central differences (h = 1e-6) of the plain FP64 device path,
+    within 1e-5 of the largest difference quotient."""
+    m, cfg = sb.build_config("c5")
+    topo = m.topology
+    rng = np.random.default_rng(55)
+    st = generic_state(topo, rng)
+    wt = rng.uniform(size=6)
+    theta = np.concatenate([[m.eps, m.delta], m.coupling])
+    J, grad = api.spin_boson_adjoint(m.omega, cfg["d"], cfg["chi"], st, cfg["dt"], wt, krylov_dim=cfg["krylov_dim"],
+                                     krylov_tolerance=1e-12, checkpoint_every=3)(theta)
+
+    def plain_J(th):
+        mm = sb.build_from_modes(m.omega, th[2:], cfg["d"], cfg["chi"], th[0], th[1])
+        A = api.httensor(topo, device=0)
+        A.set(st)
+        integ = api.fixed_step_projector_splitting_integrator(A, mm.sop, krylov_dim=cfg["krylov_dim"],
+                                                             krylov_tolerance=1e-12)
+        integ.dt = cfg["dt"]
+        out = 0.0
+        for k in range(len(wt)):
+            integ(A, mm.sop, -1j)
+            out += wt[k] * integ.mel()(sb.SZ, 0, A).real
+        return out
+
+    assert abs(plain_J(theta) - J) <= 1e-10 * max(1.0, abs(J))
+    h = 1e-6
+    idx = [0, 1, 2, 2 + 63, 2 + 127]
+    fd = []
+    for i in idx:
+        e = np.zeros_like(theta)
+        e[i] = h
+        fd.append((plain_J(theta + e) - plain_J(theta - e)) / (2 * h))
+    fd = np.array(fd)
+    assert np.max(np.abs(grad[idx] - fd)) <= 1e-5 * np.max(np.abs(fd)), (grad[idx], fd)

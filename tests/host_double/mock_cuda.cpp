@@ -79,7 +79,7 @@ cudaError_t cudaGetDeviceProperties(struct cudaDeviceProp* p, int d) { return cu
 
 namespace ttn {
 std::atomic<unsigned long long> g_launches{0};
-std::atomic<unsigned long long> g_wide_qr{0};  // QRs that took the wide (cuSOLVER) route
+std::atomic<unsigned long long> g_wide_qr{0};  // QRs of more than kQrMaxCols columns
 std::atomic<unsigned long long> g_csr_ops{0};  // sparse leaf-operator contractions applied
 
 static zc opA(const ZOperand& o, long long i, long long k) {
@@ -107,17 +107,19 @@ void zgemm(const ZGemm& g, double2* ws, size_t ws_bytes, cudaStream_t s) {
 }
 int coop_qr_grid(long long m, int n) { (void)m; (void)n; return 1; }
 size_t qr_rows_scratch_bytes(int g) { (void)g; return 1024; }
+int qr_rows_max_rows(int n) { return n <= kQrMaxCols ? kQrRowsMax : 30; }
 int qr_rows_max_grid() { return 1; }
 // the shared-memory QR: the oracle's Householder QR (one CTA holds at most kQrRowsMax rows)
 cudaError_t householder_qr_rows(double2* M, long long m, int n, double2* R, int Rt, double2* tau, double* scratch,
                                 GridBarrier* bar, int* err, int grid, cudaStream_t s, unsigned long long* phase) {
   (void)phase;
-  if (grid < 1 || (m + grid - 1) / grid > kQrRowsMax) return cudaErrorInvalidValue;
+  if (grid < 1 || (m + grid - 1) / grid > qr_rows_max_rows(n)) return cudaErrorInvalidValue;
   (void)tau; (void)scratch; (void)bar; (void)err; (void)s;
   std::vector<cd> Rr((size_t)n * n), t;
   orc::householder_qr(reinterpret_cast<cd*>(M), (size_t)m, n, Rr.data(), t);
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) R[(size_t)i * n + j] = D(Rt ? Rr[(size_t)j * n + i] : Rr[(size_t)i * n + j]);
+  if (n > kQrMaxCols) ++g_wide_qr;
   ++g_launches;
   return cudaSuccess;
 }
@@ -145,33 +147,8 @@ cudaError_t householder_qr_blocked(double2* M, long long m, int n, double2* R, i
   orc::householder_qr(reinterpret_cast<cd*>(M), (size_t)m, n, Rr.data(), t);
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) R[(size_t)i * n + j] = D(Rt ? Rr[(size_t)j * n + i] : Rr[(size_t)i * n + j]);
+  if (n > kQrMaxCols) ++g_wide_qr;
   ++g_launches;
-  return cudaSuccess;
-}
-// the cuSOLVER QR of wide bonds: the oracle's Householder QR, like the cooperative kernels
-struct WideQr {
-  long long max_elems = 0;
-  int max_n = 0;
-};
-cudaError_t wide_qr_create(WideQr** out, const long long* ms, const int* ns, int nshapes, cudaStream_t) {
-  WideQr* q = new WideQr();
-  for (int k = 0; k < nshapes; ++k) {
-    if (ns[k] < 1 || ns[k] > kMaxBond || ms[k] < ns[k]) { delete q; return cudaErrorInvalidValue; }
-    q->max_elems = std::max(q->max_elems, ms[k] * ns[k]);
-    q->max_n = std::max(q->max_n, ns[k]);
-  }
-  *out = q;
-  return cudaSuccess;
-}
-void wide_qr_destroy(WideQr* q) { delete q; }
-cudaError_t householder_qr_wide(WideQr* q, double2* M, long long m, int n, double2* R, int Rt, cudaStream_t) {
-  if (!q || n > q->max_n || m < n || m * n > q->max_elems) return cudaErrorInvalidValue;
-  std::vector<cd> Rr((size_t)n * n), t;
-  orc::householder_qr(reinterpret_cast<cd*>(M), (size_t)m, n, Rr.data(), t);
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) R[(size_t)i * n + j] = D(Rt ? Rr[(size_t)j * n + i] : Rr[(size_t)i * n + j]);
-  ++g_launches;
-  ++g_wide_qr;
   return cudaSuccess;
 }
 void permute_mode_last(const double2* A, double2* M, long long pre, int dm, long long post, cudaStream_t) {

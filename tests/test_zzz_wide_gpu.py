@@ -1,7 +1,8 @@
-"""Bonds wider than the cooperative QR kernels (64 < n <= 256): the cuSOLVER route of the
-gauge moves (ttns_lib_gb300/csrc/ttn_qr_wide.cu) against the oracle's Householder QR (the
-same LAPACK conventions, so the same gauge), and a sweep over a tree whose bonds are 70
-wide against the oracle."""
+"""Bonds wider than 64 (64 < n <= 256), which subspace expansion grows: the gauge moves'
+QR kernels in their wide instantiations (ttns_lib_gb300/csrc/ttn_qr_rows.cu with the rows in
+shared memory; ttn_qr.cu, rows in global memory, for matrices too tall for that) against the
+oracle's Householder QR (the same LAPACK conventions, so the same gauge), and a sweep over a
+tree whose bonds are 70 wide against the oracle.  No library QR is involved."""
 import numpy as np
 import pytest
 
@@ -13,7 +14,7 @@ from ttns_lib_gb300.model import Topology
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("m,n", [(300, 96), (160, 160), (2000, 256)])
+@pytest.mark.parametrize("m,n", [(300, 96), (160, 160), (2000, 256), (12000, 200)])
 def test_wide_qr_matches_the_oracle(m, n):
     rng = np.random.default_rng(m + n)
     a = rng.normal(size=(m, n)) + 1j * rng.normal(size=(m, n))

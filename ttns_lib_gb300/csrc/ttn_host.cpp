@@ -444,7 +444,6 @@ struct Integrator {
   std::vector<double2*> rmat, mel;
   double2 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w4 = nullptr, *V = nullptr, *p = nullptr,
           *gws = nullptr, *qtau = nullptr, *scal = nullptr;
-  WideQr* wide = nullptr;  // cuSOLVER QR of matricisations wider than kQrMaxCols
   int krylov_stop = 0;     // 1: Lanczos recurrences end on the residual estimate
   size_t gws_bytes = 0;
   long long maxsize = 0, ldv = 0;
@@ -527,7 +526,6 @@ struct Integrator {
   bool expanded = false;
 
   ~Integrator() {
-    wide_qr_destroy(wide);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -679,7 +677,7 @@ struct Integrator {
     wb += (size_t)(m + 1) * ldv * sizeof(double2);               // V
     wb += align256(ldv * sizeof(double2));                        // p
     wb += gws_bytes;                                              // zgemm split-K
-    wb += align256(kQrMaxCols * sizeof(double2));                 // QR tau
+    wb += align256(kMaxBond * sizeof(double2));                   // QR tau
     wb += align256(64 * sizeof(double2));                         // scalars
     work_buf.alloc(wb);
     {
@@ -693,25 +691,8 @@ struct Integrator {
       V = take((size_t)(m + 1) * ldv * sizeof(double2));
       p = take(ldv * sizeof(double2));
       gws = take(gws_bytes);
-      qtau = take(kQrMaxCols * sizeof(double2));
+      qtau = take(kMaxBond * sizeof(double2));
       scal = take(64 * sizeof(double2));
-    }
-    // bonds wider than the cooperative QR kernels take: cuSOLVER workspace for every
-    // matricisation that can be wider (gauge moves towards the root and the leaves)
-    {
-      std::vector<long long> ms;
-      std::vector<int> ns;
-      for (int i = 0; i < T.n; ++i) {
-        if (i != 0 && Z.hrank[i] > kQrMaxCols) { ms.push_back((long long)Z.dimen[i]); ns.push_back(Z.hrank[i]); }
-        if (Z.leaf(i)) continue;  // root-to-leaf moves factor branch nodes only
-        for (int mu = 0; mu < Z.nmodes[i]; ++mu) {
-          const int d = Z.dims[i][mu];
-          if (d > kQrMaxCols) { ms.push_back((long long)Z.dimen[i] * Z.hrank[i] / d); ns.push_back(d); }
-        }
-      }
-      wide_qr_destroy(wide);
-      wide = nullptr;
-      if (!ns.empty()) CK(wide_qr_create(&wide, ms.data(), ns.data(), (int)ns.size(), stream));
     }
   }
 
@@ -1335,17 +1316,14 @@ struct Integrator {
   int qr_rows_per_cta = 32;  // rows of the matrix per CTA of the panel-blocked QR (tall matrices)
   int qr_rows_target = 8;    // rows per CTA of the shared-memory QR
   void qr(double2* M, long long m, int n, double2* R, int Rt) {
-    if (n > kQrMaxCols) {
-      TTN_REQUIRE(wide, TTN_EINVAL, "no workspace for a QR wider than 64 columns");
-      CK(householder_qr_wide(wide, M, m, n, R, Rt, stream));
-      return;
-    }
-    // rows resident in shared memory: about qr_rows_target rows per CTA (one CTA up to 64
-    // rows), as long as the grid holds every row
+    TTN_REQUIRE(n >= 1 && n <= kMaxBond, TTN_ECAPACITY, "a gauge move wider than 256 columns");
+    // rows resident in shared memory: about qr_rows_target rows per CTA (one CTA while the
+    // rows fit), as long as the grid holds every row; else the panel-blocked kernel
     {
-      long long g = m <= kQrRowsMax ? 1 : (m + qr_rows_target - 1) / qr_rows_target;
+      const long long cap = qr_rows_max_rows(n);
+      long long g = m <= cap ? 1 : (m + qr_rows_target - 1) / qr_rows_target;
       if (g > qr_rows_grid) g = qr_rows_grid;
-      if ((m + g - 1) / g <= kQrRowsMax) {
+      if (cap > 0 && (m + g - 1) / g <= cap) {
         CK(householder_qr_rows(M, m, n, R, Rt, qtau, qr_scratch, bar, status, (int)g, stream));
         return;
       }
@@ -2694,26 +2672,8 @@ static int debug_qr_impl(int m, int n, double* a, double* r, int device, double*
   TTN_API_BEGIN
   TTN_REQUIRE(a && r && m >= n && n >= 1 && n <= ttn::kMaxBond, TTN_EINVAL, "bad QR shape");
   CK(cudaSetDevice(device));
-  if (n > ttn::kQrMaxCols) {
-    ttn::DevBuf wb;
-    wb.alloc(((size_t)m * n + (size_t)n * n) * sizeof(double2));
-    double2* dA = wb.as<double2>();
-    double2* dR = dA + (size_t)m * n;
-    CK(cudaMemcpy(dA, a, (size_t)m * n * sizeof(double2), cudaMemcpyHostToDevice));
-    long long mm = m;
-    ttn::WideQr* q = nullptr;
-    CK(ttn::wide_qr_create(&q, &mm, &n, 1, 0));
-    cudaError_t e = ttn::householder_qr_wide(q, dA, m, n, dR, 0, 0);
-    cudaError_t e2 = cudaDeviceSynchronize();
-    ttn::wide_qr_destroy(q);
-    CK(e);
-    CK(e2);
-    CK(cudaMemcpy(a, dA, (size_t)m * n * sizeof(double2), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(r, dR, (size_t)n * n * sizeof(double2), cudaMemcpyDeviceToHost));
-    return TTN_OK;
-  }
   ttn::DevBuf buf;
-  buf.alloc(((size_t)m * n + (size_t)n * n + ttn::kQrMaxCols) * sizeof(double2));
+  buf.alloc(((size_t)m * n + (size_t)n * n + ttn::kMaxBond) * sizeof(double2));
   double2* dA = buf.as<double2>();
   double2* dR = dA + (size_t)m * n;
   double2* dt = dR + (size_t)n * n;
@@ -2724,9 +2684,10 @@ static int debug_qr_impl(int m, int n, double* a, double* r, int device, double*
   // when the grid holds every row, else the panel-blocked kernel
   long long target = 8;
   if (const char* e = std::getenv("TTN_QR_ROWS_TARGET")) target = std::max(1, std::atoi(e));
-  long long gr = m <= ttn::kQrRowsMax ? 1 : (m + target - 1) / target;
+  const long long cap = ttn::qr_rows_max_rows(n);
+  long long gr = m <= cap ? 1 : (m + target - 1) / target;
   gr = std::min<long long>(gr, std::max(1, std::min(ttn::qr_rows_max_grid(), sms)));
-  const bool rows = (m + gr - 1) / gr <= ttn::kQrRowsMax;
+  const bool rows = cap > 0 && (m + gr - 1) / gr <= cap;
   int g = rows ? (int)gr : std::min(ttn::coop_qr_grid(m, sms), std::max(1, std::min(ttn::qr_blocked_max_grid(), sms)));
   const size_t sb = rows ? ttn::qr_rows_scratch_bytes(g) : ttn::qr_blocked_scratch_bytes(g);
   ttn::DevBuf cb;

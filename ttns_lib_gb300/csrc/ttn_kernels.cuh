@@ -60,7 +60,7 @@ struct KrylovCtl {
 };
 
 constexpr int kQrMaxCols = 64;   // widest matrix the cooperative device QR kernels accept
-constexpr int kMaxBond = 256;    // widest bond of the FP64 sweep (QRs above kQrMaxCols: ttn_qr_wide.cu)
+constexpr int kMaxBond = 256;    // widest bond of the FP64 sweep (its gauge QRs: ttn_qr_rows.cu, ttn_qr.cu)
 constexpr int kKrylovMax = 64;   // largest Krylov dimension
 
 // ---- Householder QR --------------------------------------------------------------
@@ -77,31 +77,27 @@ cudaError_t coop_qr_max_grid(int* out);
 cudaError_t householder_qr_coop(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, double* scratch,
                                 GridBarrier* bar, int* err, int grid, cudaStream_t s);
 // Panel-blocked cooperative Householder QR (ttn_qr.cu), same conventions and arguments
-// as householder_qr_coop; scratch of qr_blocked_scratch_bytes(grid) bytes.
+// as householder_qr_coop but n <= kMaxBond; scratch of qr_blocked_scratch_bytes(grid)
+// bytes; qr_blocked_max_grid() must run once before the first launch (it sets the
+// kernels' shared-memory limit).
 size_t qr_blocked_scratch_bytes(int max_grid);
 int qr_blocked_max_grid();
 cudaError_t householder_qr_blocked(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws,
                                    double* scratch, GridBarrier* bar, int* err, int grid, cudaStream_t s);
 // Householder QR with every CTA's rows held in shared memory (ttn_qr_rows.cu), same
-// conventions and arguments as householder_qr_blocked; at most kQrRowsMax rows per CTA
-// (ceil(m / grid) <= kQrRowsMax, else cudaErrorInvalidValue); scratch of
-// qr_rows_scratch_bytes(grid) bytes.
+// conventions and arguments as householder_qr_blocked, n <= kMaxBond; at most
+// qr_rows_max_rows(n) <= kQrRowsMax rows per CTA (else cudaErrorInvalidValue); scratch of
+// qr_rows_scratch_bytes(grid) bytes; qr_rows_max_grid() must run once before the first
+// launch (it sets the kernels' shared-memory limit).
 constexpr int kQrRowsMax = 64;
 size_t qr_rows_scratch_bytes(int max_grid);
+int qr_rows_max_rows(int n);
 int qr_rows_max_grid();
 // phase (optional): 16 ns counters, see ttn_qr_rows.cu
 constexpr int kQrPhases = 16;
 cudaError_t householder_qr_rows(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, double* scratch,
                                 GridBarrier* bar, int* err, int grid, cudaStream_t s,
                                 unsigned long long* phase = nullptr);
-// QR of matrices with kQrMaxCols < n <= kMaxBond (cuSOLVER zgeqrf / zungqr on a
-// column-major copy; same conventions and arguments as householder_qr_coop).  The
-// workspace is sized at creation for the (m, n) shapes listed; a later call with a
-// larger shape returns cudaErrorInvalidValue.
-struct WideQr;
-cudaError_t wide_qr_create(WideQr** out, const long long* ms, const int* ns, int nshapes, cudaStream_t s);
-void wide_qr_destroy(WideQr* q);
-cudaError_t householder_qr_wide(WideQr* q, double2* M, long long m, int n, double2* R, int Rt, cudaStream_t s);
 // r2l matricisation: M(y*pre + x, i) = A((x*dm + i)*post + y) and its inverse.
 void permute_mode_last(const double2* A, double2* M, long long pre, int dm, long long post, cudaStream_t s);
 void unpermute_mode_last(const double2* M, double2* A, long long pre, int dm, long long post, cudaStream_t s);

@@ -28,9 +28,10 @@ namespace {
 
 constexpr int BT = 256;                 // threads per CTA
 constexpr int NB = 8;                   // panel width
-constexpr int BN = kQrMaxCols;          // widest matrix
-constexpr int NP = BN / NB;             // most panels
-constexpr int PW = NB * (NB + BN);      // complex entries of one panel block V^H [V | M_trailing]
+// BN: widest matrix of an instantiation (64, or kMaxBond); BN / NB panels at most;
+// NB (NB + BN) complex entries in one panel block V^H [V | M_trailing]
+template <int BN> __host__ __device__ constexpr int np_of() { return BN / NB; }
+template <int BN> __host__ __device__ constexpr int pw_of() { return NB * (NB + BN); }
 
 struct BqrArgs {
   double2* M;
@@ -49,9 +50,11 @@ __host__ __device__ constexpr size_t off_cp(int) { return 0; }                  
 __host__ __device__ constexpr size_t off_gp(int G) { return (size_t)4 * G; }                     // [2][G][2NB]
 __host__ __device__ constexpr size_t off_cj(int G) { return off_gp(G) + (size_t)4 * NB * G; }    // [2][2+2NB]
 __host__ __device__ constexpr size_t off_pp(int G) { return off_cj(G) + 2 * (2 + 2 * NB); }      // [G][2PW]
-__host__ __device__ constexpr size_t off_pr(int G) { return off_pp(G) + (size_t)2 * PW * G; }    // [2PW]
-__host__ __device__ constexpr size_t off_vt(int G) { return off_pr(G) + 2 * PW; }                // [NP][2NB*NB]
-__host__ __device__ constexpr size_t scratch_doubles(int G) { return off_vt(G) + (size_t)NP * 2 * NB * NB; }
+template <int BN> __host__ __device__ constexpr size_t off_pr(int G) { return off_pp(G) + (size_t)2 * pw_of<BN>() * G; }
+template <int BN> __host__ __device__ constexpr size_t off_vt(int G) { return off_pr<BN>(G) + 2 * pw_of<BN>(); }
+template <int BN> __host__ __device__ constexpr size_t scratch_doubles(int G) {
+  return off_vt<BN>(G) + (size_t)np_of<BN>() * 2 * NB * NB;
+}
 
 __device__ __forceinline__ double2 cadd2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
@@ -120,12 +123,13 @@ __device__ double2 cdiv_b(double2 a, double2 b) {
   return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
 }
 
+template <int BN>
 struct Smem {
   unsigned long long umax[BT / 32];
   double dsum[BT / 32];
   double2 csum[BT / 32][NB];
   double2 tau[BN];
-  double2 T[NP][NB][NB];     // compact WY factors of every panel
+  double2 T[BN / NB][NB][NB];  // compact WY factors of every panel
   double2 P[NB][NB + BN];    // reduced panel block (Gram | projections)
   double2 W[NB][NB + BN];    // T^H P (factorisation) or T P (Q formation)
   double2 w[NB];             // column projections within the panel (times conj(tau))
@@ -135,7 +139,8 @@ struct Smem {
   int active;
 };
 
-__device__ __forceinline__ double block_sum_d(double v, Smem& S) {
+template <int BN>
+__device__ __forceinline__ double block_sum_d(double v, Smem<BN>& S) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) S.dsum[threadIdx.x >> 5] = v;
@@ -146,7 +151,8 @@ __device__ __forceinline__ double block_sum_d(double v, Smem& S) {
   __syncthreads();
   return s;
 }
-__device__ __forceinline__ unsigned long long block_max_u(unsigned long long v, Smem& S) {
+template <int BN>
+__device__ __forceinline__ unsigned long long block_max_u(unsigned long long v, Smem<BN>& S) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
@@ -172,7 +178,8 @@ __device__ __forceinline__ double2 vpanel(const BqrArgs& a, long long i, int j0,
 // Partials of column j for my rows (j < jend): scaled norm of rows > j, Gram of the
 // subdiagonal part with the panel columns c in (j, jend), and from the owner of row j:
 // alpha and M[j][c].
-__device__ void column_partials(const BqrArgs& a, int j, int jend, long long r0, long long r1, Smem& S) {
+template <int BN>
+__device__ void column_partials(const BqrArgs& a, int j, int jend, long long r0, long long r1, Smem<BN>& S) {
   const int G = gridDim.x, b = blockIdx.x, par = j & 1, n = a.n;
   double* cp = a.scr + off_cp(G) + (size_t)par * 2 * G;
   double* gp = a.scr + off_gp(G) + (size_t)par * 2 * NB * G;
@@ -237,10 +244,11 @@ __device__ void column_partials(const BqrArgs& a, int j, int jend, long long r0,
 // Panel block partials: P[k][c] = sum over my rows i >= j0 of conj(V(i,k)) X(i, c) with
 // X = [V | M[:, c0:]] (ncx = nbp + nct columns) for the factorisation, or X = M[:, c0:]
 // (ncx = nct) for the Q formation.
+template <int BN>
 __device__ void panel_partials(const BqrArgs& a, int j0, int nbp, int c0, int nct, bool with_gram, long long r0,
                                long long r1) {
   const int G = gridDim.x, b = blockIdx.x, n = a.n;
-  double* pp = a.scr + off_pp(G) + (size_t)b * 2 * PW;
+  double* pp = a.scr + off_pp(G) + (size_t)b * 2 * pw_of<BN>();
   const int ncx = (with_gram ? nbp : 0) + nct;
   const long long lo = r0 > j0 ? r0 : j0;
   for (int e = threadIdx.x; e < nbp * ncx; e += blockDim.x) {
@@ -266,17 +274,18 @@ __device__ void panel_partials(const BqrArgs& a, int j0, int nbp, int c0, int nc
 
 // every CTA reduces a slice of the panel block entries over the G partials (one warp
 // per entry), then, after a barrier, every CTA loads the whole block into S.P
-__device__ void panel_reduce(const BqrArgs& a, int nbp, int ncx, Smem& S) {
+template <int BN>
+__device__ void panel_reduce(const BqrArgs& a, int nbp, int ncx, Smem<BN>& S) {
   const int G = gridDim.x, b = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const double* pp = a.scr + off_pp(G);
-  double* pr = a.scr + off_pr(G);
+  double* pr = a.scr + off_pr<BN>(G);
   const int total = nbp * ncx;
   for (int e = b + G * warp; e < total; e += G * (BT / 32)) {
     double sx = 0.0, sy = 0.0;
     for (int q = lane; q < G; q += 32) {
-      sx += pp[(size_t)q * 2 * PW + 2 * e];
-      sy += pp[(size_t)q * 2 * PW + 2 * e + 1];
+      sx += pp[(size_t)q * 2 * pw_of<BN>() + 2 * e];
+      sy += pp[(size_t)q * 2 * pw_of<BN>() + 2 * e + 1];
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -295,7 +304,8 @@ __device__ void panel_reduce(const BqrArgs& a, int nbp, int ncx, Smem& S) {
 
 // T of panel p from its Gram matrix S.P[:, 0:nbp] and the taus (zlarft forward,
 // column-wise): T(i,i) = tau_i, T(0:i, i) = -tau_i T(0:i, 0:i) G(0:i, i)
-__device__ void form_t(int p, int j0, int nbp, Smem& S) {
+template <int BN>
+__device__ void form_t(int p, int j0, int nbp, Smem<BN>& S) {
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     for (int i = 0; i < nbp; ++i) {
@@ -319,8 +329,10 @@ __device__ void form_t(int p, int j0, int nbp, Smem& S) {
   __syncthreads();
 }
 
+template <int BN>
 __global__ void __launch_bounds__(BT) k_qr_blocked(BqrArgs a) {
-  __shared__ Smem S;
+  extern __shared__ __align__(16) unsigned char b_dyn[];
+  Smem<BN>& S = *reinterpret_cast<Smem<BN>*>(b_dyn);
   const int G = gridDim.x, b = blockIdx.x, n = a.n;
   const long long m = a.m;
   const long long r0 = b * m / G, r1 = (b + 1) * m / G;
@@ -464,13 +476,13 @@ __global__ void __launch_bounds__(BT) k_qr_blocked(BqrArgs a) {
       const long long i = j0 + aa;
       if (aa < nbp && k < nbp && i >= r0 && i < r1) {
         const double2 v = vpanel(a, i, j0, k);
-        double* vt = a.scr + off_vt(G) + (size_t)p * 2 * NB * NB;
+        double* vt = a.scr + off_vt<BN>(G) + (size_t)p * 2 * NB * NB;
         vt[2 * (aa * NB + k)] = v.x;
         vt[2 * (aa * NB + k) + 1] = v.y;
       }
     }
     const int nct = n - jend;
-    panel_partials(a, j0, nbp, jend, nct, true, r0, r1);
+    panel_partials<BN>(a, j0, nbp, jend, nct, true, r0, r1);
     grid_barrier(a.bar, a.err);
     panel_reduce(a, nbp, nbp + nct, S);
     form_t(p, j0, nbp, S);
@@ -511,7 +523,7 @@ __global__ void __launch_bounds__(BT) k_qr_blocked(BqrArgs a) {
     const int nct = n - jend;
     const long long lo = r0 > j0 ? r0 : j0;
     if (nct > 0) {
-      panel_partials(a, j0, nbp, jend, nct, false, r0, r1);
+      panel_partials<BN>(a, j0, nbp, jend, nct, false, r0, r1);
       grid_barrier(a.bar, a.err);
       panel_reduce(a, nbp, nct, S);
       // W = T (V^H Q_trailing); Q_trailing -= V W
@@ -533,7 +545,7 @@ __global__ void __launch_bounds__(BT) k_qr_blocked(BqrArgs a) {
     }
     // panel columns: Q[:, j0 + k] = e_{j0+k} - V W2, W2 = T V_top^H
     {
-      const double* vt = a.scr + off_vt(G) + (size_t)p * 2 * NB * NB;
+      const double* vt = a.scr + off_vt<BN>(G) + (size_t)p * 2 * NB * NB;
       for (int e = threadIdx.x; e < nbp * nbp; e += blockDim.x) {
         const int aa = e / nbp, k = e % nbp;
         double2 s = make_double2(0.0, 0.0);
@@ -564,22 +576,35 @@ __global__ void __launch_bounds__(BT) k_qr_blocked(BqrArgs a) {
 
 }  // namespace
 
-size_t qr_blocked_scratch_bytes(int max_grid) { return scratch_doubles(max_grid) * sizeof(double); }
+size_t qr_blocked_scratch_bytes(int max_grid) { return scratch_doubles<kMaxBond>(max_grid) * sizeof(double); }
 
-int qr_blocked_max_grid() {
+namespace {
+template <int BN> int blocked_max_grid_bn() {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_qr_blocked, BT, 0);
+  cudaFuncSetAttribute(k_qr_blocked<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem<BN>));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_qr_blocked<BN>, BT, sizeof(Smem<BN>));
   return sms * (per < 1 ? 1 : per);
+}
+}  // namespace
+
+int qr_blocked_max_grid() {
+  const int a = blocked_max_grid_bn<kQrMaxCols>(), b = blocked_max_grid_bn<kMaxBond>();
+  return a < b ? a : b;
 }
 
 cudaError_t householder_qr_blocked(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws,
                                    double* scratch, GridBarrier* bar, int* err, int grid, cudaStream_t s) {
+  if (n < 1 || n > kMaxBond || m < n || grid < 1) return cudaErrorInvalidValue;
   BqrArgs a{M, m, n, R, Rt, tau_ws, scratch, bar, err};
   void* args[] = {&a};
   ++g_launches;
-  return cudaLaunchCooperativeKernel((const void*)k_qr_blocked, dim3(grid), dim3(BT), args, 0, s);
+  if (n <= kQrMaxCols)
+    return cudaLaunchCooperativeKernel((const void*)k_qr_blocked<kQrMaxCols>, dim3(grid), dim3(BT), args,
+                                       sizeof(Smem<kQrMaxCols>), s);
+  return cudaLaunchCooperativeKernel((const void*)k_qr_blocked<kMaxBond>, dim3(grid), dim3(BT), args,
+                                     sizeof(Smem<kMaxBond>), s);
 }
 
 }  // namespace ttn

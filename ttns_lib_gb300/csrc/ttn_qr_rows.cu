@@ -22,7 +22,10 @@
 //     thread per row, so no FP64 instruction is repeated by idle warps.
 // The trailing columns are updated once per panel of 8 with the compact WY form (zlarft /
 // zlarfb), whose V^H [V | M] partials are reduced cooperatively, and Q is formed backwards
-// panel by panel (zungqr).  A CTA holds at most kQrRowsMax rows.
+// panel by panel (zungqr).  A CTA holds at most kQrRowsMax rows, fewer for wide matrices
+// (qr_rows_max_rows: the rows and the per-CTA state share the opt-in shared memory).  Two
+// instantiations: matrices of up to 64 columns, and of up to kMaxBond (bonds that subspace
+// expansion grows past 64).
 #include "ttn_coop.cuh"
 #include "ttn_kernels.cuh"
 
@@ -35,10 +38,13 @@ namespace {
 constexpr int QT = 256;                 // threads per CTA
 constexpr int QW = QT / 32;             // warps
 constexpr int QNB = 8;                  // panel width: one warp per panel column slot
-constexpr int QBN = kQrMaxCols;         // widest matrix
-constexpr int QNP = QBN / QNB;          // most panels
-constexpr int QPW = QNB * (QNB + QBN);  // complex entries of one panel block V^H [V | M_trailing]
+// BN: widest matrix of an instantiation (64, or kMaxBond for the bonds that subspace
+// expansion grows past 64); BN / QNB panels at most; QNB (QNB + BN) complex entries in one
+// panel block V^H [V | M_trailing]
+template <int BN> __host__ __device__ constexpr int qnp() { return BN / QNB; }
+template <int BN> __host__ __device__ constexpr int qpw() { return QNB * (QNB + BN); }
 constexpr int kNoScale = -100000;       // scale exponent published by a CTA with a zero column
+constexpr int kQrPartsPerLane = 8;      // column partials per lane in the reduction: grids up to 256
 static_assert(QW == QNB, "one warp per panel column slot");
 
 struct RqrArgs {
@@ -75,14 +81,16 @@ struct QrClock {
 //                           (0: unscaled, kNoScale: zero column), [1] sum |x 2^-e|^2 over
 //                           its rows below the diagonal, [2w, 2w+1] sum conj(x 2^-e) M[:, j+w]
 //   rowj [2][2 QNB]         M[j][j .. jend) from the CTA holding row j
-//   pp   [G][2 QPW]         panel block partials;  pr [2 QPW] their sums
-//   vt   [QNP][2 QNB QNB]   the top block of every panel's V (Q formation)
+//   pp   [G][2 qpw]         panel block partials;  pr [2 qpw] their sums
+//   vt   [qnp][2 QNB QNB]   the top block of every panel's V (Q formation)
 __host__ __device__ constexpr size_t rq_colw() { return 2 + 2 * QNB; }
 __host__ __device__ constexpr size_t rq_off_rowj(int G) { return (size_t)2 * G * rq_colw(); }
 __host__ __device__ constexpr size_t rq_off_pp(int G) { return rq_off_rowj(G) + 4 * QNB; }
-__host__ __device__ constexpr size_t rq_off_pr(int G) { return rq_off_pp(G) + (size_t)2 * QPW * G; }
-__host__ __device__ constexpr size_t rq_off_vt(int G) { return rq_off_pr(G) + 2 * QPW; }
-__host__ __device__ constexpr size_t rq_doubles(int G) { return rq_off_vt(G) + (size_t)QNP * 2 * QNB * QNB; }
+template <int BN> __host__ __device__ constexpr size_t rq_off_pr(int G) { return rq_off_pp(G) + (size_t)2 * qpw<BN>() * G; }
+template <int BN> __host__ __device__ constexpr size_t rq_off_vt(int G) { return rq_off_pr<BN>(G) + 2 * qpw<BN>(); }
+template <int BN> __host__ __device__ constexpr size_t rq_doubles(int G) {
+  return rq_off_vt<BN>(G) + (size_t)qnp<BN>() * 2 * QNB * QNB;
+}
 
 __device__ __forceinline__ double2 qadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 qmul(double2 a, double2 b) {
@@ -145,11 +153,13 @@ __device__ double2 qdiv(double2 a, double2 b) {  // Smith's division
   return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
 }
 
+// per-CTA state, at the start of the dynamic shared memory (the rows follow it)
+template <int BN>
 struct RSmem {
-  double2 tau[QBN];
-  double2 T[QNP][QNB][QNB];     // compact WY factors of every panel
-  double2 P[QNB][QNB + QBN];    // reduced panel block (Gram | projections)
-  double2 W[QNB][QNB + QBN];    // T^H P (factorisation) or T P (Q formation)
+  double2 tau[BN];
+  double2 T[BN / QNB][QNB][QNB];  // compact WY factors of every panel
+  double2 P[QNB][QNB + BN];       // reduced panel block (Gram | projections)
+  double2 W[QNB][QNB + BN];       // T^H P (factorisation) or T P (Q formation)
   double2 g[QNB];               // Gram sums of column j with the panel columns, relative to 2^E
   double2 rowj[QNB];            // M[j][j .. jend), read next to the partials
   double2 w[QNB];               // conj(tau) conj(v)^T M[:, c] for the panel columns c
@@ -217,7 +227,7 @@ __device__ void col_partials(const RqrArgs& a, const Rows& R, int j, int jend) {
     }
     if (lane == 0) {
       if (w == 0) {
-        cp[0] = (double)(lmax > 0.0 ? e : kNoScale);
+        reinterpret_cast<long long*>(cp)[0] = (long long)(lmax > 0.0 ? e : kNoScale);
         cp[1] = acc.x;
       } else {
         cp[2 * w] = acc.x;
@@ -234,7 +244,8 @@ __device__ void col_partials(const RqrArgs& a, const Rows& R, int j, int jend) {
 }
 
 // After the grid barrier: the column's sums over all CTAs (warp w: slot w) into S.
-__device__ void col_reduce(const RqrArgs& a, int j, int jend, RSmem& S) {
+template <int BN>
+__device__ void col_reduce(const RqrArgs& a, int j, int jend, RSmem<BN>& S) {
   const int G = gridDim.x, par = j & 1;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nc = jend - j - 1;
@@ -246,10 +257,26 @@ __device__ void col_reduce(const RqrArgs& a, int j, int jend, RSmem& S) {
   }
   if (w > nc) return;
   const double* cp = a.scr + (size_t)par * G * rq_colw();
+  // every partial of this slot loaded at once (one L2 round trip), then the common scale
+  long long ev[kQrPartsPerLane];
+  double xv[kQrPartsPerLane], yv[kQrPartsPerLane];
+#pragma unroll
+  for (int u = 0; u < kQrPartsPerLane; ++u) {
+    const int q = lane + 32 * u;
+    ev[u] = kNoScale;
+    xv[u] = yv[u] = 0.0;
+    if (q < G) {
+      const double* c = cp + (size_t)q * rq_colw();
+      ev[u] = reinterpret_cast<const long long*>(c)[0];
+      xv[u] = c[w == 0 ? 1 : 2 * w];
+      if (w) yv[u] = c[2 * w + 1];
+    }
+  }
   int emax = kNoScale;
   bool scaled = false;
-  for (int q = lane; q < G; q += 32) {
-    const int e = (int)cp[(size_t)q * rq_colw()];
+#pragma unroll
+  for (int u = 0; u < kQrPartsPerLane; ++u) {
+    const int e = (int)ev[u];
     emax = e > emax ? e : emax;
     scaled = scaled || (e != 0 && e != kNoScale);
   }
@@ -261,15 +288,15 @@ __device__ void col_reduce(const RqrArgs& a, int j, int jend, RSmem& S) {
   scaled = __any_sync(0xffffffffu, scaled);
   const int E = (emax == kNoScale) ? 0 : emax;
   double2 s = make_double2(0.0, 0.0);
-  for (int q = lane; q < G; q += 32) {
-    const double* c = cp + (size_t)q * rq_colw();
-    const int e = (int)c[0];
+#pragma unroll
+  for (int u = 0; u < kQrPartsPerLane; ++u) {
+    const int e = (int)ev[u];
     if (e == kNoScale) continue;
     if (w == 0) {
-      s.x += scaled ? qldexp(c[1], 2 * (e - E)) : c[1];
+      s.x += scaled ? qldexp(xv[u], 2 * (e - E)) : xv[u];
     } else {
-      s.x += scaled ? qldexp(c[2 * w], e - E) : c[2 * w];
-      s.y += scaled ? qldexp(c[2 * w + 1], e - E) : c[2 * w + 1];
+      s.x += scaled ? qldexp(xv[u], e - E) : xv[u];
+      s.y += scaled ? qldexp(yv[u], e - E) : yv[u];
     }
   }
 #pragma unroll
@@ -289,9 +316,10 @@ __device__ void col_reduce(const RqrArgs& a, int j, int jend, RSmem& S) {
 
 // Panel block partials: P[k][c] = sum over my rows i >= j0 of conj(V(i,k)) X(i, c) with
 // X = [V | M[:, c0:]] (the factorisation, with_gram) or X = M[:, c0:] (the Q formation).
+template <int BN>
 __device__ void panel_partials(const RqrArgs& a, const Rows& R, int j0, int nbp, int c0, int nct, bool with_gram) {
   const int G = gridDim.x, b = blockIdx.x;
-  double* pp = a.scr + rq_off_pp(G) + (size_t)b * 2 * QPW;
+  double* pp = a.scr + rq_off_pp(G) + (size_t)b * 2 * qpw<BN>();
   const int ng = with_gram ? nbp : 0;
   const int ncx = ng + nct;
   const long long lo = R.r0 > j0 ? R.r0 : j0;
@@ -314,17 +342,18 @@ __device__ void panel_partials(const RqrArgs& a, const Rows& R, int j0, int nbp,
 
 // every CTA sums a slice of the panel block entries over the G partials (one warp per
 // entry), then, after a grid barrier, every CTA loads the whole block into S.P
-__device__ void panel_reduce(const RqrArgs& a, int nbp, int ncx, RSmem& S) {
+template <int BN>
+__device__ void panel_reduce(const RqrArgs& a, int nbp, int ncx, RSmem<BN>& S) {
   const int G = gridDim.x, b = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const double* pp = a.scr + rq_off_pp(G);
-  double* pr = a.scr + rq_off_pr(G);
+  double* pr = a.scr + rq_off_pr<BN>(G);
   const int total = nbp * ncx;
   for (int e = b + G * warp; e < total; e += G * QW) {
     double sx = 0.0, sy = 0.0;
     for (int q = lane; q < G; q += 32) {
-      sx += pp[(size_t)q * 2 * QPW + 2 * e];
-      sy += pp[(size_t)q * 2 * QPW + 2 * e + 1];
+      sx += pp[(size_t)q * 2 * qpw<BN>() + 2 * e];
+      sy += pp[(size_t)q * 2 * qpw<BN>() + 2 * e + 1];
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -343,7 +372,8 @@ __device__ void panel_reduce(const RqrArgs& a, int nbp, int ncx, RSmem& S) {
 
 // T of panel p from its Gram matrix S.P[:, 0:nbp] and the taus (zlarft forward,
 // column-wise): T(i,i) = tau_i, T(0:i, i) = -tau_i T(0:i, 0:i) G(0:i, i); one warp
-__device__ void form_t(int p, int j0, int nbp, RSmem& S) {
+template <int BN>
+__device__ void form_t(int p, int j0, int nbp, RSmem<BN>& S) {
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     for (int i = 0; i < nbp; ++i) {
@@ -368,9 +398,14 @@ __device__ void form_t(int p, int j0, int nbp, RSmem& S) {
   __syncthreads();
 }
 
+// bytes of RSmem<BN>, rounded up to 256: the rows start there
+template <int BN> __host__ __device__ constexpr size_t rsmem_bytes() { return (sizeof(RSmem<BN>) + 255) / 256 * 256; }
+
+template <int BN>
 __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
-  __shared__ RSmem S;
-  extern __shared__ __align__(16) double2 q_rows[];
+  extern __shared__ __align__(256) unsigned char q_dyn[];
+  RSmem<BN>& S = *reinterpret_cast<RSmem<BN>*>(q_dyn);
+  double2* q_rows = reinterpret_cast<double2*>(q_dyn + rsmem_bytes<BN>());
   const int G = gridDim.x, b = blockIdx.x, n = a.n;
   const long long m = a.m;
   Rows R{q_rows, b * m / G, (b + 1) * m / G, n | 1};
@@ -392,7 +427,7 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
       pc.mark(0);
       if (pc.acc) pc.acc[8] += 1;
       const int nc = jend - j - 1;
-      col_reduce(a, j, jend, S);
+      col_reduce<BN>(a, j, jend, S);
       __syncthreads();
       pc.mark(1);
       if (threadIdx.x == 0) {
@@ -507,16 +542,16 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
       const long long i = j0 + aa;
       if (aa < nbp && k < nbp && i >= R.r0 && i < R.r1) {
         const double2 v = R.v(i, j0, k);
-        double* vt = a.scr + rq_off_vt(G) + (size_t)p * 2 * QNB * QNB;
+        double* vt = a.scr + rq_off_vt<BN>(G) + (size_t)p * 2 * QNB * QNB;
         vt[2 * (aa * QNB + k)] = v.x;
         vt[2 * (aa * QNB + k) + 1] = v.y;
       }
     }
     const int nct = n - jend;
-    panel_partials(a, R, j0, nbp, jend, nct, true);
+    panel_partials<BN>(a, R, j0, nbp, jend, nct, true);
     grid_barrier(a.bar, a.err);
-    panel_reduce(a, nbp, nbp + nct, S);
-    form_t(p, j0, nbp, S);
+    panel_reduce<BN>(a, nbp, nbp + nct, S);
+    form_t<BN>(p, j0, nbp, S);
     if (nct > 0) {
       // W = T^H (V^H M_trailing)
       for (int e = threadIdx.x; e < nbp * nct; e += QT) {
@@ -555,9 +590,9 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
     const int nct = n - jend;
     const long long lo = R.r0 > j0 ? R.r0 : j0;
     if (nct > 0) {
-      panel_partials(a, R, j0, nbp, jend, nct, false);
+      panel_partials<BN>(a, R, j0, nbp, jend, nct, false);
       grid_barrier(a.bar, a.err);
-      panel_reduce(a, nbp, nct, S);
+      panel_reduce<BN>(a, nbp, nct, S);
       // W = T (V^H Q_trailing); Q_trailing -= V W
       for (int e = threadIdx.x; e < nbp * nct; e += QT) {
         const int k = e / nct, c = e % nct;
@@ -577,7 +612,7 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
     }
     // panel columns: Q[:, j0 + k] = e_{j0+k} - V W2, W2 = T V_top^H
     {
-      const double* vt = a.scr + rq_off_vt(G) + (size_t)p * 2 * QNB * QNB;
+      const double* vt = a.scr + rq_off_vt<BN>(G) + (size_t)p * 2 * QNB * QNB;
       for (int e = threadIdx.x; e < nbp * nbp; e += QT) {
         const int aa = e / nbp, k = e % nbp;
         double2 s = make_double2(0.0, 0.0);
@@ -609,30 +644,76 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
   grid_barrier_end(a.bar);
 }
 
-size_t rows_smem(int rows, int n) { return (size_t)rows * (size_t)(n | 1) * sizeof(double2); }
+template <int BN> size_t rows_smem(int rows, int n) { return rsmem_bytes<BN>() + (size_t)rows * (size_t)(n | 1) * sizeof(double2); }
 
-}  // namespace
+// opt-in shared memory per block of the current device (the same for every GB300; looked
+// up once)
+int max_dyn_smem() {
+  static int v = -1;
+  if (v < 0) {
+    int dev = 0, x = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&x, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    v = x;
+  }
+  return v;
+}
 
-size_t qr_rows_scratch_bytes(int max_grid) { return rq_doubles(max_grid) * sizeof(double); }
+// dynamic shared memory an instantiation may take: the opt-in limit less its static
+// shared memory (the grid barrier's slot), which counts against the same limit
+template <int BN> int dyn_limit() {
+  static int v = -1;
+  if (v < 0) {
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, k_qr_rows<BN>);
+    v = max_dyn_smem() - (int)fa.sharedSizeBytes;
+  }
+  return v;
+}
 
-int qr_rows_max_grid() {
+template <int BN> int rows_cap(int n) {
+  const long long avail = (long long)dyn_limit<BN>() - (long long)rsmem_bytes<BN>();
+  long long r = avail > 0 ? avail / ((long long)(n | 1) * (long long)sizeof(double2)) : 0;
+  if (r > kQrRowsMax) r = kQrRowsMax;
+  return (int)r;
+}
+
+template <int BN> int max_grid_bn() {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int dyn = (int)rows_smem(kQrRowsMax, kQrMaxCols);
-  cudaFuncSetAttribute(k_qr_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_qr_rows, QT, dyn);
+  // every launch stays within the opt-in limit (rows_cap), whatever its width
+  const int dyn = dyn_limit<BN>();
+  cudaFuncSetAttribute(k_qr_rows<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_qr_rows<BN>, QT, dyn);
   return sms * (per < 1 ? 1 : per);
+}
+
+}  // namespace
+
+size_t qr_rows_scratch_bytes(int max_grid) { return rq_doubles<kMaxBond>(max_grid) * sizeof(double); }
+
+int qr_rows_max_rows(int n) { return n <= kQrMaxCols ? rows_cap<kQrMaxCols>(n) : rows_cap<kMaxBond>(n); }
+
+int qr_rows_max_grid() {
+  const int a = max_grid_bn<kQrMaxCols>(), b = max_grid_bn<kMaxBond>();
+  return a < b ? a : b;
 }
 
 cudaError_t householder_qr_rows(double2* M, long long m, int n, double2* R, int Rt, double2* tau_ws, double* scratch,
                                 GridBarrier* bar, int* err, int grid, cudaStream_t s, unsigned long long* phase) {
-  if (n < 1 || n > kQrMaxCols || m < n || grid < 1 || (m + grid - 1) / grid > kQrRowsMax) return cudaErrorInvalidValue;
+  if (n < 1 || n > kMaxBond || m < n || grid < 1 || grid > 32 * kQrPartsPerLane ||
+      (m + grid - 1) / grid > qr_rows_max_rows(n))
+    return cudaErrorInvalidValue;
   RqrArgs a{M, m, n, R, Rt, tau_ws, scratch, bar, err, phase};
   void* args[] = {&a};
   ++g_launches;
   const int rows = (int)((m + grid - 1) / grid);
-  return cudaLaunchCooperativeKernel((const void*)k_qr_rows, dim3(grid), dim3(QT), args, rows_smem(rows, n), s);
+  if (n <= kQrMaxCols)
+    return cudaLaunchCooperativeKernel((const void*)k_qr_rows<kQrMaxCols>, dim3(grid), dim3(QT), args,
+                                       rows_smem<kQrMaxCols>(rows, n), s);
+  return cudaLaunchCooperativeKernel((const void*)k_qr_rows<kMaxBond>, dim3(grid), dim3(QT), args,
+                                     rows_smem<kMaxBond>(rows, n), s);
 }
 
 }  // namespace ttn

@@ -180,6 +180,10 @@ void check_finite(const double2* x, long long n, int* status, int code, cudaStre
 double measure_fp64_fma_tflops() { return 1.0; }
 cudaError_t tc_gemm_test(const double*, const double*, double*, int, int, int*, cudaStream_t) { return cudaSuccess; }
 int expm_coop_max_grid(int) { return 1; }
+// resident vectors are a placement inside the device kernel; the double computes the same
+// values from the global buffers
+size_t expm_smem_vecs_bytes(int m, long long ldt) { return 8192 + (size_t)(m + 5) * (size_t)ldt * 16; }
+size_t expm_smem_vecs_max_bytes() { return 227 * 1024 - 16384; }
 size_t expm_partial_bytes(int g) { return (size_t)(2 * g + 1) * 64 * 16; }
 
 static void apply_prog(const ExpmArgs& a, const double2* x, double2* out) {

@@ -683,6 +683,25 @@ __device__ void reduce_partials(const double2* part, int nq, double2* out, Red& 
   __syncthreads();
 }
 
+// sums over the whole launch of the nq per-warp values in sm.w into out (every CTA): for one
+// CTA straight from shared memory (the same order as the two-pass form, which adds only
+// zeros past the first partial), else through the partials and a grid barrier
+__device__ void launch_sum(const ExpmArgs& a, Red& sm, int nq, double2* part, double2* out) {
+  if (gridDim.x == 1) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+      double2 s = make_double2(0.0, 0.0);
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = cadd(s, sm.w[w][q]);
+      out[q] = s;
+    }
+    __syncthreads();
+    return;
+  }
+  store_partials(sm, nq, part);
+  grid_barrier(a.bar, a.err);
+  reduce_partials(part, nq, out, sm);
+}
+
 // The small exponential of the step control, F = exp(zc * Haug) e1, by one warp.
 // Haug is the Lanczos tridiagonal (d on the diagonal, e[i] coupling rows i-1 and i) of
 // size mb, bordered when aug is set by row mb = betm at column mb-1 and row mb+1 = 1 at
@@ -702,6 +721,7 @@ struct CtlSmem {
   double2 t[2][EQ + 2];
   double w[2][EQ + 2];
 };
+constexpr size_t kCtlBytes = (sizeof(CtlSmem) + 255) / 256 * 256;  // where resident vectors start
 constexpr int kMaxScaling = 4096;   // ||zc Haug||_inf above this fails the step (error bit 4)
 constexpr int kMaxTaylor = 34;
 __constant__ unsigned char kTaylorK[32] = {10, 12, 14, 15, 16, 17, 18, 19, 19, 20, 21, 22, 23, 23, 24, 25,
@@ -727,6 +747,60 @@ __device__ __forceinline__ double haug_row(int i, int mb, double betm, const dou
 __device__ bool warp_expm_e1(int mb, bool aug, double betm, double2 zc, CtlSmem& S) {
   const int lane = threadIdx.x & 31;
   const int mx = mb + (aug ? 2 : 0);
+  if (mx <= 32 && (zc.x == 0.0 || zc.y == 0.0)) {
+    // The usual case, one segment (||zc Haug||_inf <= 4) of real arithmetic, in registers:
+    // lane i holds row i of Haug as (diagonal, coupling to row i-1, coupling to row i+1)
+    // and the current term; the neighbours' terms come by shuffles and the coefficients
+    // ck d_i, ck e_i, ck e_{i+1} are formed off the chain, so one Taylor term costs three
+    // dependent FP64 operations.  The row-sum maximum is taken on the bit patterns (the
+    // sums are non-negative) and |zc| without a hypot.
+    double di = 0.0, em = 0.0, ep = 0.0, rs = 0.0;
+    if (lane < mb) {
+      di = S.d[lane];
+      em = lane > 0 ? S.e[lane] : 0.0;
+      ep = lane + 1 < mb ? S.e[lane + 1] : 0.0;
+      rs = fabs(di) + fabs(em) + fabs(ep);
+    } else if (lane == mb && aug) {
+      em = betm;
+      rs = fabs(betm);
+    } else if (lane == mb + 1 && aug) {
+      em = 1.0;
+      rs = 1.0;
+    }
+    long long rb = __double_as_longlong(rs);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long t = __shfl_xor_sync(0xffffffffu, rb, o);
+      rb = t > rb ? t : rb;
+    }
+    const bool real_z = (zc.y == 0.0), imag_z = (zc.x == 0.0);
+    const double az = real_z ? fabs(zc.x) : fabs(zc.y);
+    const double nrm = __longlong_as_double(rb) * az;
+    if (nrm <= 4.0) {
+      int kb = (int)ceil(nrm * 8.0) - 1;
+      kb = kb < 0 ? 0 : (kb > 31 ? 31 : kb);
+      const int K = kTaylorK[kb];
+      const double sg = real_z ? (zc.x < 0.0 ? -1.0 : 1.0) : (zc.y < 0.0 ? -1.0 : 1.0);
+      double t = lane == 0 ? 1.0 : 0.0, x0 = t, x1 = 0.0;
+      for (int k = 1; k <= K; ++k) {
+        const double ck = az * kInvK[k];
+        const double cd = ck * di, ce = ck * em, cp = ck * ep;
+        const double tm = __shfl_up_sync(0xffffffffu, t, 1);
+        const double tp = __shfl_down_sync(0xffffffffu, t, 1);
+        const double tn = fma(cp, tp, fma(ce, tm, cd * t));
+        // u^k: real_z: sg^k; imag_z: sg^k i^k
+        const bool odd = (k & 1) != 0;
+        double sk = odd ? sg : 1.0;
+        if (imag_z && (k & 3) >= 2) sk = -sk;
+        if (imag_z && odd) x1 = fma(sk, tn, x1);
+        else x0 = fma(sk, tn, x0);
+        t = tn;
+      }
+      if (lane < mx) S.x[lane] = make_double2(x0, x1);
+      __syncwarp();
+      return true;
+    }
+  }
   double rn = 0.0;
   for (int i = lane; i < mx; i += 32) {
     double r;
@@ -811,6 +885,8 @@ __device__ bool warp_expm_e1(int mb, bool aug, double betm, double2 zc, CtlSmem&
 // the recurrence at dimension jj (as an exact breakdown does) when
 // beta_0 beta_jj |e_{jj-1}^T exp(c tau T_jj) e_1| <= tol for the remaining interval tau.
 // Kept out of line so that the registers of the Lanczos loop do not grow.
+// The final test compares squares unless they lie within 1e-12 of the threshold, where it
+// falls back to the product with the modulus (a hypot costs about 700 cycles of one warp).
 __device__ __noinline__ void residual_stop(KrylovCtl* ctl, int jj, int m, double beta, CtlSmem& S) {
   const int lane = threadIdx.x & 31;
   for (int i = lane; i < jj; i += 32) {
@@ -823,7 +899,14 @@ __device__ __noinline__ void residual_stop(KrylovCtl* ctl, int jj, int m, double
   const bool ok = warp_expm_e1(jj, false, 0.0, zc, S);
   if (lane == 0 && ok && ctl->mb == m) {
     const double2 last = S.x[jj - 1];
-    if (ctl->beta * beta * hypot(last.x, last.y) <= ctl->tol) {
+    const double f = ctl->beta * beta, tol = ctl->tol;
+    const double l2 = f * f * fma(last.x, last.x, last.y * last.y), t2 = tol * tol;
+    bool stop;
+    if (l2 > 1e-290 && l2 < 1e290 && t2 > 1e-290 && t2 < 1e290 && fabs(l2 - t2) > 1e-12 * t2)
+      stop = l2 < t2;
+    else
+      stop = f * hypot(last.x, last.y) <= tol;
+    if (stop) {
       ctl->mb = jj;
       ctl->k1 = 0;
     }
@@ -907,23 +990,29 @@ __device__ void control(const ExpmArgs& a, CtlSmem& S) {
     if (s_accept || s_fail) break;
     ++ireject;
   }
+  const double t_step = s_tstep, err_loc = s_err, xm = s_xm;
+  const bool good = !s_fail && isfinite(t_step) && t_step > 0.0 && isfinite(err_loc);
+  if (good) {
+    // the combination coefficients, one per lane
+    const int mx = mb + (k1 > 1 ? k1 - 1 : 0);
+    for (int q = lane; q < 72; q += 32) {
+      const double2 c = (q < mx) ? cscale(beta, S.x[q]) : make_double2(0.0, 0.0);
+      ctl->coef[2 * q] = c.x;
+      ctl->coef[2 * q + 1] = c.y;
+    }
+  }
   if (lane == 0) {
-    const double t_step = s_tstep, err_loc = s_err, xm = s_xm;
     if (s_fail) {
       ctl->err |= 1;
       ctl->done = 1;
-    } else if (!isfinite(t_step) || !(t_step > 0.0) || !isfinite(err_loc)) {
+    } else if (!good) {
       ctl->err |= 8;
       ctl->done = 1;
     } else {
-      const int mx = mb + (k1 > 1 ? k1 - 1 : 0);
-      for (int q = 0; q < 72; ++q) {
-        double2 c = (q < mx) ? cscale(beta, S.x[q]) : make_double2(0.0, 0.0);
-        ctl->coef[2 * q] = c.x;
-        ctl->coef[2 * q + 1] = c.y;
-      }
-      ctl->t_now += t_step;
-      if (k1 != 0) {
+      const double t_now = ctl->t_now + t_step;
+      ctl->t_now = t_now;
+      // the next sub-step's size; none follows the last one
+      if (k1 != 0 && !(t_now >= ctl->t_out)) {
         double tn = gamma * t_step * pow(t_step * tol / fmax(err_loc, 1e-300), xm);
         double sc = pow(10.0, floor(log10(tn)) - 1.0);
         ctl->t_new = ceil(tn / sc) * sc;
@@ -931,12 +1020,16 @@ __device__ void control(const ExpmArgs& a, CtlSmem& S) {
       }
       ctl->napps += mb + (k1 != 0 ? 1 : 0);
       ctl->substeps += 1;
-      if (ctl->t_now >= ctl->t_out) ctl->done = 1;
+      if (t_now >= ctl->t_out) ctl->done = 1;
     }
   }
   __syncwarp();
 }
 
+// SV: the one-CTA form with the vectors resident in shared memory (ExpmArgs::smem_vecs; no
+// tensor-core ops), a separate instantiation so that the general form keeps its vector
+// pointers in the parameter space
+template <bool SV>
 __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
   __shared__ Red sm;
   __shared__ double2 red[EQ];
@@ -959,7 +1052,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
   }
   TcState tcs;
   TcState* tcp = nullptr;
-  if (a.mixed) {
+  if (!SV && a.mixed) {
     if (threadIdx.x == 0) {
       tc::mbar_init(&s_mbar[0], 1);
       tc::mbar_init(&s_mbar[1], 1);
@@ -983,6 +1076,18 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
     tcs.e_n = reinterpret_cast<int*>(dsm + 2 * (TC_A_CHUNK_BYTES + TC_B_CHUNK_BYTES));
     tcp = &tcs;
     build_tc_images(a);
+  }
+  if (SV) {
+    // one CTA, small problem: the basis, p and the temporaries after the controller's
+    // scratch, so that the Lanczos passes and the matvec read shared memory, not L2
+    double2* b = reinterpret_cast<double2*>(dsm + kCtlBytes);
+    a.V = b;
+    a.ldv = a.ldt;
+    b += (size_t)(a.m + 1) * a.ldt;
+    a.p = b;
+    a.t1 = b + a.ldt;
+    a.t2 = b + 2 * a.ldt;
+    a.t3 = b + 3 * a.ldt;
   }
   KrylovCtl* ctl = a.ctl;
   const long long n = a.n;
@@ -1032,10 +1137,8 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
       }
       s = wsum(s);
       if (lane == 0) sm.w[warp][0] = make_double2(s, 0.0);
-      store_partials(sm, 1, pa);
+      launch_sum(a, sm, 1, pa, red);
     }
-    grid_barrier(a.bar, a.err);
-    reduce_partials(pa, 1, red, sm);
     {
       const double beta = sqrt(red[0].x);
       const double inv = beta > 0.0 ? 1.0 / beta : 0.0;
@@ -1077,10 +1180,8 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
         s.x = wsum(s.x);
         s.y = wsum(s.y);
         if (lane == 0) sm.w[warp][0] = s;
-        store_partials(sm, 1, pa);
+        launch_sum(a, sm, 1, pa, red);
       }
-      grid_barrier(a.bar, a.err);
-      reduce_partials(pa, 1, red, sm);
       const double alpha = red[0].x;
       const double bj = (j > 0) ? ctl->bet[j] : 0.0;
       const double2* Vm = a.V + (long long)(j > 0 ? j - 1 : 0) * a.ldv;
@@ -1108,24 +1209,39 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
           for (int u = 0; u < 4; ++u)
             if (q0 + u <= j) s[u] = cadd(s[u], cmulc(a.V[(long long)(q0 + u) * a.ldv + i], pi));
         }
+        // warp sums of the eight doubles by a transposing butterfly: at offsets 16, 8, 4
+        // each lane keeps half of its values and adds the partner's copy of that half, then
+        // two plain levels; 9 FP64 additions per lane instead of 40 (one warp's FP64
+        // instruction occupies the SM's FP64 pipe for 16 cycles on GB300).  Lane 4 v ends
+        // with double v (s[v / 2], real part when v is even).
+        {
+          double v8[8] = {s[0].x, s[0].y, s[1].x, s[1].y, s[2].x, s[2].y, s[3].x, s[3].y};
+          const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0, b2 = (lane & 4) != 0;
+          double w4[4], w2[2];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            s[u].x += __shfl_xor_sync(0xffffffffu, s[u].x, o);
-            s[u].y += __shfl_xor_sync(0xffffffffu, s[u].y, o);
+          for (int k = 0; k < 4; ++k) {
+            const double give = b4 ? v8[k] : v8[k + 4];
+            w4[k] = (b4 ? v8[k + 4] : v8[k]) + __shfl_xor_sync(0xffffffffu, give, 16);
           }
-        }
-        if (lane == 0) {
 #pragma unroll
-          for (int u = 0; u < 4; ++u)
-            if (q0 + u <= j) sm.w[warp][q0 + u] = s[u];
+          for (int k = 0; k < 2; ++k) {
+            const double give = b3 ? w4[k] : w4[k + 2];
+            w2[k] = (b3 ? w4[k + 2] : w4[k]) + __shfl_xor_sync(0xffffffffu, give, 8);
+          }
+          double w1 = (b2 ? w2[1] : w2[0]) + __shfl_xor_sync(0xffffffffu, b2 ? w2[0] : w2[1], 4);
+          w1 += __shfl_xor_sync(0xffffffffu, w1, 2);
+          w1 += __shfl_xor_sync(0xffffffffu, w1, 1);
+          const int v = lane >> 2;
+          if ((lane & 3) == 0 && q0 + (v >> 1) <= j)
+            reinterpret_cast<double*>(&sm.w[warp][q0 + (v >> 1)])[v & 1] = w1;
         }
       }
-      store_partials(sm, j + 1, pb);
       if (blockIdx.x == 0 && threadIdx.x == 0) ctl->alpha[j] = alpha;
-      grid_barrier(a.bar, a.err);
-      if (gridDim.x >= kSliceReduceGrid) {
+      if (gridDim.x == 1) {
+        launch_sum(a, sm, j + 1, pb, red);
+      } else if (gridDim.x >= kSliceReduceGrid) {
+        store_partials(sm, j + 1, pb);
+        grid_barrier(a.bar, a.err);
         // CTA q < j + 1 reduces coefficient q over all partials (same order as
         // reduce_partials), then everyone reads the j + 1 results: one more barrier instead
         // of every CTA summing (j + 1) x grid partials in FP64
@@ -1141,7 +1257,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
         for (int q = threadIdx.x; q <= j; q += blockDim.x) red[q] = rq[q];
         __syncthreads();
       } else {
-        reduce_partials(pb, j + 1, red, sm);
+        launch_sum(a, sm, j + 1, pb, red);
       }
       pc.mark(3);
       {
@@ -1161,10 +1277,8 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
         }
         s = wsum(s);
         if (lane == 0) sm.w[warp][0] = make_double2(s, 0.0);
-        store_partials(sm, 1, pa);
+        launch_sum(a, sm, 1, pa, red);
       }
-      grid_barrier(a.bar, a.err);
-      reduce_partials(pa, 1, red, sm);
       {
         const double beta = sqrt(red[0].x);
         // max over the rows q <= j of |alpha_q| + beta_q + beta_{q+1}: the rows below j were
@@ -1252,7 +1366,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
     }
     pc.mark(7);
   }
-  if (a.mixed) {
+  if (!SV && a.mixed) {
     tc::fence_before();
     __syncthreads();
     if ((threadIdx.x >> 5) == 0) {
@@ -1273,12 +1387,31 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
 
 static size_t dyn_smem(int mixed) { return mixed ? (TC_SMEM > sizeof(CtlSmem) ? TC_SMEM : sizeof(CtlSmem)) : sizeof(CtlSmem); }
 
+size_t expm_smem_vecs_bytes(int m, long long ldt) { return kCtlBytes + (size_t)(m + 5) * (size_t)ldt * sizeof(double2); }
+
+// the opt-in shared memory per block less the kernel's static shared memory (the same for
+// every GB300; looked up once)
+size_t expm_smem_vecs_max_bytes() {
+  static long long v = -1;
+  if (v < 0) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, k_expm_coop<true>);
+    v = (long long)optin - (long long)fa.sharedSizeBytes;
+    if (v < 0) v = 0;
+  }
+  return (size_t)v;
+}
+
 int expm_coop_max_grid(int mixed) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaFuncSetAttribute(k_expm_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem(1));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expm_coop, ET, dyn_smem(mixed));
+  cudaFuncSetAttribute(k_expm_coop<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem(1));
+  cudaFuncSetAttribute(k_expm_coop<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)expm_smem_vecs_max_bytes());
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expm_coop<false>, ET, dyn_smem(mixed));
   return sms * (per < 1 ? 1 : per);
 }
 
@@ -1288,9 +1421,16 @@ size_t expm_partial_bytes(int max_grid) { return (size_t)(2 * max_grid + 1) * EQ
 cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s, int threads) {
   if (threads <= 0 || threads > ET || (threads & 31) || a.mixed) threads = ET;  // tensor-core ops need ET
   ExpmArgs b = a;
+  size_t dyn = dyn_smem(a.mixed);
+  if (a.smem_vecs) {
+    if (grid != 1 || a.mixed || a.apply_only || a.ldt < a.n || expm_smem_vecs_bytes(a.m, a.ldt) > expm_smem_vecs_max_bytes())
+      return cudaErrorInvalidValue;
+    dyn = expm_smem_vecs_bytes(a.m, a.ldt);
+  }
   void* args[] = {&b};
   ++g_launches;
-  return cudaLaunchCooperativeKernel((const void*)k_expm_coop, dim3(grid), dim3(threads), args, dyn_smem(a.mixed), s);
+  return cudaLaunchCooperativeKernel(a.smem_vecs ? (const void*)k_expm_coop<true> : (const void*)k_expm_coop<false>,
+                                     dim3(grid), dim3(threads), args, dyn, s);
 }
 
 }  // namespace ttn

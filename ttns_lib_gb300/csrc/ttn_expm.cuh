@@ -64,6 +64,10 @@ struct ExpmArgs {
                          // Lanczos passes assume)
   int tpo;               // lanes per output element of the element-wise program ops (1, 2, 4
                          // or 8; above 1 the program needs tail_barrier)
+  int smem_vecs;         // 1 (one-CTA launches of small problems): the basis V, p and the
+                         // temporaries live in the launch's shared memory, ldt elements
+                         // each, instead of at V / p / t1..t3
+  long long ldt;
 };
 constexpr int kPhases = 16;  // begin, matvec, alpha, reorth coefficients, reorth + norm,
                              // ||H V_m||, control, combine, sub-steps, launches; then inside
@@ -75,6 +79,10 @@ int expm_coop_max_grid(int mixed);
 size_t expm_partial_bytes(int max_grid);
 // threads per CTA: a multiple of 32 up to 256 (tensor-core programs always use 256)
 cudaError_t expm_coop(const ExpmArgs& a, int grid, cudaStream_t s, int threads = 256);
+// shared memory of a one-CTA launch with the vectors resident (smem_vecs): m + 5 vectors of
+// ldt elements after the controller's scratch; and the most a launch may take
+size_t expm_smem_vecs_bytes(int m, long long ldt);
+size_t expm_smem_vecs_max_bytes();
 // whether a contraction can run on the tensor cores
 // Tensor-core contractions need rank-64 operands and enough 64-column tiles to occupy the
 // device; smaller ones run faster as element-wise FP64 contractions.

@@ -462,6 +462,7 @@ struct Integrator {
   // compiled matrix-vector programs for the persistent Krylov kernel
   DevBuf prog_buf, expm_part_buf;
   std::vector<int> heff_off, heff_n, kbond_off, kbond_n;
+  std::vector<long long> heff_ext, kbond_ext;  // most elements any op of the program reads or writes
   long long* nh_dev = nullptr;
   double* flops_dev = nullptr;   // matvec flops executed by the persistent kernels
   // host mirrors
@@ -721,6 +722,7 @@ struct Integrator {
       if (const char* e = std::getenv("TTN_EXPM_ELEMS_PER_CTA")) expm_elems_per_cta = std::max(1, std::atoi(e));
       if (const char* e = std::getenv("TTN_EXPM_TPO")) expm_tpo_max = std::max(1, std::min(8, std::atoi(e)));
       if (const char* e = std::getenv("TTN_EXPM_TPO_MIN_FLOPS")) expm_tpo_min_flops = std::atof(e);
+      if (const char* e = std::getenv("TTN_EXPM_SMEM_VECS")) expm_smem_vecs = std::atoi(e) != 0;
       if (const char* e = std::getenv("TTN_QR_ROWS_PER_CTA")) qr_rows_per_cta = std::max(1, std::atoi(e));
       if (const char* e = std::getenv("TTN_EXPM_ELEMS_PER_THREAD")) expm_elems_per_thread = std::max(0.1, std::atof(e));
       expm_max_grid = std::max(1, expm_coop_max_grid(0));
@@ -1202,7 +1204,18 @@ struct Integrator {
     heff_off.assign(T.n, 0); heff_n.assign(T.n, 0); kbond_off.assign(T.n, 0); kbond_n.assign(T.n, 0);
     heff_tc.assign(T.n, 0); kbond_tc.assign(T.n, 0);
     heff_tail.assign(T.n, 0); kbond_tail.assign(T.n, 0);
+    heff_ext.assign(T.n, 0); kbond_ext.assign(T.n, 0);
     max_tc_images = 0;
+    auto extent = [](const std::vector<MvOp>& ops) {
+      long long e = 0;
+      for (const auto& o : ops) {
+        long long t = o.na;
+        if (o.kind == MV_MODE || o.kind == MV_CSR) t = o.na * o.d * o.nb;
+        else if (o.kind == MV_MF) t = o.na * o.d;
+        e = std::max(e, t);
+      }
+      return e;
+    };
     // a tensor-core op wrote the result buffer (1) after the program's last barrier
     auto tail_needed = [](const std::vector<MvOp>& ops) {
       bool pending = false;
@@ -1222,11 +1235,13 @@ struct Integrator {
       auto h = heff_program(i);
       heff_tc[i] = mark(h);
       heff_tail[i] = tail_needed(h);
+      heff_ext[i] = extent(h);
       heff_off[i] = (int)all.size(); heff_n[i] = (int)h.size();
       all.insert(all.end(), h.begin(), h.end());
       auto k = kbond_program(i);
       kbond_tc[i] = mark(k);
       kbond_tail[i] = tail_needed(k);
+      kbond_ext[i] = extent(k);
       kbond_off[i] = (int)all.size(); kbond_n[i] = (int)k.size();
       all.insert(all.end(), k.begin(), k.end());
     }
@@ -1242,6 +1257,7 @@ struct Integrator {
   long long expm_elems_per_cta = 64;  // at least this many vector elements per CTA
   int expm_tpo_max = 8;               // most lanes per output element of the element-wise ops
   double expm_tpo_min_flops = 2000.0; // matvec flops per vector element from which they are split
+  bool expm_smem_vecs = true;         // one-CTA launches with the vectors in shared memory
   // threads per CTA: about expm_elems_per_thread vector elements per thread, 64..256 (the
   // FP64 warp reductions cost the same per warp whatever the data, so tiny problems run on
   // fewer warps)
@@ -1297,6 +1313,15 @@ struct Integrator {
         a.tpo = tpo;
         a.tail_barrier = 1;
         threads = (int)std::min<long long>(256, ((n * tpo + grid - 1) / grid + 31) / 32 * 32);
+      }
+    }
+    // one-CTA launches keep their vectors in shared memory when they fit
+    if (grid == 1 && expm_smem_vecs && !a.mixed && !apply_only) {
+      const long long ext = kind == 0 ? heff_ext[nd] : kbond_ext[nd];
+      const long long ldt = (std::max(ext, n) + 1) / 2 * 2;
+      if (expm_smem_vecs_bytes(a.m, ldt) <= expm_smem_vecs_max_bytes()) {
+        a.smem_vecs = 1;
+        a.ldt = ldt;
       }
     }
     CK(expm_coop(a, grid, stream, threads));

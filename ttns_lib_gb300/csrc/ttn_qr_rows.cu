@@ -185,8 +185,10 @@ struct Rows {
 };
 
 // Partials of column j (panel columns up to jend) over my rows, published by warp w for
-// slot w; the row j entries by the CTA that holds row j.
-__device__ void col_partials(const RqrArgs& a, const Rows& R, int j, int jend) {
+// slot w; the row j entries by the CTA that holds row j.  A one-CTA launch writes the sums
+// straight into S (what col_reduce would make of a single partial).
+template <int BN>
+__device__ void col_partials(const RqrArgs& a, const Rows& R, int j, int jend, RSmem<BN>& S) {
   const int G = gridDim.x, b = blockIdx.x, par = j & 1;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nc = jend - j - 1;
@@ -226,7 +228,14 @@ __device__ void col_partials(const RqrArgs& a, const Rows& R, int j, int jend) {
       if (w) acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
     }
     if (lane == 0) {
-      if (w == 0) {
+      if (G == 1) {
+        if (w == 0) {
+          S.nrm2 = acc.x;
+          S.E = lmax > 0.0 ? e : 0;
+        } else {
+          S.g[w] = acc;
+        }
+      } else if (w == 0) {
         reinterpret_cast<long long*>(cp)[0] = (long long)(lmax > 0.0 ? e : kNoScale);
         cp[1] = acc.x;
       } else {
@@ -236,10 +245,14 @@ __device__ void col_partials(const RqrArgs& a, const Rows& R, int j, int jend) {
     }
   }
   if (j >= R.r0 && j < R.r1 && w == QW - 1 && lane <= nc) {
-    double* rj = a.scr + rq_off_rowj(G) + (size_t)par * 2 * QNB;
     const double2 v = R.at(j, j + lane);
-    rj[2 * lane] = v.x;
-    rj[2 * lane + 1] = v.y;
+    if (G == 1) {
+      S.rowj[lane] = v;
+    } else {
+      double* rj = a.scr + rq_off_rowj(G) + (size_t)par * 2 * QNB;
+      rj[2 * lane] = v.x;
+      rj[2 * lane + 1] = v.y;
+    }
   }
 }
 
@@ -249,6 +262,7 @@ __device__ void col_reduce(const RqrArgs& a, int j, int jend, RSmem<BN>& S) {
   const int G = gridDim.x, par = j & 1;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nc = jend - j - 1;
+  if (G == 1) return;  // col_partials wrote S
   // row j of the panel (alpha and the entries the w_c need), loaded by the last warp while
   // the others load the partials
   if (w == QW - 1 && lane <= nc) {
@@ -314,10 +328,14 @@ __device__ void col_reduce(const RqrArgs& a, int j, int jend, RSmem<BN>& S) {
   }
 }
 
+template <int BN>
+__device__ void panel_reduce(const RqrArgs& a, int nbp, int ncx, RSmem<BN>& S);
+
 // Panel block partials: P[k][c] = sum over my rows i >= j0 of conj(V(i,k)) X(i, c) with
 // X = [V | M[:, c0:]] (the factorisation, with_gram) or X = M[:, c0:] (the Q formation).
 template <int BN>
-__device__ void panel_partials(const RqrArgs& a, const Rows& R, int j0, int nbp, int c0, int nct, bool with_gram) {
+__device__ void panel_partials(const RqrArgs& a, const Rows& R, int j0, int nbp, int c0, int nct, bool with_gram,
+                               RSmem<BN>& S) {
   const int G = gridDim.x, b = blockIdx.x;
   double* pp = a.scr + rq_off_pp(G) + (size_t)b * 2 * qpw<BN>();
   const int ng = with_gram ? nbp : 0;
@@ -335,9 +353,24 @@ __device__ void panel_partials(const RqrArgs& a, const Rows& R, int j0, int nbp,
     }
     if (i < R.r1) s0 = qfmac(s0, R.v(i, j0, k), c < ng ? R.v(i, j0, c) : R.at(i, c0 + c - ng));
     const double2 s = qadd(s0, s1);
-    pp[2 * e] = s.x;
-    pp[2 * e + 1] = s.y;
+    if (G == 1) {
+      S.P[k][c] = s;  // a single partial is the sum
+    } else {
+      pp[2 * e] = s.x;
+      pp[2 * e + 1] = s.y;
+    }
   }
+}
+
+// the panel block sums in S.P: one CTA has them already, several reduce their partials
+template <int BN>
+__device__ void panel_sums(const RqrArgs& a, int nbp, int ncx, RSmem<BN>& S) {
+  if (gridDim.x == 1) {
+    __syncthreads();
+    return;
+  }
+  grid_barrier(a.bar, a.err);
+  panel_reduce<BN>(a, nbp, ncx, S);
 }
 
 // every CTA sums a slice of the panel block entries over the G partials (one warp per
@@ -417,7 +450,7 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
   grid_barrier_begin(a.bar);
   for (int e = threadIdx.x; e < nr * n; e += QT) R.p[(e / n) * R.lds + e % n] = a.M[(R.r0 + e / n) * n + e % n];
   __syncthreads();
-  col_partials(a, R, 0, n < QNB ? n : QNB);
+  col_partials<BN>(a, R, 0, n < QNB ? n : QNB, S);
   // ------------------------------------------------------------------ factorisation
   for (int p = 0; p < npan; ++p) {
     const int j0 = p * QNB, nbp = (n - j0) < QNB ? (n - j0) : QNB, jend = j0 + nbp;
@@ -533,7 +566,7 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
       }
       __syncthreads();
       pc.mark(4);
-      if (j + 1 < jend) col_partials(a, R, j + 1, jend);
+      if (j + 1 < jend) col_partials<BN>(a, R, j + 1, jend, S);
       pc.mark(5);
     }
     // ---- panel done: V top block for the Q formation, Gram and projections, T, update
@@ -548,9 +581,8 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
       }
     }
     const int nct = n - jend;
-    panel_partials<BN>(a, R, j0, nbp, jend, nct, true);
-    grid_barrier(a.bar, a.err);
-    panel_reduce<BN>(a, nbp, nbp + nct, S);
+    panel_partials<BN>(a, R, j0, nbp, jend, nct, true, S);
+    panel_sums<BN>(a, nbp, nbp + nct, S);
     form_t<BN>(p, j0, nbp, S);
     if (nct > 0) {
       // W = T^H (V^H M_trailing)
@@ -570,7 +602,7 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
         R.at(i, jend + c) = x;
       }
       __syncthreads();
-      col_partials(a, R, jend, jend + ((n - jend) < QNB ? (n - jend) : QNB));
+      col_partials<BN>(a, R, jend, jend + ((n - jend) < QNB ? (n - jend) : QNB), S);
     }
   }
   pc.mark(6);
@@ -590,9 +622,8 @@ __global__ void __launch_bounds__(QT) k_qr_rows(RqrArgs a) {
     const int nct = n - jend;
     const long long lo = R.r0 > j0 ? R.r0 : j0;
     if (nct > 0) {
-      panel_partials<BN>(a, R, j0, nbp, jend, nct, false);
-      grid_barrier(a.bar, a.err);
-      panel_reduce<BN>(a, nbp, nct, S);
+      panel_partials<BN>(a, R, j0, nbp, jend, nct, false, S);
+      panel_sums<BN>(a, nbp, nct, S);
       // W = T (V^H Q_trailing); Q_trailing -= V W
       for (int e = threadIdx.x; e < nbp * nct; e += QT) {
         const int k = e / nct, c = e % nct;

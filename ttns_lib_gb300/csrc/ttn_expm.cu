@@ -676,8 +676,7 @@ __device__ void reduce_partials(const double2* part, int nq, double2* out, Red& 
   for (int q = w; q < nq; q += (int)(blockDim.x >> 5)) {
     double2 s = make_double2(0.0, 0.0);
     for (int b = lane; b < G; b += 32) s = cadd(s, part[(long long)b * nq + q]);
-    s.x = wsum(s.x);
-    s.y = wsum(s.y);
+    s = warp_sum2(s);
     if (lane == 0) out[q] = s;
   }
   __syncthreads();
@@ -1177,8 +1176,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
           s = cadd(s, cmulc(v1, p1));
         }
         if (i < n) s = cadd(s, cmulc(Vj[i], a.p[i]));
-        s.x = wsum(s.x);
-        s.y = wsum(s.y);
+        s = warp_sum2(s);
         if (lane == 0) sm.w[warp][0] = s;
         launch_sum(a, sm, 1, pa, red);
       }
@@ -1249,8 +1247,7 @@ __global__ void __launch_bounds__(ET, 2) k_expm_coop(ExpmArgs a_in) {
         if ((int)blockIdx.x <= j && warp == 0) {
           double2 t = make_double2(0.0, 0.0);
           for (int b = lane; b < (int)gridDim.x; b += 32) t = cadd(t, pb[(long long)b * (j + 1) + blockIdx.x]);
-          t.x = wsum(t.x);
-          t.y = wsum(t.y);
+          t = warp_sum2(t);
           if (lane == 0) rq[blockIdx.x] = t;
         }
         grid_barrier(a.bar, a.err);

@@ -46,11 +46,6 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-__device__ __forceinline__ double2 warp_sum2(double2 v) {
-  v.x = warp_sum(v.x);
-  v.y = warp_sum(v.y);
-  return v;
-}
 
 // =====================================================================================
 // complex FP64 GEMM

@@ -222,10 +222,11 @@ __device__ void col_partials(const RqrArgs& a, const Rows& R, int j, int jend, R
         acc = qfmac(acc, x, R.at(i, j + w));
       }
     }
+    if (w) {
+      acc = warp_sum2(acc);
+    } else {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-      if (w) acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      for (int o = 16; o > 0; o >>= 1) acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
     }
     if (lane == 0) {
       if (G == 1) {
@@ -313,10 +314,11 @@ __device__ void col_reduce(const RqrArgs& a, int j, int jend, RSmem<BN>& S) {
       s.y += scaled ? qldexp(yv[u], e - E) : yv[u];
     }
   }
+  if (w) {
+    s = warp_sum2(s);
+  } else {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
-    if (w) s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    for (int o = 16; o > 0; o >>= 1) s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
   }
   if (lane == 0) {
     if (w == 0) {
@@ -388,11 +390,9 @@ __device__ void panel_reduce(const RqrArgs& a, int nbp, int ncx, RSmem<BN>& S) {
       sx += pp[(size_t)q * 2 * qpw<BN>() + 2 * e];
       sy += pp[(size_t)q * 2 * qpw<BN>() + 2 * e + 1];
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      sx += __shfl_xor_sync(0xffffffffu, sx, o);
-      sy += __shfl_xor_sync(0xffffffffu, sy, o);
-    }
+    const double2 t = warp_sum2(make_double2(sx, sy));
+    sx = t.x;
+    sy = t.y;
     if (lane == 0) {
       pr[2 * e] = sx;
       pr[2 * e + 1] = sy;

@@ -7,6 +7,8 @@ results must equal the one-at-a-time results exactly, whatever the thread count.
 import numpy as np
 import pytest
 
+from helpers import generic_state
+from oracle.oracle import Oracle
 from ttns_lib_gb300 import api
 from ttns_lib_gb300 import spin_boson as sb
 
@@ -56,3 +58,32 @@ def test_batch_step_reports_the_failing_instance():
     other.init_product(psi0=[1.0, 0.0], seed=0)
     with pytest.raises(api.TTNError, match="instance 2"):
         api.batch_step([good[0][2], good[1][2], it], [good[0][1], good[1][1], other], -1j, threads=2)
+
+
+def test_batch_instances_match_the_oracle():
+    """Uneven instances stepped together by ttn_batch_step from generic states, each against
+    the oracle stepping the same instance: <sz> to 1e-10 after every step and the node
+    tensors to 1e-9 after three."""
+    rng = np.random.default_rng(9)
+    inst = []
+    for spec in SPECS[:4]:
+        m = sb.build(spec["N"], spec["alpha"], spec["wc"], spec["d"], spec["chi"], spec["eps"], spec["delta"],
+                     spec["beta"])
+        st = generic_state(m.topology, rng)
+        orc = Oracle(m.topology, m.sop, krylov_dim=10, krylov_tol=1e-12)
+        orc.set_state(st)
+        A = api.httensor(m.topology)
+        A.set(st)
+        it = api.fixed_step_projector_splitting_integrator(A, m.sop, krylov_dim=10, krylov_tolerance=1e-12)
+        it.dt = 0.05
+        inst.append((m, orc, A, it))
+    for k in range(3):
+        api.batch_step([it for _, _, _, it in inst], [A for _, _, A, _ in inst], -1j, threads=0)
+        for i, (m, orc, A, it) in enumerate(inst):
+            orc.step(0.05)
+            szo = orc.expect(0, sb.SZ).real
+            szd = it.mel()(sb.SZ, 0, A).real
+            assert abs(szo - szd) < 1e-10, (i, k, szo, szd)
+    for i, (m, orc, A, it) in enumerate(inst):
+        for a, b in zip(A.get(), orc.get_state()):
+            assert np.linalg.norm(a - b) <= 1e-9 * max(np.linalg.norm(b), 1e-300), i

@@ -128,8 +128,7 @@ int ttn_integrator_nh_applications(const ttn_integrator* it, long long* out);
  * builds the full krylov_dim space and controls the step size with Sidje's error estimate;
  * mode 1 ends the Lanczos recurrence as soon as beta_0 beta_{j+1} |e_j^T exp(c tau T) e_1|
  * for the whole remaining interval is below krylov_tol, which reproduces the reference's
- * H-application counts on its examples.  FP64 integrators only; the adjoint sweep takes
- * mode 0. */
+ * H-application counts on its examples.  Both precisions; the adjoint sweep takes mode 0. */
 int ttn_integrator_set_krylov_stop(ttn_integrator* it, int mode);
 /* one-site and two-site subspace expansions so far (Nonesite / Ntwosite,
  * include/ttns_lib/tdvp_core/subspace_expansion_projector_splitting_engine.hpp:513-514):
